@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 Euler solver: cell-stage updates per second.
+
+A "step" is one solver iteration (all RK stages of the explicit scheme) over
+the whole mesh; one cell-stage update is one RK stage applied to one cell, so
+value = ncell * stages * steps / time.
+
+Default workload: the large-mesh configuration -- NACA 0012 O-grid 2048 x 1024
+(4,194,304 triangles, seeded diagonals and 5% jitter), Morton-ordered cells,
+M 0.78, alpha 2.0 deg, FP32 stencil with FP64 geometry and residual norm,
+residual smoothing on (2 sweeps), the reference's 4-stage RK.  Its working set
+(~1 GB) is far larger than the 129 MB L2, so no L2 flush is needed between
+steps.
+
+Arms:
+  --impl gb300      (default) the CUDA path through the C ABI
+  --impl reference  the CPU path of the reference scheme (the oracle port of
+                    its GPU loop, OpenMP on all host cores) on the same
+                    workload, one iteration per step
+
+N > 1 (torchrun): replicas only -- the reference path has no domain
+decomposition; each rank solves its own copy, no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (ni, nj, mach, alpha, cfl, precision, ordering, description)
+    "large": dict(ni=2048, nj=1024, ma=0.78, alpha=2.0, cfl=2.0,
+                  desc="NACA0012 O-grid 2048x1024 (4194304 tri), Morton, M0.78 a2.0, FP32 stencil, "
+                       "IRS 2 sweeps eps 0.8, 4-stage RK"),
+    "transonic": dict(ni=512, nj=128, ma=0.80, alpha=1.25, cfl=2.0,
+                      desc="NACA0012 O-grid 512x128 (131072 tri), Morton, M0.80 a1.25, FP32 stencil, "
+                           "IRS 2 sweeps eps 0.8, 4-stage RK"),
+}
+
+PASS_NAMES = ["faces", "flux", "smooth", "update", "resid"]
+
+
+def bytes_per_cell(prec_bytes: int) -> dict:
+    """Algorithmic (compulsory) bytes per cell of each pass, from the arrays it
+    touches: every element read or written once per launch, neighbour gathers
+    perfectly reused.  T = stencil precision, int4 topology 16 B."""
+    T = prec_bytes
+    topo = 16
+    W, S2x3, R2x3, A, FS, dt, V4 = 4 * T, 6 * T, 6 * T, T, 12 * T, T, 4 * T
+    return {
+        "faces": W + topo + S2x3 + R2x3 + A + FS + dt,   # reads W,topo,S,R,area -> FS, dt
+        "flux": topo + S2x3 + FS + V4,                   # reads topo,S,FS -> res
+        "smooth": topo + V4 + V4 + V4,                   # reads topo,src,res -> dst
+        "update": topo + V4 + V4 + dt + A + V4 + V4,     # topo,src,res,dt,area,W0 -> W
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.gpu = gpu_index
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu_index}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax = max(smax, float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def make_params(e2d, wl, precision):
+    return e2d.default_params(ma=wl["ma"], alpha_deg=wl["alpha"], cfl=wl["cfl"], precision=precision,
+                              ordering=e2d.E2D_ORDER_MORTON, maxstep=1000000)
+
+
+def cpu_port_rate(wl, steps_wanted: float, threads: int | None = None, mesh=None):
+    """Oracle port of the reference loop on the host cores: returns
+    (cell-stage/s, iterations run, seconds, threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    import gpueularsolver2d_gb300 as e2d
+    if mesh is None:
+        mesh = e2d.Mesh.ogrid(wl["ni"], wl["nj"], seed=1)
+    x, y, tri = mesh.nodes()
+    p = pyoracle.params(ma=wl["ma"], alpha_deg=wl["alpha"], cfl=wl["cfl"])
+    case = pyoracle.Case(x, y, tri, p)
+    if threads:
+        pyoracle.set_threads(threads)
+    th = pyoracle.threads()
+    n = max(1, int(steps_wanted))
+    t0 = time.perf_counter()
+    k = len(case.run(n))
+    dt = time.perf_counter() - t0
+    return case.ncell * p.rk_stages * k / dt, k, dt, th
+
+
+def run_reference(args, rank: int, world: int):
+    """--impl reference: the reference scheme's CPU path on the host cores."""
+    if rank != 0:
+        return
+    wl = WORKLOADS[args.workload]
+    import gpueularsolver2d_gb300 as e2d
+    mesh = e2d.Mesh.ogrid(wl["ni"], wl["nj"], seed=1)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    x, y, tri = mesh.nodes()
+    p = pyoracle.params(ma=wl["ma"], alpha_deg=wl["alpha"], cfl=wl["cfl"])
+    case = pyoracle.Case(x, y, tri, p)
+    th = pyoracle.threads()
+    case.run(args.warmup)
+    t0 = time.perf_counter()
+    k = len(case.run(args.steps))
+    dt = time.perf_counter() - t0
+    rate = case.ncell * p.rk_stages * k / dt
+    line = {
+        "impl": "reference", "metric": "cell-stage updates/s", "value": rate, "unit": "cell-stage/s",
+        "n_gpus": world, "steps": k, "warmup": args.warmup, "ms_per_step": dt / k * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded NACA0012 O-grid)",
+        "config": {"workload": wl["desc"], "cells": case.ncell, "stages": p.rk_stages,
+                   "parallelism": f"replicas{world}"},
+        "cpu_baseline": {"value": rate, "unit": "cell-stage/s", "cores": th, "kind": "port",
+                         "sample": f"{k} iterations of the full {case.ncell}-cell workload"},
+        "e2e": {"value": rate, "unit": "cell-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank: int, world: int):
+    import numpy as np
+    import torch
+    import gpueularsolver2d_gb300 as e2d
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    wl = WORKLOADS[args.workload]
+    prec = e2d.E2D_FP64 if args.fp64 else e2d.E2D_FP32
+    mesh = e2d.Mesh.ogrid(wl["ni"], wl["nj"], seed=1)
+    params = make_params(e2d, wl, prec)
+    solver = e2d.Solver(mesh, params)
+    ncell, stages = solver.ncell, params.rk_stages
+    launches = solver.launches_per_iteration()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    solver.step(args.warmup)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    solver.step(args.steps)          # CUDA events on the solver's stream bracket the K steps
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    dev_ms = solver.last_device_ms()
+    barrier()
+    clocks = sampler.stop()
+    t_local = dev_ms / 1e3
+    if dist is not None:
+        t = torch.tensor([t_local], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    else:
+        t_max = t_local
+    value = world * ncell * stages * args.steps / t_max
+
+    # per-pass device time inside the same iteration sequence (events around every launch)
+    prof_iters = 3
+    ms, nl = solver.profile_passes(prof_iters)
+    tbytes = 8 if prec == e2d.E2D_FP64 else 4
+    bpc = bytes_per_cell(tbytes)
+    per_pass = {}
+    for k, name in enumerate(PASS_NAMES):
+        if nl[k] == 0:
+            continue
+        avg = ms[k] / nl[k]
+        entry = {"launches": int(nl[k]), "avg_ms": avg, "share": ms[k] / ms.sum()}
+        if name in bpc:
+            entry["algo_bytes_per_launch"] = bpc[name] * ncell
+            entry["achieved_gbs"] = bpc[name] * ncell / (avg / 1e3) / 1e9
+        per_pass[name] = entry
+    dom = max((n for n in per_pass if n in bpc), key=lambda n: per_pass[n]["avg_ms"] * per_pass[n]["launches"])
+    peak, peak_kind = measured_peak_hbm()
+    achieved = per_pass[dom]["achieved_gbs"]
+    stage_bytes = sum(bpc[n] * (args_sweeps_count(params) if n == "smooth" else 1) for n in bpc)
+    roofline = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
+                "traffic": traffic_from_profiles(dom, ncell),
+                "algo_bytes_per_cell_stage": stage_bytes,
+                "whole_step_frac": stage_bytes * ncell * stages * args.steps / t_local / 1e9 / peak}
+
+    # end to end through the C ABI with host buffers: every step uploads the
+    # state from pinned host memory, iterates once and reads the state back
+    pin_in = torch.empty((ncell, 4), dtype=torch.float64, pin_memory=True).numpy()
+    pin_out = torch.empty((ncell, 4), dtype=torch.float64, pin_memory=True).numpy()
+    pin_in[:] = solver.state()
+    e2e_steps = max(3, min(args.steps, 10))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        solver.set_state(pin_in)
+        solver.step(1)
+        solver.state_into(pin_out)
+    torch.cuda.synchronize()
+    e2e_t = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_t], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e_rate = world * ncell * stages * e2e_steps / e2e_t
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        del solver
+        torch.cuda.synchronize()
+        rate, k, dt, th = cpu_port_rate(wl, 2, mesh=mesh)
+        cpu = {"value": rate, "unit": "cell-stage/s", "cores": th, "kind": "port",
+               "sample": f"{k} iterations of the full {ncell}-cell workload on {th} threads ({dt:.1f} s)"}
+    if rank == 0:
+        line = {
+            "metric": "cell-stage updates/s", "value": value, "unit": "cell-stage/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == e2d.E2D_FP64 else "f32",
+            "data": "synthetic (seeded NACA0012 O-grid)",
+            "config": {"workload": wl["desc"], "cells": ncell, "stages": stages,
+                       "parallelism": f"replicas{world}",
+                       "l2": "inputs larger than L2 (working set > 1 GB), no flush"},
+            "wall_ms_per_step": wall / args.steps * 1e3,
+            "roofline": roofline, "passes": per_pass,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_rate, "unit": "cell-stage/s", "steps": e2e_steps,
+                    "h2d_bytes_per_step": int(pin_in.nbytes), "d2h_bytes_per_step": int(pin_out.nbytes)},
+            "gpu_launches": launches * args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def args_sweeps_count(params) -> int:
+    return max(0, params.irs_sweeps - 1)
+
+
+def traffic_from_profiles(kernel: str, ncell: int):
+    """DRAM bytes per launch from the committed ncu summary, scaled to ncell."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            t = json.load(f)
+        e = t[f"k_{kernel}"]
+        return e["dram_bytes_per_cell"] * ncell
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="large")
+    ap.add_argument("--fp64", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,205 @@
+"""Python view of the C ABI: ``Mesh`` and ``Solver`` handles over libeuler2d.
+
+The calls map one to one onto include/euler2d.h; numpy arrays cross the
+boundary as plain pointers.  Cell arrays are in file order.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._lib import (E2D_FP32, E2D_FP64, E2D_ORDER_FILE, E2D_ORDER_MORTON, MeshInfo, Params,
+                   check, load)
+
+__all__ = ["Mesh", "Solver", "Params", "default_params", "read_input", "E2D_FP32", "E2D_FP64",
+           "E2D_ORDER_FILE", "E2D_ORDER_MORTON"]
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+def default_params(**kw) -> Params:
+    """Reference defaults, with any field overridden by keyword."""
+    p = Params()
+    check(load().e2d_params_default(ctypes.byref(p)))
+    for k, v in kw.items():
+        if k == "rk_coef":
+            for i, c in enumerate(v):
+                p.rk_coef[i] = c
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def read_input(path: str, p: Params | None = None) -> Params:
+    p = p or default_params()
+    check(load().e2d_input_read(path.encode(), ctypes.byref(p)))
+    return p
+
+
+class Mesh:
+    def __init__(self, handle: int):
+        self._h = ctypes.c_void_p(handle)
+
+    @classmethod
+    def read(cls, path: str) -> "Mesh":
+        h = ctypes.c_void_p()
+        check(load().e2d_mesh_read(path.encode(), ctypes.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def from_arrays(cls, x, y, tri) -> "Mesh":
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.ascontiguousarray(y, np.float64)
+        tri = np.ascontiguousarray(tri, np.int32).reshape(-1)
+        h = ctypes.c_void_p()
+        check(load().e2d_mesh_from_arrays(len(x), len(tri) // 3, _dp(x), _dp(y), _ip(tri),
+                                          ctypes.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def ogrid(cls, ni: int, nj: int, r_far: float = 20.0, dy_wall: float = 2e-3,
+              jitter: float = 0.05, seed: int = 1) -> "Mesh":
+        h = ctypes.c_void_p()
+        check(load().e2d_mesh_ogrid_naca0012(ni, nj, r_far, dy_wall, jitter, seed, ctypes.byref(h)))
+        return cls(h.value)
+
+    def write(self, path: str) -> None:
+        check(load().e2d_mesh_write(path.encode(), self._h))
+
+    def info(self, wall_box: float = 2.0) -> MeshInfo:
+        i = MeshInfo()
+        check(load().e2d_mesh_info_get(self._h, wall_box, ctypes.byref(i)))
+        return i
+
+    def topology(self, wall_box: float = 2.0):
+        """(edge_int[nedge,7], edge_dbl[nedge,5], cell_int[ncell,7], cell_dbl[ncell,3])."""
+        inf = self.info(wall_box)
+        ei = np.zeros((inf.nedge, 7), np.int32)
+        ed = np.zeros((inf.nedge, 5))
+        ci = np.zeros((inf.ncell, 7), np.int32)
+        cd = np.zeros((inf.ncell, 3))
+        check(load().e2d_mesh_topology(self._h, wall_box, _ip(ei), _dp(ed), _ip(ci), _dp(cd)))
+        return ei, ed, ci, cd
+
+    def nodes(self):
+        inf = self.info()
+        x = np.zeros(inf.nnode)
+        y = np.zeros(inf.nnode)
+        tri = np.zeros((inf.ncell, 3), np.int32)
+        check(load().e2d_mesh_nodes(self._h, _dp(x), _dp(y), _ip(tri)))
+        return x, y, tri
+
+    def order(self, ordering: int) -> np.ndarray:
+        perm = np.zeros(self.info().ncell, np.int32)
+        check(load().e2d_mesh_order(self._h, ordering, _ip(perm)))
+        return perm
+
+    def close(self) -> None:
+        if self._h:
+            load().e2d_mesh_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Solver:
+    def __init__(self, mesh: Mesh, params: Params):
+        self.mesh = mesh
+        self.params = params
+        self.ncell = mesh.info(params.wall_box).ncell
+        h = ctypes.c_void_p()
+        check(load().e2d_solver_create(mesh._h, ctypes.byref(params), ctypes.byref(h)))
+        self._h = h
+
+    def step(self, n: int) -> None:
+        check(load().e2d_step(self._h, n))
+
+    def solve(self, max_steps: int, epsl: float) -> np.ndarray:
+        hist = np.zeros(max(1, max_steps))
+        n = ctypes.c_int32()
+        check(load().e2d_solve(self._h, max_steps, epsl, _dp(hist), ctypes.byref(n)))
+        return hist[: n.value].copy()
+
+    def progress(self):
+        st = ctypes.c_int32()
+        r = ctypes.c_double()
+        check(load().e2d_progress(self._h, ctypes.byref(st), ctypes.byref(r)))
+        return st.value, r.value
+
+    def history(self) -> np.ndarray:
+        n = ctypes.c_int32()
+        check(load().e2d_residual_history(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(max(1, n.value))
+        check(load().e2d_residual_history(self._h, _dp(out), n.value, ctypes.byref(n)))
+        return out[: n.value]
+
+    def set_residual_norm(self, epsm: float) -> None:
+        check(load().e2d_set_residual_norm(self._h, epsm))
+
+    def residual_norm(self) -> float:
+        v = ctypes.c_double()
+        check(load().e2d_get_residual_norm(self._h, ctypes.byref(v)))
+        return v.value
+
+    def state(self) -> np.ndarray:
+        w = np.zeros((self.ncell, 4))
+        check(load().e2d_get_state(self._h, _dp(w)))
+        return w
+
+    def state_into(self, out: np.ndarray) -> None:
+        """Copy the state into a caller buffer (e.g. pinned memory), [ncell, 4] float64."""
+        if out.dtype != np.float64 or not out.flags.c_contiguous or out.size != 4 * self.ncell:
+            raise ValueError("need a C-contiguous float64 [ncell, 4] buffer")
+        check(load().e2d_get_state(self._h, _dp(out)))
+
+    def set_state(self, w) -> None:
+        w = np.ascontiguousarray(w, np.float64).reshape(self.ncell, 4)
+        check(load().e2d_set_state(self._h, _dp(w)))
+
+    def forces(self):
+        cl = ctypes.c_double()
+        cd = ctypes.c_double()
+        check(load().e2d_forces(self._h, ctypes.byref(cl), ctypes.byref(cd)))
+        return cl.value, cd.value
+
+    def write_residual_plt(self, path: str) -> None:
+        check(load().e2d_write_residual_plt(self._h, path.encode()))
+
+    def last_device_ms(self) -> float:
+        v = ctypes.c_double()
+        check(load().e2d_last_device_ms(self._h, ctypes.byref(v)))
+        return v.value
+
+    def launches_per_iteration(self) -> int:
+        v = ctypes.c_int32()
+        check(load().e2d_launches_per_iteration(self._h, ctypes.byref(v)))
+        return v.value
+
+    def profile_passes(self, iters: int):
+        """Per-pass device ms summed over iters iterations, and launch counts."""
+        ms = np.zeros(5)
+        nl = np.zeros(5, np.int32)
+        check(load().e2d_profile_passes(self._h, iters, _dp(ms), _ip(nl)))
+        return ms, nl
+
+    def close(self) -> None:
+        if self._h:
+            load().e2d_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

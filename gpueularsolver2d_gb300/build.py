@@ -1,0 +1,84 @@
+"""Build ``libeuler2d.so`` (and the ``e2d_solve`` command) for sm_103a in-tree.
+
+nvcc cross-compiles without a GPU, so this runs on any machine with the CUDA
+13 toolkit.  Translation units are compiled in parallel; the FP64 kernels are
+compiled without FMA contraction so that they reproduce the CPU oracle bit for
+bit, the FP32 kernels with contraction and fast division / square root.
+Host code is compiled with ``-ffp-contract=off`` so the set-up geometry is the
+same IEEE arithmetic on x86-64 and aarch64.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+LIBDIR = os.path.join(PKG, "lib")
+OBJDIR = os.path.join(PKG, "_build")
+LIB = os.path.join(LIBDIR, "libeuler2d.so")
+CLI = os.path.join(LIBDIR, "e2d_solve")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_COMMON = [*ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+               "-Xcompiler", "-ffp-contract=off", f"-I{os.path.join(ROOT, 'include')}"]
+
+UNITS = {
+    "mesh.o": ("mesh.cpp", ["g++", "-O2", "-fPIC", "-std=c++17", "-ffp-contract=off",
+                            "-Wall", f"-I{os.path.join(ROOT, 'include')}"]),
+    "solver.o": ("solver.cu", ["nvcc", *NVCC_COMMON]),
+    "resid.o": ("resid.cu", ["nvcc", *NVCC_COMMON]),
+    "kernels_f64.o": ("kernels_f64.cu", ["nvcc", *NVCC_COMMON, "--fmad=false"]),
+    "kernels_f32.o": ("kernels_f32.cu", ["nvcc", *NVCC_COMMON, "--fmad=true",
+                                          "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
+}
+HEADERS = ["internal.h", "dev_types.h", "kernels.cuh"]
+
+
+def _stale(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _compile(obj: str, src: str, cmd: list[str], verbose_ptxas: bool) -> None:
+    extra = ["-Xptxas", "-v"] if verbose_ptxas and cmd[0] == "nvcc" else []
+    full = [*cmd, *extra, "-c", os.path.join(CSRC, src), "-o", os.path.join(OBJDIR, obj)]
+    res = subprocess.run(full, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(full)}\n{res.stdout}\n{res.stderr}")
+    if verbose_ptxas:
+        sys.stderr.write(res.stderr)
+
+
+def build(force: bool = False, verbose_ptxas: bool = False) -> str:
+    os.makedirs(LIBDIR, exist_ok=True)
+    os.makedirs(OBJDIR, exist_ok=True)
+    hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "euler2d.h"),
+                                                       __file__]
+    todo = []
+    for obj, (src, cmd) in UNITS.items():
+        deps = [os.path.join(CSRC, src), *hdrs]
+        if force or verbose_ptxas or _stale(os.path.join(OBJDIR, obj), deps):
+            todo.append((obj, src, cmd))
+    with ThreadPoolExecutor(max(1, len(todo))) as ex:
+        for f in [ex.submit(_compile, o, s, c, verbose_ptxas) for o, s, c in todo]:
+            f.result()
+    objs = [os.path.join(OBJDIR, o) for o in UNITS]
+    if force or todo or _stale(LIB, objs):
+        tmp = LIB + ".tmp"
+        subprocess.run(["nvcc", *ARCH, "-shared", "-o", tmp, *objs], check=True)
+        os.replace(tmp, LIB)
+    cli_src = os.path.join(CSRC, "e2d_solve_main.cpp")
+    if os.path.exists(cli_src) and (force or _stale(CLI, [cli_src, LIB])):
+        subprocess.run(["g++", "-O2", "-std=c++17", f"-I{os.path.join(ROOT, 'include')}", cli_src,
+                        "-o", CLI, f"-L{LIBDIR}", "-leuler2d", "-Wl,-rpath,$ORIGIN"], check=True)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose_ptxas="--ptxas" in sys.argv))

@@ -1,0 +1,84 @@
+// dev_types.h -- types shared by the host solver and the kernel translation
+// units, and the per-precision launch entry points.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace e2d {
+
+template <typename T> struct alignas(4 * sizeof(T)) V4 { T x, y, z, w; };
+template <typename T> struct alignas(2 * sizeof(T)) V2 { T x, y; };
+
+// Device-side iteration control, one per solver (or per batched case).
+struct Ctl {
+    int step;        // iterations completed
+    int halt;        // nonzero: every kernel returns at once (1 done, 2 diverged)
+    int target;      // halt when step reaches this
+    int check_epsl;  // halt when Resd <= epsl
+    int nbad;        // cells with rho <= 0, p <= 0 or NaN after the last iteration
+    int fixed_norm;  // epsm given by the caller
+    double epsl, epsm, resd;
+};
+
+// Flow constants of one case (gpu_init.cu:63-93).
+template <typename T> struct Flow {
+    T gamma, ui, vi, ain, tin, vin, R, pis, cfl, dt_cap, eps_entropy, irs_eps;
+};
+
+// Cell-local mesh data in internal order (n cells).
+//   topo[i] = {f0, f1, f2, clog}; face code f >= 0: (nb << 3) | (right << 2) | slot,
+//   -1 far field, -2 wall.  slot = face index of this edge in the neighbour;
+//   right = this cell is the edge's right cell in the reference numbering.
+//   S[k*n+i] = outward normal of face k in the cell's own node order,
+//              (vectory, vectorx) of gpu_init.cu:153-154, so |S| = face length.
+//   R[k*n+i] = face midpoint minus cell centroid.
+template <typename T> struct MeshDev {
+    int n;
+    const int4 *__restrict__ topo;
+    const V2<T> *__restrict__ S;
+    const V2<T> *__restrict__ R;
+    const T *__restrict__ area;
+};
+
+// Everything one iteration needs.
+template <typename T> struct Plan {
+    MeshDev<T> m;
+    Flow<T> f;
+    V4<T> *W[2];   // W[0] holds the iteration's start state and its result
+    V4<T> *FS;     // [3n] face-side states
+    T *dt;         // [n]
+    V4<T> *res;    // [n]
+    V4<T> *sm[2];  // [n] smoothing sweeps (ping-pong)
+    double *part;  // [blocks] FP64 partials of sum (rho - rho0)^2
+    Ctl *ctl;
+    double *hist;
+    int hist_cap;
+    int stages;
+    T rk[8];
+    int sweeps;
+    int block;
+};
+
+template <typename T> int launches_per_iteration(const Plan<T> &p) {
+    return p.stages * (3 + (p.sweeps > 1 ? p.sweeps - 1 : 0)) + 1;
+}
+
+// Enqueue one iteration (all RK stages + the residual) on a stream.
+// Instantiated for double in kernels_f64.cu and for float in kernels_f32.cu.
+template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s);
+
+// Same, with an event pair around every launch (per-pass timing).
+template <typename T> int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, int *kind);
+
+// FP64 file-order state <-> T internal-order state (perm[i] = file index).
+template <typename T>
+void enqueue_import(int n, const int *perm, const double *wfile, V4<T> *W, cudaStream_t s);
+template <typename T>
+void enqueue_export(int n, const int *perm, const V4<T> *W, double *wfile, cudaStream_t s);
+
+// Residual kernel launcher (resid.cu).
+void enqueue_resid(const double *part, int nparts, Ctl *ctl, double *hist, int hist_cap,
+                   cudaStream_t s);
+
+}  // namespace e2d

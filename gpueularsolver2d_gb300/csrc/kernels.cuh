@@ -1,0 +1,503 @@
+// kernels.cuh -- the solve-path kernels for sm_103a, templated on the stencil
+// precision T (double or float).
+//
+// One RK stage is four passes over the cells (a grid-wide dependency
+// separates each pair):
+//   A  k_faces : boundary ghosts + Green-Gauss gradient + neighbour min/max
+//                + per-face limited reconstruction of the cell's own side of
+//                its three faces + spectral radius sum -> local time step
+//   B  k_flux  : per cell, Roe flux of its three faces from the two face-side
+//                states, summed with the reference's signs and face order
+//   C  k_smooth: implicit residual smoothing sweep (all but the last sweep)
+//   D  k_update: last smoothing sweep + magnitude clamp + RK update, and on
+//                the last stage the (rho - rho0)^2 block partials
+// and k_resid folds the partials into Resd on the last stage.
+//
+// Every cell gathers its own faces, so nothing is accumulated with atomics
+// and the result does not depend on scheduling.  Interior fluxes are
+// evaluated by both cells of a face from identical inputs, so both see the
+// same value.  The arithmetic of each quantity follows the reference kernel
+// it replaces operation by operation (cited per function); compiled without
+// FMA contraction, the FP64 instantiation reproduces the CPU oracle bit for
+// bit.
+#pragma once
+
+#include "dev_types.h"
+
+namespace e2d {
+
+template <typename T> __device__ __forceinline__ T tabs(T v) { return fabs(v); }
+template <typename T> __device__ __forceinline__ T tsqrt(T v) { return sqrt(v); }
+template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return fmin(a, b); }
+template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return fmax(a, b); }
+
+template <typename T> __device__ __forceinline__ T comp(const V4<T> &v, int k) {
+    return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
+}
+
+// gpu_solver.cu:49-60 (kernel_CalculationPTA): pressure and sound speed
+template <typename T> __device__ __forceinline__ void pta(const V4<T> &w, T g, T &P, T &A) {
+    T U = w.y / w.x;
+    T V = w.z / w.x;
+    T E = w.w / w.x - T(0.5) * (U * U + V * V);
+    P = (g - T(1.0)) * w.x * E;
+    A = tsqrt(g * P / w.x);
+}
+
+// gpu_solver.cu:62-135 (kernel_Far_Boundary): far-field ghost state from the
+// interior state dw (with its P, A) and the face vector (vectorx, vectory).
+template <typename T>
+__device__ __noinline__ V4<T> far_ghost(const V4<T> dw, T P, T A, T vectorx, T vectory,
+                                        const Flow<T> f) {
+    const T g = f.gamma;
+    T nn = tsqrt(vectorx * vectorx + vectory * vectory);
+    T nx = vectory / nn;
+    T ny = vectorx / nn;
+    T UD = dw.y / dw.x;
+    T VD = dw.z / dw.x;
+    T Un = tabs(f.ui * nx + f.vi * ny);
+    T Uncell = UD * nx + VD * ny;
+    V4<T> w0 = dw;
+    if (Un / f.ain > T(1.0)) {
+        if (!(Uncell > T(0.0))) {
+            w0.x = T(1.0);
+            w0.y = f.ui;
+            w0.z = f.vi;
+            w0.w = f.R * f.tin / (f.vin * f.vin) / (g - T(1.0)) + T(0.50);
+        }
+    } else {
+        T PA = f.pis, PD = P, AD = A, ROUD = dw.x, PB, UB, VB;
+        if (Uncell > T(0.0)) {
+            PB = PA;
+            w0.x = ROUD + (PB - PD) / AD / AD;
+            UB = UD + nx * (PD - PB) / ROUD / AD;
+            VB = VD + ny * (PD - PB) / ROUD / AD;
+        } else {
+            PB = T(0.5) * (PA + PD - ROUD * AD * (nx * (f.ui - UD) + ny * (f.vi - VD)));
+            w0.x = T(1.0) + (PB - PA) / AD / AD;
+            UB = f.ui - nx * (PA - PB) / ROUD / AD;
+            VB = f.vi - ny * (PA - PB) / ROUD / AD;
+        }
+        w0.y = UB * w0.x;
+        w0.z = VB * w0.x;
+        w0.w = PB / (g - T(1.0)) + T(0.5) * (UB * UB + VB * VB) * w0.x;
+    }
+    return w0;
+}
+
+// gpu_solver.cu:188-221: slip-wall ghost (velocity mirrored in the face)
+template <typename T>
+__device__ __forceinline__ V4<T> wall_ghost(const V4<T> &dw, T vectorx, T vectory, T vectorn) {
+    T nij0 = vectory / vectorn;
+    T nij1 = vectorx / vectorn;
+    T UU = dw.y / dw.x;
+    T VV = dw.z / dw.x;
+    T UV = UU * nij0 + VV * nij1;
+    UU = UU - T(2) * UV * nij0;
+    VV = VV - T(2) * UV * nij1;
+    V4<T> o = dw;
+    o.y = dw.x * UU;
+    o.z = dw.x * VV;
+    return o;
+}
+
+// Ghost state across a boundary face code (-1 far, -2 wall).
+template <typename T>
+__device__ __forceinline__ V4<T> ghost(int code, const V4<T> &U, T Sx, T Sy, const Flow<T> &f) {
+    if (code == -1) {
+        T P, A;
+        pta(U, f.gamma, P, A);
+        return far_ghost(U, P, A, Sy, Sx, f);
+    }
+    T vn = tsqrt(Sy * Sy + Sx * Sx);
+    return wall_ghost(U, Sy, Sx, vn);
+}
+
+// gpu_solver.cu:385-454 (kernel_deltT): face spectral radius from the mean of
+// the two unreconstructed states.  Symmetric in (a, b) and in the sign of S.
+template <typename T>
+__device__ __forceinline__ T spectral_radius(const V4<T> &a, const V4<T> &b, T vectorx, T vectory,
+                                             T g) {
+    T rou = (a.x + b.x) * T(0.5);
+    T u = (a.y + b.y) / rou * T(0.5);
+    T v = (a.z + b.z) / rou * T(0.5);
+    T EE = (a.w + b.w) * T(0.5) / rou - (u * u + v * v) * T(0.5);
+    T VC = u * vectory + v * vectorx;
+    T p = rou * EE * (g - T(1.0));
+    T CS = tsqrt((g * p / rou) * (vectorx * vectorx + vectory * vectory));
+    return tabs(VC) + CS;
+}
+
+// gpu_solver.cu:552-566 (kernel_Calc_Function)
+template <typename T>
+__device__ __forceinline__ void calc_function(const V4<T> &w, T g, T &A, T &U, T &V, T &H, T &P) {
+    T temp = T(1.0) / w.x;
+    U = w.y * temp;
+    V = w.z * temp;
+    P = (g - T(1.0)) * w.x * (w.w * temp - T(0.5) * (U * U + V * V));
+    A = tsqrt(g * P * temp);
+    H = w.w * temp + P * temp;
+}
+
+// gpu_solver.cu:569-647 (kernel_ROE_SCHEME): Roe flux with Harten's entropy
+// fix of width eps through the unit normal (nx, ny).
+template <typename T>
+__device__ __forceinline__ V4<T> roe(const V4<T> &LW, const V4<T> &RW, T nx, T ny, T g, T epsilon) {
+    T A0, U0, V0, H0, P0, A1, U1, V1, H1, P1;
+    calc_function(LW, g, A0, U0, V0, H0, P0);
+    calc_function(RW, g, A1, U1, V1, H1, P1);
+    T M0 = (U0 * nx + V0 * ny);
+    T M1 = (U1 * nx + V1 * ny);
+    T DVC = M1 - M0;
+    T lrou = LW.x, rrou = RW.x;
+    T sl = tsqrt(lrou), sr = tsqrt(rrou);
+    T ROUB = sl * sr;
+    T UB = (U0 * sl + U1 * sr) / (sl + sr);
+    T VB = (V0 * sl + V1 * sr) / (sl + sr);
+    T HB = (H0 * sl + H1 * sr) / (sl + sr);
+    T QB = UB * UB + VB * VB;
+    T AB = tsqrt((g - T(1.0)) * (HB - QB / T(2.0)));
+    T VC = UB * nx + VB * ny;
+    T AD0, AD1, AD2;
+    if (tabs(VC - AB) < epsilon) AD0 = ((VC - AB) * (VC - AB) + epsilon * epsilon) / (T(2) * epsilon);
+    else AD0 = tabs(VC - AB);
+    if (tabs(VC) < epsilon) AD1 = (VC * VC + epsilon * epsilon) / (T(2) * epsilon);
+    else AD1 = tabs(VC);
+    if (tabs(VC + AB) < epsilon) AD2 = ((VC + AB) * (VC + AB) + epsilon * epsilon) / (T(2) * epsilon);
+    else AD2 = tabs(VC + AB);
+    T dP = P1 - P0;
+    T F00 = AD0 * (dP - ROUB * AB * DVC) / (T(2.0) * AB * AB);
+    T F01 = F00 * (UB - AB * nx);
+    T F02 = F00 * (VB - AB * ny);
+    T F03 = F00 * (HB - AB * VC);
+    T F10 = AD1 * ((rrou - lrou) - dP / (AB * AB));
+    T F11 = F10 * UB + AD1 * ROUB * (U1 - U0 - DVC * nx);
+    T F12 = F10 * VB + AD1 * ROUB * (V1 - V0 - DVC * ny);
+    T F13 = F10 * QB * T(0.5) + AD1 * ROUB * (UB * (U1 - U0) + VB * (V1 - V0) - DVC * VC);
+    T F20 = AD2 * (dP + ROUB * AB * DVC) / (T(2.0) * AB * AB);
+    T F21 = F20 * (UB + AB * nx);
+    T F22 = F20 * (VB + AB * ny);
+    T F23 = F20 * (HB + AB * VC);
+    T WL0 = lrou * M0;
+    T WL1 = U0 * WL0 + nx * P0;
+    T WL2 = V0 * WL0 + ny * P0;
+    T WL3 = WL0 * H0;
+    T WR0 = rrou * M1;
+    T WR1 = U1 * WR0 + nx * P1;
+    T WR2 = V1 * WR0 + ny * P1;
+    T WR3 = WR0 * H1;
+    V4<T> F;
+    F.x = T(0.5) * ((WL0 + WR0) - (F00 + F10 + F20));
+    F.y = T(0.5) * ((WL1 + WR1) - (F01 + F11 + F21));
+    F.z = T(0.5) * ((WL2 + WR2) - (F02 + F12 + F22));
+    F.w = T(0.5) * ((WL3 + WR3) - (F03 + F13 + F23));
+    return F;
+}
+
+// ---------------------------------------------------------------------------
+// Pass A: gpu_solver.cu:137-223 (kernel_Boundary), 225-383 (kernel_Gradient),
+// 385-454 (kernel_deltT), 456-549 (kernel_Limiter / kernel_LBJinterpolate),
+// and the dt part of 768-878 (kernel_Flux_e2c).
+// FS[k*n+i] receives the state on the cell's own side of face k: the limited
+// reconstruction for an interior face, the cell state itself for a boundary
+// face (the reference's boundary faces are first order).
+template <typename T>
+__global__ void __launch_bounds__(256) k_faces(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ W,
+                                               V4<T> *__restrict__ FS, T *__restrict__ dt,
+                                               const Ctl *__restrict__ ctl) {
+    if (ctl->halt) return;
+    const int n = m.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int4 tp = m.topo[i];
+    const int code[3] = {tp.x, tp.y, tp.z};
+    const V4<T> U = W[i];
+    V2<T> S[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) S[k] = m.S[k * n + i];
+    V4<T> nbv[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        nbv[k] = code[k] >= 0 ? W[code[k] >> 3] : ghost(code[k], U, S[k].x, S[k].y, f);
+    T g0[4] = {T(0.0), T(0.0), T(0.0), T(0.0)}, g1[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};
+    T jmax[4], jmin[4];
+    T Tsum = T(0);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            T c = comp(nbv[k], q);
+            if (k == 0) { jmax[q] = c; jmin[q] = c; }
+            else {
+                if (c < jmin[q]) jmin[q] = c;
+                if (c > jmax[q]) jmax[q] = c;
+            }
+            T u = comp(U, q);
+            g0[q] += T(0.5) * (u + c) * S[k].x;
+            g1[q] += T(0.5) * (u + c) * S[k].y;
+        }
+        Tsum += spectral_radius(U, nbv[k], S[k].y, S[k].x, f.gamma);
+    }
+    const T A = m.area[i];
+    const T rA = T(1.0) / A;
+    T gx[4], gy[4], umax[4], umin[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        gx[q] = g0[q] * rA;
+        gy[q] = g1[q] * rA;
+        umax[q] = tmax(comp(U, q), jmax[q]);
+        umin[q] = tmin(comp(U, q), jmin[q]);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        V4<T> o = U;
+        if (code[k] >= 0) {
+            const V2<T> r = m.R[k * n + i];
+            T fi = T(1.0), d[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                T delt2 = gx[q] * r.x + gy[q] * r.y;
+                T u = comp(U, q);
+                if (delt2 > T(0)) fi = tmin((umax[q] - u) / delt2, T(1.0));
+                if (delt2 < T(0)) fi = tmin((umin[q] - u) / delt2, T(1.0));
+                if (delt2 == T(0)) fi = T(1.0);
+                delt2 *= fi;
+                d[q] = u + delt2;
+            }
+            o.x = d[0]; o.y = d[1]; o.z = d[2]; o.w = d[3];
+        }
+        FS[k * n + i] = o;
+    }
+    dt[i] = tmin(A * f.cfl / Tsum, f.dt_cap);
+}
+
+// ---------------------------------------------------------------------------
+// Pass B: gpu_solver.cu:651-764 (kernel_Flux2) evaluated per cell for its
+// three faces, summed as gpu_solver.cu:798-825 (+F where the cell is the
+// edge's left cell, -F where it is the right cell, in face order).
+template <typename T>
+__global__ void __launch_bounds__(256) k_flux(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ FS,
+                                              V4<T> *__restrict__ res, const Ctl *__restrict__ ctl) {
+    if (ctl->halt) return;
+    const int n = m.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int4 tp = m.topo[i];
+    const int code[3] = {tp.x, tp.y, tp.z};
+    V4<T> r;
+    r.x = T(0.0); r.y = T(0.0); r.z = T(0.0); r.w = T(0.0);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const V2<T> S = m.S[k * n + i];
+        const V4<T> own = FS[k * n + i];
+        const T vn = tsqrt(S.y * S.y + S.x * S.x);
+        T nx = S.x / vn, ny = S.y / vn;
+        V4<T> F;
+        bool right = false;
+        if (code[k] >= 0) {
+            const int c = code[k];
+            const V4<T> oth = FS[(c & 3) * n + (c >> 3)];
+            right = (c >> 2) & 1;
+            F = right ? roe(oth, own, -nx, -ny, f.gamma, f.eps_entropy)
+                      : roe(own, oth, nx, ny, f.gamma, f.eps_entropy);
+        } else {
+            const V4<T> gst = ghost(code[k], own, S.x, S.y, f);
+            F = roe(own, gst, nx, ny, f.gamma, f.eps_entropy);
+        }
+        F.x *= vn; F.y *= vn; F.z *= vn; F.w *= vn;
+        if (right) { r.x -= F.x; r.y -= F.y; r.z -= F.z; r.w -= F.w; }
+        else { r.x += F.x; r.y += F.y; r.z += F.z; r.w += F.w; }
+    }
+    res[i] = r;
+}
+
+// Sum of the interior neighbours' values in face order (gpu_solver.cu:1658-1666)
+template <typename T>
+__device__ __forceinline__ V4<T> nb_sum(const int4 tp, const V4<T> *__restrict__ src) {
+    V4<T> d;
+    d.x = T(0.0); d.y = T(0.0); d.z = T(0.0); d.w = T(0.0);
+    const int code[3] = {tp.x, tp.y, tp.z};
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        if (code[k] >= 0) {
+            const V4<T> v = src[code[k] >> 3];
+            d.x += v.x; d.y += v.y; d.z += v.z; d.w += v.w;
+        }
+    return d;
+}
+
+// ---------------------------------------------------------------------------
+// Pass C: gpu_solver.cu:1635-1673 (kernel_Smooth1): one Jacobi-type sweep
+// dst = (eps * sum_interior src + res) / (1 + eps * CLog).
+template <typename T>
+__global__ void __launch_bounds__(256) k_smooth(MeshDev<T> m, T eps, const V4<T> *__restrict__ src,
+                                                const V4<T> *__restrict__ res, V4<T> *__restrict__ dst,
+                                                const Ctl *__restrict__ ctl) {
+    if (ctl->halt) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.n) return;
+    const int4 tp = m.topo[i];
+    const V4<T> d = nb_sum(tp, src);
+    const V4<T> r0 = res[i];
+    const T den = T(1.0) + (eps) * T(tp.w);
+    V4<T> o;
+    o.x = (d.x * (eps) + r0.x) / den;
+    o.y = (d.y * (eps) + r0.y) / den;
+    o.z = (d.z * (eps) + r0.z) / den;
+    o.w = (d.w * (eps) + r0.w) / den;
+    dst[i] = o;
+}
+
+// ---------------------------------------------------------------------------
+// Pass D: gpu_solver.cu:1675-1720 (kernel_Smooth2, last sweep + clamp) fused
+// with 938-966 (kernel_RKStep); on the last stage also 968-1020 (kernel_drou)
+// as FP64 block partials and a count of unphysical cells.
+template <typename T>
+__global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, int smooth,
+                                                const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
+                                                const T *__restrict__ dt, const V4<T> *W0, V4<T> *Wout,
+                                                double *__restrict__ part, Ctl *ctl) {
+    if (ctl->halt) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double d2 = 0.0;
+    int bad = 0;
+    if (i < m.n) {
+        const int4 tp = m.topo[i];
+        V4<T> r = res[i];
+        if (smooth) {
+            const V4<T> d = nb_sum(tp, src);
+            const T eps = f.irs_eps;
+            const T den = T(1.0) + (eps) * T(tp.w);
+            T s0 = (d.x * (eps) + r.x) / den, s1 = (d.y * (eps) + r.y) / den;
+            T s2 = (d.z * (eps) + r.z) / den, s3 = (d.w * (eps) + r.w) / den;
+            if (tabs(r.x) > tabs(s0)) r.x = s0;
+            if (tabs(r.y) > tabs(s1)) r.y = s1;
+            if (tabs(r.z) > tabs(s2)) r.z = s2;
+            if (tabs(r.w) > tabs(s3)) r.w = s3;
+        }
+        T RK = rk;
+        RK *= dt[i];
+        const T A = m.area[i];
+        const V4<T> w0 = W0[i];
+        V4<T> w;
+        w.x = w0.x - RK * r.x / A;
+        w.y = w0.y - RK * r.y / A;
+        w.z = w0.z - RK * r.z / A;
+        w.w = w0.w - RK * r.w / A;
+        Wout[i] = w;
+        if (part) {
+            double dd = (double)w.x - (double)w0.x;
+            d2 = dd * dd;
+            double q = 0.5 * ((double)w.y * (double)w.y + (double)w.z * (double)w.z) / (double)w.x;
+            bad = !(w.x > T(0)) || !((double)w.w - q > 0.0);
+        }
+    }
+    if (!part) return;
+    // deterministic block reduction: fixed shuffle tree, then warps in order
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d2 += __shfl_down_sync(0xffffffffu, d2, o);
+    unsigned badmask = __ballot_sync(0xffffffffu, bad);
+    __shared__ double ws[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        ws[wid] = d2;
+        if (badmask) atomicAdd(&ctl->nbad, __popc(badmask));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += ws[k];
+        part[blockIdx.x] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// State exchange with the caller: FP64 in file order <-> T in internal order.
+template <typename T>
+__global__ void k_import(int n, const int *__restrict__ perm, const double *__restrict__ wfile,
+                         V4<T> *__restrict__ W) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *s = wfile + 4 * (size_t)perm[i];
+    V4<T> o;
+    o.x = (T)s[0]; o.y = (T)s[1]; o.z = (T)s[2]; o.w = (T)s[3];
+    W[i] = o;
+}
+
+template <typename T>
+__global__ void k_export(int n, const int *__restrict__ perm, const V4<T> *__restrict__ W,
+                         double *__restrict__ wfile) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const V4<T> v = W[i];
+    double *d = wfile + 4 * (size_t)perm[i];
+    d[0] = (double)v.x; d[1] = (double)v.y; d[2] = (double)v.z; d[3] = (double)v.w;
+}
+
+template <typename T>
+void enqueue_import(int n, const int *perm, const double *wfile, V4<T> *W, cudaStream_t s) {
+    k_import<T><<<(n + 255) / 256, 256, 0, s>>>(n, perm, wfile, W);
+}
+
+template <typename T>
+void enqueue_export(int n, const int *perm, const V4<T> *W, double *wfile, cudaStream_t s) {
+    k_export<T><<<(n + 255) / 256, 256, 0, s>>>(n, perm, W, wfile);
+}
+
+// ---------------------------------------------------------------------------
+// One iteration: gpu_solver.cu:2200-2434 without the W -> W0 copies.  W[0]
+// holds the start state; stage 0 reads it and writes W[1], middle stages
+// update W[1] in place, and the last stage writes the result back into W[0]
+// (each cell reads its own W0 before overwriting it), so W[0] is also the
+// next iteration's W0.
+template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
+    const int n = p.m.n, B = p.block, G = (n + B - 1) / B;
+    for (int st = 0; st < p.stages; st++) {
+        const bool last = st == p.stages - 1;
+        V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
+        V4<T> *Wout = last ? p.W[0] : p.W[1];
+        k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl);
+        k_flux<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
+        const V4<T> *src = p.res;
+        for (int sw = 0; sw + 1 < p.sweeps; sw++) {
+            V4<T> *dst = p.sm[sw & 1];
+            k_smooth<T><<<G, B, 0, s>>>(p.m, p.f.irs_eps, src, p.res, dst, p.ctl);
+            src = dst;
+        }
+        k_update<T><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
+                                    p.W[0], Wout, last ? p.part : nullptr, p.ctl);
+    }
+    enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, s);
+}
+
+// Same launches as enqueue_iteration, with events recorded around each one.
+// ev[2*j], ev[2*j+1] bracket launch j; kind[j] is 0 faces, 1 flux, 2 smooth,
+// 3 update, 4 resid.  Returns the number of launches.
+template <typename T>
+int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, int *kind) {
+    const int n = p.m.n, B = p.block, G = (n + B - 1) / B;
+    int j = 0;
+    auto mark = [&](int k) { kind[j] = k; cudaEventRecord(ev[2 * j], s); };
+    auto done = [&]() { cudaEventRecord(ev[2 * j + 1], s); j++; };
+    for (int st = 0; st < p.stages; st++) {
+        const bool last = st == p.stages - 1;
+        V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
+        V4<T> *Wout = last ? p.W[0] : p.W[1];
+        mark(0); k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl); done();
+        mark(1); k_flux<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl); done();
+        const V4<T> *src = p.res;
+        for (int sw = 0; sw + 1 < p.sweeps; sw++) {
+            V4<T> *dst = p.sm[sw & 1];
+            mark(2); k_smooth<T><<<G, B, 0, s>>>(p.m, p.f.irs_eps, src, p.res, dst, p.ctl); done();
+            src = dst;
+        }
+        mark(3);
+        k_update<T><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
+                                    p.W[0], Wout, last ? p.part : nullptr, p.ctl);
+        done();
+    }
+    mark(4); enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, s); done();
+    return j;
+}
+
+}  // namespace e2d

@@ -1,0 +1,41 @@
+// resid.cu -- residual of one iteration (gpu_solver.cu:2404-2433).
+#include "dev_types.h"
+
+namespace e2d {
+
+// drou = sum of the per-block partials in a fixed order, then
+// Resd = sqrt((drou + 1e-32) / EPSM) with EPSM = drou of iteration 1 unless
+// the caller fixed it.  Sets halt when the loop condition of
+// gpu_solver.cu:2200 (step < MAXSTEP && Resd > EPSL) fails or the state went
+// unphysical.  One block of 256 threads.
+__global__ void __launch_bounds__(256) k_resid(const double *__restrict__ part, int nparts, Ctl *ctl,
+                                               double *hist, int hist_cap) {
+    if (ctl->halt) return;
+    __shared__ double sh[256];
+    double s = 0.0;
+    for (int k = threadIdx.x; k < nparts; k += 256) s += part[k];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    const double drou = sh[0];
+    const int step = ctl->step + 1;
+    if (step == 1 && !ctl->fixed_norm) ctl->epsm = drou;
+    const double resd = sqrt((drou + 1.0E-32) / ctl->epsm);
+    if (step - 1 < hist_cap) hist[step - 1] = resd;
+    ctl->step = step;
+    ctl->resd = resd;
+    if (ctl->nbad) ctl->halt = 2;
+    else if (ctl->check_epsl && !(resd > ctl->epsl)) ctl->halt = 1;
+    else if (step >= ctl->target) ctl->halt = 1;
+}
+
+void enqueue_resid(const double *part, int nparts, Ctl *ctl, double *hist, int hist_cap,
+                   cudaStream_t s) {
+    k_resid<<<1, 256, 0, s>>>(part, nparts, ctl, hist, hist_cap);
+}
+
+}  // namespace e2d

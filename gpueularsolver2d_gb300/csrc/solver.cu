@@ -1,0 +1,554 @@
+// solver.cu -- the single-case solver behind the C ABI: set-up of the
+// cell-local device layout, device arena, CUDA-graph iteration batches and
+// the solve / state / residual-history entry points.
+//
+// Replaces ROE_SOLVER (gpu_solver.cu:2171-2473) and the memory helpers it
+// calls (cpuMalloc / gpuMalloc / struct2Array / copyH2D / copyD2H,
+// gpu_solver.cu:1505-1630, 1908-2169).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "dev_types.h"
+#include "internal.h"
+
+using namespace e2d;
+
+#define CK(call)                                                                       \
+    do {                                                                               \
+        cudaError_t err_ = (call);                                                     \
+        if (err_ != cudaSuccess) {                                                     \
+            set_error(std::string("CUDA: ") + #call + ": " + cudaGetErrorString(err_)); \
+            return E2D_ERR_CUDA;                                                       \
+        }                                                                              \
+    } while (0)
+
+namespace e2d {
+
+// gpu_fvm.cu:8-9
+static const double kR = 287.06;
+static const double kPi = 3.14159265358979;
+
+// Free-stream constants exactly as Initialization computes them
+// (gpu_init.cu:63-93), including PIS = P of the free-stream cell state.
+struct FreeStream {
+    double alpha, ain, vin, ui, vi, rho_e, pis;
+};
+
+FreeStream free_stream(const e2d_params &p) {
+    FreeStream s;
+    const double g = p.gamma;
+    s.alpha = p.alpha_deg * kPi / 180.0;
+    s.ain = std::sqrt(g * kR * p.tin);
+    s.vin = p.ma * s.ain;
+    s.ui = std::cos(s.alpha);
+    s.vi = std::sin(s.alpha);
+    s.rho_e = kR * p.tin / (s.vin * s.vin) / (g - 1.0) + 0.50;
+    // CalculationPTA of (1, cos a, sin a, rho_e)
+    double d = 1.0, du = std::cos(s.alpha), dv = std::sin(s.alpha), de = s.rho_e;
+    double U = du / d, V = dv / d;
+    double E = de / d - 0.5 * (U * U + V * V);
+    s.pis = (g - 1.0) * d * E;
+    return s;
+}
+
+// Cell-local layout in FP64, internal order.
+struct HostLayout {
+    int n = 0;
+    std::vector<int> perm, iperm;        // internal -> file, file -> internal
+    std::vector<int32_t> topo;           // [4n]
+    std::vector<double> S, R;            // [3n*2] each
+    std::vector<double> area;            // [n]
+    std::vector<int> wall_cell, wall_k;  // internal cell and face of every wall face
+};
+
+int build_layout(e2d_mesh *m, const e2d_params &p, HostLayout &L) {
+    int rc = build_topology(m, p.wall_box);
+    if (rc) return rc;
+    const MeshTopo &t = m->topo;
+    const int n = m->ncell;
+    if ((int64_t)n >= (1 << 28)) { set_error("mesh too large (limit 2^28 cells)"); return E2D_ERR_CAPACITY; }
+    L.n = n;
+    cell_order(m, p.ordering, L.perm);
+    L.iperm.assign(n, 0);
+    for (int i = 0; i < n; i++) L.iperm[L.perm[i]] = i;
+    L.topo.assign(4 * (size_t)n, 0);
+    L.S.assign(6 * (size_t)n, 0.0);
+    L.R.assign(6 * (size_t)n, 0.0);
+    L.area.assign(n, 0.0);
+    const double *X = m->x.data() - 1, *Y = m->y.data() - 1;
+    for (int i = 0; i < n; i++) {
+        const int c = L.perm[i];
+        for (int k = 0; k < 3; k++) {
+            const int cf = 3 * c + k;
+            const int nb = t.nb[cf];
+            L.topo[4 * (size_t)i + k] = nb >= 0 ? (L.iperm[nb] << 3) | (t.is_right[cf] << 2) | t.nb_slot[cf] : nb;
+            if (nb == -2) { L.wall_cell.push_back(i); L.wall_k.push_back(k); }
+            const int N1 = m->tri[3 * (size_t)c + (k + 1) % 3], N2 = m->tri[3 * (size_t)c + (k + 2) % 3];
+            const double vectorx = X[N1] - X[N2], vectory = Y[N2] - Y[N1];
+            L.S[2 * ((size_t)k * n + i)] = vectory;
+            L.S[2 * ((size_t)k * n + i) + 1] = vectorx;
+            const int e = t.celledge[cf] - 1;
+            L.R[2 * ((size_t)k * n + i)] = t.emx[e] - t.cx[c];
+            L.R[2 * ((size_t)k * n + i) + 1] = t.emy[e] - t.cy[c];
+        }
+        L.topo[4 * (size_t)i + 3] = t.clog[c];
+        L.area[i] = t.area[c];
+    }
+    return E2D_OK;
+}
+
+// Device arena: one cudaMalloc carved into 256-byte aligned pieces.
+struct Arena {
+    char *base = nullptr;
+    size_t cap = 0, used = 0;
+    ~Arena() { if (base) cudaFree(base); }
+    static size_t up(size_t b) { return (b + 255) & ~(size_t)255; }
+    void *take(size_t b) { void *p = base + used; used += up(b); return p; }
+};
+
+struct SolverBase {
+    virtual ~SolverBase() {}
+    virtual int upload_state(const double *w_file) = 0;
+    virtual int download_state(double *w_file) = 0;
+    virtual int enqueue(cudaStream_t s) = 0;
+    virtual int launches() const = 0;
+    virtual int nblocks() const = 0;
+    virtual int enqueue_timed(cudaStream_t s, cudaEvent_t *ev, int *kind) = 0;
+};
+
+template <typename T> struct SolverT : SolverBase {
+    HostLayout *L;
+    Arena arena;
+    Plan<T> plan;
+    int *perm_dev = nullptr;       // [n] internal -> file
+    double *wfile_dev = nullptr;   // [4n] FP64 state in file order (exchange buffer)
+    cudaStream_t *stream = nullptr;
+
+    explicit SolverT(HostLayout *l) : L(l) {}
+
+    int init(const e2d_params &p, const FreeStream &fs, Ctl *ctl, int block) {
+        const int n = L->n;
+        const int G = (n + block - 1) / block;
+        size_t bytes = Arena::up(sizeof(int4) * n) + 2 * Arena::up(sizeof(V2<T>) * 3 * n) +
+                       Arena::up(sizeof(T) * n) * 2 + Arena::up(sizeof(V4<T>) * n) * 5 +
+                       Arena::up(sizeof(V4<T>) * 3 * n) + Arena::up(sizeof(double) * G) +
+                       Arena::up(sizeof(int) * n) + Arena::up(sizeof(double) * 4 * n);
+        CK(cudaMalloc((void **)&arena.base, bytes));
+        arena.cap = bytes;
+        int4 *topo = (int4 *)arena.take(sizeof(int4) * n);
+        V2<T> *S = (V2<T> *)arena.take(sizeof(V2<T>) * 3 * n);
+        V2<T> *R = (V2<T> *)arena.take(sizeof(V2<T>) * 3 * n);
+        T *area = (T *)arena.take(sizeof(T) * n);
+        plan.W[0] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
+        plan.W[1] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
+        plan.FS = (V4<T> *)arena.take(sizeof(V4<T>) * 3 * n);
+        plan.dt = (T *)arena.take(sizeof(T) * n);
+        plan.res = (V4<T> *)arena.take(sizeof(V4<T>) * n);
+        plan.sm[0] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
+        plan.sm[1] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
+        plan.part = (double *)arena.take(sizeof(double) * G);
+        perm_dev = (int *)arena.take(sizeof(int) * n);
+        wfile_dev = (double *)arena.take(sizeof(double) * 4 * n);
+        CK(cudaMemcpy(perm_dev, L->perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(topo, L->topo.data(), sizeof(int4) * n, cudaMemcpyHostToDevice));
+        std::vector<T> tmp(6 * (size_t)n);
+        for (size_t k = 0; k < tmp.size(); k++) tmp[k] = (T)L->S[k];
+        CK(cudaMemcpy(S, tmp.data(), sizeof(T) * tmp.size(), cudaMemcpyHostToDevice));
+        for (size_t k = 0; k < tmp.size(); k++) tmp[k] = (T)L->R[k];
+        CK(cudaMemcpy(R, tmp.data(), sizeof(T) * tmp.size(), cudaMemcpyHostToDevice));
+        for (int k = 0; k < n; k++) tmp[k] = (T)L->area[k];
+        CK(cudaMemcpy(area, tmp.data(), sizeof(T) * n, cudaMemcpyHostToDevice));
+        CK(cudaMemset(plan.W[1], 0, sizeof(V4<T>) * n));
+        CK(cudaMemset(plan.part, 0, sizeof(double) * G));
+        plan.m = MeshDev<T>{n, topo, S, R, area};
+        Flow<T> &f = plan.f;
+        f.gamma = (T)p.gamma; f.ui = (T)fs.ui; f.vi = (T)fs.vi; f.ain = (T)fs.ain; f.tin = (T)p.tin;
+        f.vin = (T)fs.vin; f.R = (T)kR; f.pis = (T)fs.pis; f.cfl = (T)p.cfl; f.dt_cap = (T)p.dt_cap;
+        f.eps_entropy = (T)p.entropy_eps; f.irs_eps = (T)p.irs_eps;
+        plan.ctl = ctl;
+        plan.hist = nullptr;
+        plan.hist_cap = 0;
+        plan.stages = p.rk_stages;
+        for (int k = 0; k < 8; k++) plan.rk[k] = (T)p.rk_coef[k];
+        plan.sweeps = p.irs_sweeps;
+        plan.block = block;
+        return E2D_OK;
+    }
+
+    // Caller's FP64 file-order buffer -> device (one copy; from pinned memory
+    // it runs at full PCIe/C2C speed), then a permute-and-convert kernel.
+    int upload_state(const double *w) override {
+        const int n = L->n;
+        CK(cudaMemcpyAsync(wfile_dev, w, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, *stream));
+        enqueue_import<T>(n, perm_dev, wfile_dev, plan.W[0], *stream);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(*stream));
+        return E2D_OK;
+    }
+
+    int download_state(double *w) override {
+        const int n = L->n;
+        enqueue_export<T>(n, perm_dev, plan.W[0], wfile_dev, *stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(w, wfile_dev, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, *stream));
+        CK(cudaStreamSynchronize(*stream));
+        return E2D_OK;
+    }
+
+    int enqueue_timed(cudaStream_t s, cudaEvent_t *ev, int *kind) override {
+        return enqueue_iteration_timed<T>(plan, s, ev, kind);
+    }
+
+    int enqueue(cudaStream_t s) override {
+        enqueue_iteration<T>(plan, s);
+        CK(cudaGetLastError());
+        return E2D_OK;
+    }
+
+    int launches() const override { return launches_per_iteration(plan); }
+    int nblocks() const override { return (L->n + plan.block - 1) / plan.block; }
+};
+
+}  // namespace e2d
+
+struct e2d_solver {
+    e2d_params prm;
+    HostLayout L;
+    FreeStream fs;
+    std::unique_ptr<SolverBase> impl;
+    Ctl *ctl_dev = nullptr;
+    Ctl *ctl_host = nullptr;  // pinned mirror
+    double *hist_dev = nullptr;
+    int hist_cap = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaGraphExec_t gexec = nullptr;
+    int graph_iters = 8;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_ms = 0.0;
+    std::vector<double> hist;  // host copy of Resd[1..step]
+
+    ~e2d_solver() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+        if (ctl_dev) cudaFree(ctl_dev);
+        if (ctl_host) cudaFreeHost(ctl_host);
+        if (hist_dev) cudaFree(hist_dev);
+    }
+};
+
+namespace {
+
+int push_ctl(e2d_solver *s) {
+    CK(cudaMemcpyAsync(s->ctl_dev, s->ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, s->stream));
+    return E2D_OK;
+}
+
+int pull_ctl(e2d_solver *s) {
+    CK(cudaMemcpyAsync(s->ctl_host, s->ctl_dev, sizeof(Ctl), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return E2D_OK;
+}
+
+// The history buffer lives behind a pointer captured in the graph, so it is
+// sized once per growth and the graph is rebuilt when it moves.
+int ensure_hist(e2d_solver *s, int need) {
+    if (need <= s->hist_cap) return E2D_OK;
+    int cap = std::max(need, std::max(1024, 2 * s->hist_cap));
+    double *nh = nullptr;
+    CK(cudaMalloc((void **)&nh, sizeof(double) * cap));
+    if (s->hist_dev) {
+        CK(cudaMemcpyAsync(nh, s->hist_dev, sizeof(double) * s->hist_cap, cudaMemcpyDeviceToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        cudaFree(s->hist_dev);
+    }
+    s->hist_dev = nh;
+    s->hist_cap = cap;
+    if (s->gexec) { cudaGraphExecDestroy(s->gexec); s->gexec = nullptr; }
+    return E2D_OK;
+}
+
+template <typename T> void set_hist(SolverBase *b, double *h, int cap) {
+    auto *t = static_cast<SolverT<T> *>(b);
+    t->plan.hist = h;
+    t->plan.hist_cap = cap;
+}
+
+int build_graph(e2d_solver *s) {
+    if (s->gexec) return E2D_OK;
+    if (s->prm.precision == E2D_FP64) set_hist<double>(s->impl.get(), s->hist_dev, s->hist_cap);
+    else set_hist<float>(s->impl.get(), s->hist_dev, s->hist_cap);
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = E2D_OK;
+    for (int it = 0; it < s->graph_iters && rc == E2D_OK; it++) rc = s->impl->enqueue(s->stream);
+    cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) { set_error(std::string("graph capture: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
+    e = cudaGraphInstantiate(&s->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { s->gexec = nullptr; set_error(std::string("graph instantiate: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
+    return E2D_OK;
+}
+
+// Runs up to n iterations (fewer if the residual test stops the loop).
+int run(e2d_solver *s, int n, bool check, double epsl, int poll_every) {
+    if (n <= 0) return E2D_OK;
+    int rc = ensure_hist(s, s->ctl_host->step + n);
+    if (rc) return rc;
+    if ((rc = build_graph(s))) return rc;
+    Ctl &c = *s->ctl_host;
+    c.halt = 0;
+    c.nbad = 0;
+    c.target = c.step + n;
+    c.check_epsl = check ? 1 : 0;
+    c.epsl = epsl;
+    if ((rc = push_ctl(s))) return rc;
+    const int launches = (n + s->graph_iters - 1) / s->graph_iters;
+    CK(cudaEventRecord(s->ev0, s->stream));
+    for (int k = 0; k < launches; k++) {
+        CK(cudaGraphLaunch(s->gexec, s->stream));
+        if (check && poll_every > 0 && (k + 1) % poll_every == 0 && k + 1 < launches) {
+            if ((rc = pull_ctl(s))) return rc;
+            if (c.halt) break;
+        }
+    }
+    CK(cudaEventRecord(s->ev1, s->stream));
+    if ((rc = pull_ctl(s))) return rc;
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    s->last_ms = ms;
+    int have = (int)s->hist.size();
+    if (c.step > have) {
+        s->hist.resize(c.step);
+        CK(cudaMemcpy(s->hist.data() + have, s->hist_dev + have, sizeof(double) * (c.step - have),
+                      cudaMemcpyDeviceToHost));
+    }
+    if (c.halt == 2) {
+        set_error("solution diverged: non-positive density or pressure (or NaN) at step " + std::to_string(c.step));
+        return E2D_ERR_DIVERGED;
+    }
+    return E2D_OK;
+}
+
+bool valid_params(const e2d_params *p) {
+    if (!(p->gamma > 1.0) || !(p->ma > 0.0) || !(p->tin > 0.0) || !(p->cfl > 0.0)) return false;
+    if (p->rk_stages < 1 || p->rk_stages > 8 || p->irs_sweeps < 0 || p->irs_sweeps > 16) return false;
+    if (p->precision != E2D_FP64 && p->precision != E2D_FP32) return false;
+    if (p->ordering != E2D_ORDER_FILE && p->ordering != E2D_ORDER_MORTON) return false;
+    if (p->block_size != 0 && (p->block_size < 32 || p->block_size > 256 || p->block_size % 32)) return false;
+    if (p->graph_iters < 0 || p->graph_iters > 256) return false;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int e2d_solver_create(e2d_mesh *m, const e2d_params *p, e2d_solver **out) {
+    if (!m || !p || !out) { set_error("null argument"); return E2D_ERR_ARG; }
+    *out = nullptr;
+    if (!valid_params(p)) { set_error("invalid parameters"); return E2D_ERR_ARG; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        set_error("no CUDA device: the solver runs on the GPU only");
+        return E2D_ERR_CUDA;
+    }
+    auto s = std::make_unique<e2d_solver>();
+    s->prm = *p;
+    int rc = build_layout(m, *p, s->L);
+    if (rc) return rc;
+    s->fs = free_stream(*p);
+    CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    s->own_stream = true;
+    CK(cudaEventCreate(&s->ev0));
+    CK(cudaEventCreate(&s->ev1));
+    CK(cudaMalloc((void **)&s->ctl_dev, sizeof(Ctl)));
+    CK(cudaMallocHost((void **)&s->ctl_host, sizeof(Ctl)));
+    std::memset(s->ctl_host, 0, sizeof(Ctl));
+    s->ctl_host->resd = 100.0;  // gpu_solver.cu:2185 Resd[0]=100
+    CK(cudaMemcpy(s->ctl_dev, s->ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice));
+    s->graph_iters = p->graph_iters > 0 ? p->graph_iters : 8;
+    const int block = p->block_size > 0 ? p->block_size : 128;
+    if (p->precision == E2D_FP64) {
+        auto *t = new SolverT<double>(&s->L);
+        t->stream = &s->stream;
+        s->impl.reset(t);
+        if ((rc = t->init(*p, s->fs, s->ctl_dev, block))) return rc;
+    } else {
+        auto *t = new SolverT<float>(&s->L);
+        t->stream = &s->stream;
+        s->impl.reset(t);
+        if ((rc = t->init(*p, s->fs, s->ctl_dev, block))) return rc;
+    }
+    // free-stream state (gpu_init.cu:79-86)
+    std::vector<double> w0(4 * (size_t)s->L.n);
+    for (int i = 0; i < s->L.n; i++) {
+        w0[4 * (size_t)i] = 1.0; w0[4 * (size_t)i + 1] = std::cos(s->fs.alpha);
+        w0[4 * (size_t)i + 2] = std::sin(s->fs.alpha); w0[4 * (size_t)i + 3] = s->fs.rho_e;
+    }
+    if ((rc = s->impl->upload_state(w0.data()))) return rc;
+    if ((rc = ensure_hist(s.get(), std::max(1024, p->maxstep > 0 ? p->maxstep : 0)))) return rc;
+    *out = s.release();
+    return E2D_OK;
+}
+
+void e2d_solver_destroy(e2d_solver *s) { delete s; }
+
+int e2d_step(e2d_solver *s, int32_t n) {
+    if (!s || n < 0) { set_error("bad argument"); return E2D_ERR_ARG; }
+    return run(s, n, false, 0.0, 0);
+}
+
+int e2d_solve(e2d_solver *s, int32_t max_steps, double epsl, double *resid_history, int32_t *nsteps) {
+    if (!s || max_steps < 0) { set_error("bad argument"); return E2D_ERR_ARG; }
+    const int step0 = s->ctl_host->step;
+    int rc = E2D_OK;
+    // gpu_solver.cu:2200: while (step < MAXSTEP && Resd[step] > EPSL)
+    if (s->ctl_host->resd > epsl) rc = run(s, max_steps, true, epsl, std::max(1, 64 / s->graph_iters));
+    const int done = s->ctl_host->step - step0;
+    if (nsteps) *nsteps = done;
+    if (resid_history) std::memcpy(resid_history, s->hist.data() + step0, sizeof(double) * done);
+    if (s->prm.verbose)
+        for (int k = step0; k < step0 + done; k++) std::printf("%d,%1.20lf\n", k + 1, s->hist[k]);
+    return rc;
+}
+
+int e2d_progress(e2d_solver *s, int32_t *step, double *resd) {
+    if (!s) { set_error("null argument"); return E2D_ERR_ARG; }
+    if (step) *step = s->ctl_host->step;
+    if (resd) *resd = s->ctl_host->resd;
+    return E2D_OK;
+}
+
+int e2d_residual_history(e2d_solver *s, double *out, int32_t cap, int32_t *n) {
+    if (!s) { set_error("null argument"); return E2D_ERR_ARG; }
+    int k = std::min((int)s->hist.size(), std::max(0, (int)cap));
+    if (out && k) std::memcpy(out, s->hist.data(), sizeof(double) * k);
+    if (n) *n = (int)s->hist.size();
+    return E2D_OK;
+}
+
+int e2d_set_residual_norm(e2d_solver *s, double epsm) {
+    if (!s) { set_error("null argument"); return E2D_ERR_ARG; }
+    s->ctl_host->fixed_norm = epsm > 0.0;
+    if (epsm > 0.0) s->ctl_host->epsm = epsm;
+    return push_ctl(s);
+}
+
+int e2d_get_residual_norm(e2d_solver *s, double *epsm) {
+    if (!s || !epsm) { set_error("null argument"); return E2D_ERR_ARG; }
+    *epsm = s->ctl_host->epsm;
+    return E2D_OK;
+}
+
+int e2d_get_state(e2d_solver *s, double *w) {
+    if (!s || !w) { set_error("null argument"); return E2D_ERR_ARG; }
+    return s->impl->download_state(w);
+}
+
+int e2d_set_state(e2d_solver *s, const double *w) {
+    if (!s || !w) { set_error("null argument"); return E2D_ERR_ARG; }
+    return s->impl->upload_state(w);
+}
+
+int e2d_profile_passes(e2d_solver *s, int32_t iters, double *ms, int32_t *launches) {
+    if (!s || !ms || iters < 1) { set_error("bad argument"); return E2D_ERR_ARG; }
+    int rc = ensure_hist(s, s->ctl_host->step + iters);
+    if (rc) return rc;
+    if ((rc = build_graph(s))) return rc;  // sets the history pointer of the plan
+    Ctl &c = *s->ctl_host;
+    c.halt = 0; c.nbad = 0; c.target = c.step + iters; c.check_epsl = 0;
+    if ((rc = push_ctl(s))) return rc;
+    const int per = s->impl->launches();
+    std::vector<cudaEvent_t> ev(2 * (size_t)per * iters);
+    std::vector<int> kind((size_t)per * iters);
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    int j = 0;
+    for (int it = 0; it < iters; it++) j += s->impl->enqueue_timed(s->stream, ev.data() + 2 * j, kind.data() + j);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    for (int k = 0; k < 5; k++) { ms[k] = 0.0; if (launches) launches[k] = 0; }
+    for (int q = 0; q < j; q++) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, ev[2 * q], ev[2 * q + 1]));
+        ms[kind[q]] += t;
+        if (launches) launches[kind[q]]++;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    if ((rc = pull_ctl(s))) return rc;
+    int have = (int)s->hist.size();
+    if (c.step > have) {
+        s->hist.resize(c.step);
+        CK(cudaMemcpy(s->hist.data() + have, s->hist_dev + have, sizeof(double) * (c.step - have),
+                      cudaMemcpyDeviceToHost));
+    }
+    return c.halt == 2 ? E2D_ERR_DIVERGED : E2D_OK;
+}
+
+int e2d_forces(e2d_solver *s, double *cl, double *cd) {
+    if (!s) { set_error("null argument"); return E2D_ERR_ARG; }
+    std::vector<double> w(4 * (size_t)s->L.n);
+    int rc = e2d_get_state(s, w.data());
+    if (rc) return rc;
+    const double g = s->prm.gamma, pinf = s->fs.pis;
+    double fx = 0.0, fy = 0.0;
+    const int n = s->L.n;
+    for (size_t q = 0; q < s->L.wall_cell.size(); q++) {
+        const int i = s->L.wall_cell[q], k = s->L.wall_k[q];
+        const double *u = &w[4 * (size_t)s->L.perm[i]];
+        const double p = (g - 1.0) * (u[3] - 0.5 * (u[1] * u[1] + u[2] * u[2]) / u[0]);
+        fx += (p - pinf) * s->L.S[2 * ((size_t)k * n + i)];
+        fy += (p - pinf) * s->L.S[2 * ((size_t)k * n + i) + 1];
+    }
+    const double ca = std::cos(s->fs.alpha), sa = std::sin(s->fs.alpha);
+    if (cd) *cd = (fx * ca + fy * sa) / 0.5;
+    if (cl) *cl = (-fx * sa + fy * ca) / 0.5;
+    return E2D_OK;
+}
+
+int e2d_write_residual_plt(e2d_solver *s, const char *path) {
+    if (!s || !path) { set_error("null argument"); return E2D_ERR_ARG; }
+    FILE *fp = std::fopen(path, "w");
+    if (!fp) { set_error(std::string("cannot write ") + path); return E2D_ERR_IO; }
+    const int step = (int)s->hist.size();
+    // gpu_fvm.cu:165-175
+    std::fprintf(fp, "TITLE     = \"Dataset\"\nVARIABLES = \"Time\" \"Resid\" \n");
+    std::fprintf(fp, "ZONE I=%d J=%d f=point \n", step, 1);
+    for (int i = 1; i <= step; i++)
+        if (i % 100 == 0) std::fprintf(fp, "%d %20.10lf\n", i, s->hist[i - 1]);
+    std::fclose(fp);
+    return E2D_OK;
+}
+
+int e2d_last_device_ms(e2d_solver *s, double *ms) {
+    if (!s || !ms) { set_error("null argument"); return E2D_ERR_ARG; }
+    *ms = s->last_ms;
+    return E2D_OK;
+}
+
+int e2d_launches_per_iteration(e2d_solver *s, int32_t *n) {
+    if (!s || !n) { set_error("null argument"); return E2D_ERR_ARG; }
+    *n = s->impl->launches();
+    return E2D_OK;
+}
+
+int e2d_set_stream(e2d_solver *s, void *cuda_stream) {
+    if (!s) { set_error("null argument"); return E2D_ERR_ARG; }
+    CK(cudaStreamSynchronize(s->stream));
+    if (s->own_stream) cudaStreamDestroy(s->stream);
+    s->own_stream = cuda_stream == nullptr;
+    if (s->own_stream) CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    else s->stream = (cudaStream_t)cuda_stream;
+    return E2D_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,181 @@
+/*
+ * euler2d.h -- C ABI of the GB300 cell-centred finite-volume Euler solver
+ * for triangle meshes (libeuler2d.so).
+ *
+ * The library is a drop-in for the solve path of GPUEularSolver2D: it reads
+ * the same mesh and input files, builds the same edge numbering, runs the same
+ * scheme (far-field Riemann-invariant and slip-wall ghosts, Green-Gauss
+ * gradient, per-face Barth-Jespersen-type limited MUSCL reconstruction, Roe
+ * flux with Harten entropy fix, local time step, implicit residual smoothing,
+ * multistage Runge-Kutta) and reports the same residual history.  Reference
+ * functions are cited as file:line of that project.
+ *
+ * Conventions (new; the reference has no error handling):
+ *   - every function returns an int status: 0 success, < 0 error, and
+ *     e2d_last_error() describes the last error of the calling thread;
+ *   - opaque handles own all their host and device memory;
+ *   - a solver is bound to one CUDA stream and must be driven from one thread
+ *     at a time;
+ *   - cell data crossing this interface is in FILE order (the order of the
+ *     cells in the mesh file, 0-based here, 1-based in the reference), whatever
+ *     internal renumbering the solver uses;
+ *   - conserved variables are (rho, rho u, rho v, rho E), non-dimensional with
+ *     rho_inf = 1 and |V_inf| = 1 as in the reference (gpu_init.cu:63-93).
+ */
+#ifndef EULER2D_H
+#define EULER2D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define E2D_OK 0
+#define E2D_ERR_ARG -1       /* bad argument                            */
+#define E2D_ERR_IO -2        /* file cannot be opened / parsed          */
+#define E2D_ERR_MESH -3      /* invalid mesh (area <= 0, non-manifold)  */
+#define E2D_ERR_CUDA -4      /* CUDA runtime error / no device          */
+#define E2D_ERR_DIVERGED -5  /* non-positive density or pressure, NaN   */
+#define E2D_ERR_CAPACITY -6  /* request beyond a fixed capacity         */
+
+#define E2D_FP64 0           /* FP64 stencil (parity variant)          */
+#define E2D_FP32 1           /* FP32 stencil, FP64 geometry and norms  */
+
+#define E2D_ORDER_FILE 0     /* cells in file order                    */
+#define E2D_ORDER_MORTON 1   /* cells sorted by centroid Morton code   */
+
+typedef struct e2d_mesh e2d_mesh;
+typedef struct e2d_solver e2d_solver;
+typedef struct e2d_batch e2d_batch;
+
+/* Solver parameters.  The first eight fields are the reference's input.dat
+ * (gpu_init.cu:41); the rest are constants the reference hard-codes, exposed
+ * with the reference values as defaults. */
+typedef struct e2d_params {
+    double ma;           /* free-stream Mach number              (MA)      */
+    double alpha_deg;    /* angle of attack, degrees             (ALPHA)   */
+    double gamma;        /* ratio of specific heats              (GAMA)    */
+    double pin;          /* free-stream pressure, Pa             (PIN)     */
+    double tin;          /* free-stream temperature, K           (TIN)     */
+    double cfl;          /* CFL number                           (CFL)     */
+    double epsl;         /* stop when Resd <= epsl               (EPSL)    */
+    int32_t maxstep;     /* iteration limit                      (MAXSTEP) */
+    int32_t rk_stages;   /* 1..8; reference 4 (gpu_solver.cu:2211)         */
+    double rk_coef[8];   /* reference {0.0833,0.2069,0.4265,1.0} (gpu_fvm.cu:10) */
+    double irs_eps;      /* smoothing coefficient; reference 0.8 (gpu_solver.cu:1633) */
+    int32_t irs_sweeps;  /* 0 = off; reference 2 (gpu_solver.cu:1722-1728) */
+    int32_t precision;   /* E2D_FP64 (default) or E2D_FP32                 */
+    double dt_cap;       /* local time step cap; reference 0.1 (gpu_solver.cu:831) */
+    double entropy_eps;  /* Harten fix width; reference 0.05 (gpu_solver.cu:603) */
+    double wall_box;     /* boundary face is wall if |mid x|,|mid y| < wall_box;
+                            reference 2.0 (gpu_init.cu:190)                 */
+    int32_t ordering;    /* E2D_ORDER_FILE (default) or E2D_ORDER_MORTON    */
+    int32_t block_size;  /* threads per CTA, 0 = tuned default              */
+    int32_t graph_iters; /* iterations captured per CUDA graph, 0 = default */
+    int32_t verbose;     /* e2d_solve prints "step,resid" lines like the
+                            reference (gpu_solver.cu:2433) when nonzero     */
+} e2d_params;
+
+typedef struct e2d_mesh_info {
+    int32_t ncell, nnode, nedge, nwall, nfar;
+} e2d_mesh_info;
+
+/* ---- errors ----------------------------------------------------------- */
+const char *e2d_last_error(void);
+const char *e2d_version(void);
+
+/* ---- parameters ------------------------------------------------------- */
+/* Reference defaults (input.dat fields: M 0.5, alpha 0, gamma 1.4,
+ * p 101325 Pa, T 288.15 K, CFL 1, EPSL 1e-6, MAXSTEP 100). */
+int e2d_params_default(e2d_params *p);
+/* Reads input.dat: "MA ALPHA GAMA PIN TIN CFL EPSL MAXSTEP" (gpu_init.cu:34-42);
+ * fields not in the file are left as they are in *p. */
+int e2d_input_read(const char *path, e2d_params *p);
+
+/* ---- meshes ----------------------------------------------------------- */
+/* Reads a reference .dat mesh: "Nnode Ncell", Nnode x, Nnode y, then 3
+ * 1-based CCW node ids per cell (gpu_init.cu:5-33, replaces inputMesh). */
+int e2d_mesh_read(const char *path, e2d_mesh **out);
+/* Writes the same format (%.17g, so a read gives back the same doubles). */
+int e2d_mesh_write(const char *path, const e2d_mesh *m);
+/* Builds a mesh from arrays: x,y [nnode]; tri [3*ncell] 1-based node ids. */
+int e2d_mesh_from_arrays(int32_t nnode, int32_t ncell, const double *x, const double *y,
+                         const int32_t *tri, e2d_mesh **out);
+/* O-grid around NACA 0012 (chord 1, closed trailing edge): ni points around,
+ * nj cell layers out to a circle of radius r_far chords, first wall spacing
+ * dy_wall chords with geometric stretching, each quad split along a seeded
+ * random diagonal and interior nodes jittered by +-jitter of the local
+ * spacing.  Writes 2*ni*nj cells and ni*(nj+1) nodes.  No reference
+ * counterpart. */
+int e2d_mesh_ogrid_naca0012(int32_t ni, int32_t nj, double r_far, double dy_wall,
+                            double jitter, uint64_t seed, e2d_mesh **out);
+void e2d_mesh_free(e2d_mesh *m);
+/* Runs the set-up (geometry, edge discovery, boundary tags) if needed. */
+int e2d_mesh_info_get(e2d_mesh *m, double wall_box, e2d_mesh_info *info);
+/* Set-up in reference numbering, after the interior/far/wall partition of
+ * changeEdge (gpu_solver.cu:1832-1906); all ids 1-based as in the reference.
+ *   ei [nedge*7]: ELog, left_cell, right_cell, farfieldid, wallid, node1, node2
+ *   ed [nedge*5]: vectorn, vectorx, vectory, midx, midy
+ *   ci [ncell*7]: CLog, celledge[0..2], neicell[0..2]
+ *   cd [ncell*3]: area, centre x, centre y
+ * Replaces CalculationMeshGeo (gpu_init.cu:100-228); any pointer may be NULL. */
+int e2d_mesh_topology(e2d_mesh *m, double wall_box, int32_t *ei, double *ed, int32_t *ci,
+                      double *cd);
+/* Mesh nodes and cells: x,y [nnode], tri [3*ncell] (1-based). */
+int e2d_mesh_nodes(const e2d_mesh *m, double *x, double *y, int32_t *tri);
+/* Cell order used by a given ordering: perm[k] = 0-based file index of the
+ * cell at internal position k.  No reference counterpart. */
+int e2d_mesh_order(e2d_mesh *m, int32_t ordering, int32_t *perm);
+
+/* ---- solver ----------------------------------------------------------- */
+/* Set-up + device upload + free-stream state (gpu_init.cu:63-93,
+ * gpu_solver.cu:2187-2194); replaces Initialization, Cuda_Init and the
+ * set-up half of ROE_SOLVER.  Uses the current CUDA device. */
+int e2d_solver_create(e2d_mesh *m, const e2d_params *p, e2d_solver **out);
+void e2d_solver_destroy(e2d_solver *s);
+/* Iterates like ROE_SOLVER (gpu_solver.cu:2200-2434): stops when
+ * Resd <= epsl or after max_steps more iterations.  resid_history receives
+ * Resd of each iteration run (may be NULL); *nsteps the number run. */
+int e2d_solve(e2d_solver *s, int32_t max_steps, double epsl, double *resid_history,
+              int32_t *nsteps);
+/* Exactly n iterations, no convergence stop (residuals are still recorded). */
+int e2d_step(e2d_solver *s, int32_t n);
+/* Total iterations so far and the last Resd. */
+int e2d_progress(e2d_solver *s, int32_t *step, double *resd);
+/* Residual history Resd[1..step] of every iteration so far (cap entries). */
+int e2d_residual_history(e2d_solver *s, double *out, int32_t cap, int32_t *n);
+/* Residual normalisation: Resd = sqrt((drou + 1e-32) / epsm); by default
+ * epsm is drou of iteration 1 (gpu_solver.cu:2428).  Setting it > 0 fixes it. */
+int e2d_set_residual_norm(e2d_solver *s, double epsm);
+int e2d_get_residual_norm(e2d_solver *s, double *epsm);
+/* Conserved state in file order, [ncell*4] FP64. */
+int e2d_get_state(e2d_solver *s, double *w);
+int e2d_set_state(e2d_solver *s, const double *w);
+/* Lift and drag coefficients from the wall pressure of the wall cells
+ * (sum over wall faces of (p - p_inf) S, rotated by alpha, divided by
+ * 0.5 rho_inf V_inf^2 c = 0.5), accumulated in FP64.  No reference
+ * counterpart. */
+int e2d_forces(e2d_solver *s, double *cl, double *cd);
+/* unresidual.plt as the reference writes it (gpu_fvm.cu:165-175): every
+ * 100th step. */
+int e2d_write_residual_plt(e2d_solver *s, const char *path);
+/* Device time of the kernels of the last e2d_step/e2d_solve call, ms,
+ * measured with CUDA events on the solver's stream. */
+int e2d_last_device_ms(e2d_solver *s, double *ms);
+/* Kernel launches per iteration (all passes of all stages). */
+int e2d_launches_per_iteration(e2d_solver *s, int32_t *n);
+/* Runs iters iterations launching the kernels one by one (no graph) with a
+ * CUDA event pair around every launch, and returns the summed device time per
+ * pass kind: ms[0] ghosts+gradient+reconstruction (pass A), ms[1] flux
+ * gather (pass B), ms[2] smoothing sweeps (pass C), ms[3] smoothing + RK
+ * update (pass D), ms[4] residual; launches[k] (may be NULL) the launch
+ * counts.  The iterations advance the solution like e2d_step. */
+int e2d_profile_passes(e2d_solver *s, int32_t iters, double *ms, int32_t *launches);
+/* Sets the CUDA stream used by the solver (default: a stream it owns). */
+int e2d_set_stream(e2d_solver *s, void *cuda_stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

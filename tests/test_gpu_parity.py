@@ -1,0 +1,115 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+The FP64 variant must reproduce the oracle bit for bit (same IEEE operations,
+no FMA contraction); the FP32 variant is reported against the FP64 run of the
+same code with the tolerance written in each test.
+"""
+import numpy as np
+import pytest
+
+import gpueularsolver2d_gb300 as e2d
+
+pytestmark = pytest.mark.gpu
+
+BLAZEK5 = [0.0695, 0.1602, 0.2898, 0.5060, 1.0]
+
+
+def run_pair(mesh, oracle, nsteps, **kw):
+    p = e2d.default_params(**kw)
+    s = e2d.Solver(mesh, p)
+    x, y, tri = mesh.nodes()
+    c = oracle.Case(x, y, tri, oracle.params_from_e2d(p))
+    r_ref = c.run(nsteps)
+    s.step(nsteps)
+    return s, c, r_ref
+
+
+@pytest.mark.parametrize("kw", [
+    dict(ma=0.5, alpha_deg=1.25, cfl=1.5),
+    dict(ma=0.8, alpha_deg=1.25, cfl=2.0, irs_eps=0.6, rk_stages=5, rk_coef=BLAZEK5),
+    dict(ma=0.5, alpha_deg=-2.0, cfl=1.0, irs_sweeps=0),
+    dict(ma=0.7, alpha_deg=3.0, cfl=1.5, irs_sweeps=3, ordering=e2d.E2D_ORDER_MORTON),
+])
+def test_fp64_bit_exact_vs_oracle(lib, oracle, kw):
+    mesh = e2d.Mesh.ogrid(48, 12, seed=7)
+    s, c, r_ref = run_pair(mesh, oracle, 25, **kw)
+    w = s.state()
+    assert np.array_equal(w, c.state()), np.max(np.abs(w - c.state()))
+    hist = s.history()
+    assert len(hist) == 25
+    np.testing.assert_allclose(hist, r_ref, rtol=1e-12, atol=0)
+
+
+def test_fp64_bit_exact_128x32_morton(lib, oracle):
+    mesh = e2d.Mesh.ogrid(128, 32, seed=1)
+    s, c, r_ref = run_pair(mesh, oracle, 40, ma=0.5, alpha_deg=1.25, cfl=2.0,
+                           ordering=e2d.E2D_ORDER_MORTON)
+    assert np.array_equal(s.state(), c.state())
+    np.testing.assert_allclose(s.history(), r_ref, rtol=1e-12)
+
+
+def test_fp32_close_to_fp64(lib):
+    mesh = e2d.Mesh.ogrid(128, 32, seed=1)
+    kw = dict(ma=0.5, alpha_deg=1.25, cfl=2.0)
+    s64 = e2d.Solver(mesh, e2d.default_params(**kw))
+    s32 = e2d.Solver(mesh, e2d.default_params(precision=e2d.E2D_FP32, **kw))
+    s64.step(50)
+    s32.step(50)
+    w64, w32 = s64.state(), s32.state()
+    rel = np.max(np.abs(w32 - w64)) / np.max(np.abs(w64))
+    # FP32 stencil against the FP64 run of the same code after 50 iterations
+    assert rel < 1e-3, rel
+    np.testing.assert_allclose(s32.history(), s64.history(), rtol=5e-2)
+
+
+def test_solve_stops_like_reference_loop(lib, oracle):
+    mesh = e2d.Mesh.ogrid(32, 8, seed=3)
+    p = e2d.default_params(ma=0.5, alpha_deg=1.25, cfl=1.5)
+    s = e2d.Solver(mesh, p)
+    x, y, tri = mesh.nodes()
+    c = oracle.Case(x, y, tri, oracle.params_from_e2d(p))
+    full = c.run(200)
+    epsl = float(full[120])  # stop exactly where the reference loop would
+    s2 = e2d.Solver(mesh, p)
+    hist = s2.solve(500, epsl)
+    k = int(np.argmax(full <= epsl)) + 1
+    assert len(hist) == k
+    np.testing.assert_allclose(hist, full[:k], rtol=1e-12)
+    # a second solve with the same target runs nothing (Resd already <= EPSL)
+    assert len(s2.solve(10, epsl)) == 0
+
+
+def test_split_steps_equal_one_run(lib):
+    mesh = e2d.Mesh.ogrid(40, 10, seed=5)
+    p = e2d.default_params(ma=0.6, alpha_deg=2.0, cfl=1.5, graph_iters=4)
+    a = e2d.Solver(mesh, p)
+    b = e2d.Solver(mesh, p)
+    a.step(11)
+    for n in (3, 1, 7):
+        b.step(n)
+    assert np.array_equal(a.state(), b.state())
+    assert np.array_equal(a.history(), b.history())
+
+
+def test_ordering_invariance(lib):
+    # the per-cell arithmetic does not depend on the cell order
+    mesh = e2d.Mesh.ogrid(96, 24, seed=11)
+    for prec in (e2d.E2D_FP64, e2d.E2D_FP32):
+        kw = dict(ma=0.75, alpha_deg=1.0, cfl=2.0, precision=prec)
+        a = e2d.Solver(mesh, e2d.default_params(ordering=e2d.E2D_ORDER_FILE, **kw))
+        b = e2d.Solver(mesh, e2d.default_params(ordering=e2d.E2D_ORDER_MORTON, **kw))
+        a.step(20)
+        b.step(20)
+        assert np.array_equal(a.state(), b.state())
+
+
+def test_state_roundtrip_and_forces(lib):
+    mesh = e2d.Mesh.ogrid(64, 16, seed=2)
+    s = e2d.Solver(mesh, e2d.default_params(ma=0.5, alpha_deg=2.0, cfl=1.5))
+    s.step(30)
+    w = s.state()
+    s2 = e2d.Solver(mesh, e2d.default_params(ma=0.5, alpha_deg=2.0, cfl=1.5))
+    s2.set_state(w)
+    assert np.array_equal(s2.state(), w)
+    cl, cd = s.forces()
+    assert np.isfinite(cl) and np.isfinite(cd)
