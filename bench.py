@@ -39,6 +39,9 @@ WORKLOADS = {
     "large": dict(ni=2048, nj=1024, ma=0.78, alpha=2.0, cfl=2.0,
                   desc="NACA0012 O-grid 2048x1024 (4194304 tri), Morton, M0.78 a2.0, FP32 stencil, "
                        "IRS 2 sweeps eps 0.8, 4-stage RK"),
+    "medium": dict(ni=1024, nj=512, ma=0.78, alpha=2.0, cfl=2.0,
+                   desc="NACA0012 O-grid 1024x512 (1048576 tri), Morton, M0.78 a2.0, FP32 stencil, "
+                        "IRS 2 sweeps eps 0.8, 4-stage RK"),
     "transonic": dict(ni=512, nj=128, ma=0.80, alpha=1.25, cfl=2.0,
                       desc="NACA0012 O-grid 512x128 (131072 tri), Morton, M0.80 a1.25, FP32 stencil, "
                            "IRS 2 sweeps eps 0.8, 4-stage RK"),
@@ -161,9 +164,15 @@ def run_reference(args, rank: int, world: int):
     p = pyoracle.params(ma=wl["ma"], alpha_deg=wl["alpha"], cfl=wl["cfl"])
     case = pyoracle.Case(x, y, tri, p)
     th = pyoracle.threads()
-    case.run(args.warmup)
+    # warm-up, timing the last warm-up iteration to size the timed sample so
+    # the run stays within about a minute of host time
+    case.run(max(0, args.warmup - 1))
     t0 = time.perf_counter()
-    k = len(case.run(args.steps))
+    case.run(1)
+    t_it = time.perf_counter() - t0
+    k_want = max(1, min(args.steps, int(60.0 / max(t_it, 1e-6))))
+    t0 = time.perf_counter()
+    k = len(case.run(k_want))
     dt = time.perf_counter() - t0
     rate = case.ncell * p.rk_stages * k / dt
     line = {
@@ -174,7 +183,8 @@ def run_reference(args, rank: int, world: int):
         "config": {"workload": wl["desc"], "cells": case.ncell, "stages": p.rk_stages,
                    "parallelism": f"replicas{world}"},
         "cpu_baseline": {"value": rate, "unit": "cell-stage/s", "cores": th, "kind": "port",
-                         "sample": f"{k} iterations of the full {case.ncell}-cell workload"},
+                         "sample": f"{k} of the {args.steps} requested iterations (capped at ~60 s of host "
+                                   f"time) of the full {case.ncell}-cell workload on {th} threads"},
         "e2e": {"value": rate, "unit": "cell-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -320,7 +330,7 @@ def traffic_from_profiles(kernel: str, ncell: int):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="large")

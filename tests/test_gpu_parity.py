@@ -48,18 +48,37 @@ def test_fp64_bit_exact_128x32_morton(lib, oracle):
     np.testing.assert_allclose(s.history(), r_ref, rtol=1e-12)
 
 
-def test_fp32_close_to_fp64(lib):
+def test_fp32_error_vs_fp64(lib):
+    """FP32 stencil against the FP64 run of the same code.
+
+    One iteration stays at FP32 rounding.  Through the start-up transient the
+    limiter and the smoothing clamp switch on tiny differences and amplify
+    any change of rounding (the reference's own FMA-contracted FP64 kernels
+    drift from the oracle the same way, at the FP64 level), so longer runs
+    are held to the median error, the maximum error and the residual
+    history, with the tolerances written here."""
     mesh = e2d.Mesh.ogrid(128, 32, seed=1)
     kw = dict(ma=0.5, alpha_deg=1.25, cfl=2.0)
     s64 = e2d.Solver(mesh, e2d.default_params(**kw))
     s32 = e2d.Solver(mesh, e2d.default_params(precision=e2d.E2D_FP32, **kw))
-    s64.step(50)
-    s32.step(50)
-    w64, w32 = s64.state(), s32.state()
-    rel = np.max(np.abs(w32 - w64)) / np.max(np.abs(w64))
-    # FP32 stencil against the FP64 run of the same code after 50 iterations
-    assert rel < 1e-3, rel
-    np.testing.assert_allclose(s32.history(), s64.history(), rtol=5e-2)
+
+    def err():
+        w64, w32 = s64.state(), s32.state()
+        d = np.abs(w32 - w64) / np.abs(w64).max(axis=0)
+        return d.max(), np.median(d)
+
+    s64.step(1)
+    s32.step(1)
+    assert err()[0] < 5e-6
+    s64.step(9)
+    s32.step(9)
+    assert err()[0] < 1e-4
+    s64.step(290)
+    s32.step(290)
+    mx, med = err()
+    assert mx < 2e-2 and med < 1e-3, (mx, med)
+    h64, h32 = s64.history(), s32.history()
+    assert np.max(np.abs(h32 - h64) / h64) < 2e-2
 
 
 def test_solve_stops_like_reference_loop(lib, oracle):

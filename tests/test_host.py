@@ -1,0 +1,131 @@
+"""Host-side logic of libeuler2d (no GPU needed): the C ABI loads and exports
+every symbol the header declares, the mesh reader/writer and generator, the
+O(N) set-up against the oracle's restatement of CalculationMeshGeo +
+changeEdge, the Morton permutation, and error reporting."""
+import os
+import re
+import tempfile
+
+import numpy as np
+import pytest
+
+import gpueularsolver2d_gb300 as e2d
+from gpueularsolver2d_gb300 import _lib
+from conftest import ROOT, reference_mesh
+
+
+def header_functions(name):
+    text = open(os.path.join(ROOT, "include", name)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(e2d_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    fns = header_functions("euler2d.h")
+    assert len(fns) > 20
+    for f in fns:
+        assert hasattr(lib, f), f
+        assert f in _lib.SIGNATURES, f
+
+
+@pytest.mark.parametrize("ni,nj,seed", [(16, 4, 1), (48, 12, 7), (128, 32, 1), (100, 20, 42)])
+def test_setup_matches_oracle(lib, oracle, ni, nj, seed):
+    mesh = e2d.Mesh.ogrid(ni, nj, seed=seed)
+    x, y, tri = mesh.nodes()
+    case = oracle.Case(x, y, tri, oracle.params())
+    for a, b in zip(mesh.topology(), case.topology()):
+        assert np.array_equal(a, b)
+    assert np.array_equal(mesh.order(e2d.E2D_ORDER_MORTON) + 1, case.morton())
+    assert np.array_equal(mesh.order(e2d.E2D_ORDER_FILE), np.arange(case.ncell))
+
+
+@pytest.mark.parametrize("name", ["2822-3k.dat", "2822-1w.dat", "2822-5w.dat", "2822-9w.dat"])
+def test_setup_matches_oracle_on_reference_meshes(lib, oracle, name):
+    path = reference_mesh(name)
+    if path is None:
+        pytest.skip("reference meshes not available")
+    mesh = e2d.Mesh.read(path)
+    case = oracle.Case.from_file(path, oracle.params())
+    for a, b in zip(mesh.topology(), case.topology()):
+        assert np.array_equal(a, b)
+    assert np.array_equal(mesh.order(e2d.E2D_ORDER_MORTON) + 1, case.morton())
+
+
+def test_ogrid_sizes_and_tags(lib):
+    for ni, nj in [(16, 4), (128, 32), (256, 64)]:
+        inf = e2d.Mesh.ogrid(ni, nj).info()
+        assert (inf.ncell, inf.nnode, inf.nedge, inf.nwall, inf.nfar) == (
+            2 * ni * nj, ni * (nj + 1), 3 * ni * nj + ni, ni, ni)
+
+
+def test_ogrid_deterministic_and_ccw(lib):
+    a = e2d.Mesh.ogrid(64, 16, seed=5).nodes()
+    b = e2d.Mesh.ogrid(64, 16, seed=5).nodes()
+    c = e2d.Mesh.ogrid(64, 16, seed=6).nodes()
+    assert all(np.array_equal(u, v) for u, v in zip(a, b))
+    assert not np.array_equal(a[0], c[0])
+    x, y, tri = a
+    t = tri - 1
+    area = 0.5 * ((y[t[:, 2]] - y[t[:, 0]]) * (x[t[:, 1]] - x[t[:, 0]])
+                  - (y[t[:, 1]] - y[t[:, 0]]) * (x[t[:, 2]] - x[t[:, 0]]))
+    assert area.min() > 0
+    r = np.hypot(x - 0.5, y)
+    assert abs(r.max() - 20.0) < 1e-9
+
+
+def test_mesh_write_read_roundtrip(lib):
+    m = e2d.Mesh.ogrid(32, 8, seed=2)
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "m.dat")
+        m.write(p)
+        m2 = e2d.Mesh.read(p)
+    for u, v in zip(m.nodes(), m2.nodes()):
+        assert np.array_equal(u, v)
+
+
+def test_input_read(lib):
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "input.dat")
+        with open(p, "w") as f:
+            f.write("0.8 1.25 1.4 101325 288.15 4.0 1e-6 5000\n")
+        prm = e2d.read_input(p)
+        assert (prm.ma, prm.alpha_deg, prm.cfl, prm.epsl, prm.maxstep) == (0.8, 1.25, 4.0, 1e-6, 5000)
+        assert prm.rk_stages == 4 and prm.irs_eps == 0.8 and prm.irs_sweeps == 2
+        with open(p, "w") as f:
+            f.write("0.8 1.25\n")
+        with pytest.raises(_lib.E2DError) as ei:
+            e2d.read_input(p)
+        assert ei.value.code == -2
+
+
+def test_errors(lib):
+    with pytest.raises(_lib.E2DError) as ei:
+        e2d.Mesh.read("/nonexistent/mesh.dat")
+    assert ei.value.code == -2
+    x = np.array([0.0, 1.0, 0.0, 1.0])
+    y = np.array([0.0, 0.0, 1.0, 1.0])
+    cw = e2d.Mesh.from_arrays(x, y, np.array([[1, 3, 2]]))  # clockwise cell
+    with pytest.raises(_lib.E2DError) as ei:
+        cw.info()
+    assert ei.value.code == -3 and "area" in str(ei.value)
+    fan = e2d.Mesh.from_arrays(np.array([0.0, 1.0, 0.5, 0.5, 0.5]), np.array([0.0, 0.0, 1.0, -1.0, 2.0]),
+                               np.array([[1, 2, 3], [2, 1, 4], [1, 2, 5]]))
+    with pytest.raises(_lib.E2DError) as ei:
+        fan.info()
+    assert ei.value.code == -3
+    bad = e2d.Mesh.from_arrays(x, y, np.array([[1, 2, 9]]))
+    with pytest.raises(_lib.E2DError):
+        bad.info()
+    with pytest.raises(_lib.E2DError) as ei:
+        e2d.Solver(e2d.Mesh.ogrid(16, 4), e2d.default_params(rk_stages=9))
+    assert ei.value.code == -1
+
+
+def test_truncated_mesh_file(lib):
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "m.dat")
+        with open(p, "w") as f:
+            f.write("4 2\n0 1 0 1\n0 0 1\n")
+        with pytest.raises(_lib.E2DError) as ei:
+            e2d.Mesh.read(p)
+        assert ei.value.code == -2
