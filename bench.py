@@ -125,9 +125,9 @@ def measured_peak_hbm() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def make_params(e2d, wl, precision):
+def make_params(e2d, wl, precision, block=0):
     return e2d.default_params(ma=wl["ma"], alpha_deg=wl["alpha"], cfl=wl["cfl"], precision=precision,
-                              ordering=e2d.E2D_ORDER_MORTON, maxstep=1000000)
+                              ordering=e2d.E2D_ORDER_MORTON, maxstep=1000000, block_size=block)
 
 
 def cpu_port_rate(wl, steps_wanted: float, threads: int | None = None, mesh=None):
@@ -204,7 +204,7 @@ def run_gpu(args, rank: int, world: int):
     wl = WORKLOADS[args.workload]
     prec = e2d.E2D_FP64 if args.fp64 else e2d.E2D_FP32
     mesh = e2d.Mesh.ogrid(wl["ni"], wl["nj"], seed=1)
-    params = make_params(e2d, wl, prec)
+    params = make_params(e2d, wl, prec, args.block)
     solver = e2d.Solver(mesh, params)
     ncell, stages = solver.ncell, params.rk_stages
     launches = solver.launches_per_iteration()
@@ -335,6 +335,7 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="large")
     ap.add_argument("--fp64", action="store_true")
+    ap.add_argument("--block", type=int, default=0, help="threads per CTA (0: library default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -21,14 +21,17 @@ LIBDIR = os.path.join(PKG, "lib")
 OBJDIR = os.path.join(PKG, "_build")
 LIB = os.path.join(LIBDIR, "libeuler2d.so")
 CLI = os.path.join(LIBDIR, "e2d_solve")
+COMPAT = os.path.join(LIBDIR, "libeuler2d_compat.a")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = [*ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                "-Xcompiler", "-ffp-contract=off", f"-I{os.path.join(ROOT, 'include')}"]
 
+GXX = ["g++", "-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall",
+       f"-I{os.path.join(ROOT, 'include')}"]
 UNITS = {
-    "mesh.o": ("mesh.cpp", ["g++", "-O2", "-fPIC", "-std=c++17", "-ffp-contract=off",
-                            "-Wall", f"-I{os.path.join(ROOT, 'include')}"]),
+    "mesh.o": ("mesh.cpp", GXX),
+    "output.o": ("output.cpp", GXX),
     "solver.o": ("solver.cu", ["nvcc", *NVCC_COMMON]),
     "resid.o": ("resid.cu", ["nvcc", *NVCC_COMMON]),
     "kernels_f64.o": ("kernels_f64.cu", ["nvcc", *NVCC_COMMON, "--fmad=false"]),
@@ -47,6 +50,8 @@ def _stale(target: str, deps: list[str]) -> bool:
 
 def _compile(obj: str, src: str, cmd: list[str], verbose_ptxas: bool) -> None:
     extra = ["-Xptxas", "-v"] if verbose_ptxas and cmd[0] == "nvcc" else []
+    if cmd[0] == "nvcc":  # tuning experiments: extra nvcc flags, e.g. -DE2D_MINB_FACES=6
+        extra += os.environ.get("E2D_NVCC_EXTRA", "").split()
     full = [*cmd, *extra, "-c", os.path.join(CSRC, src), "-o", os.path.join(OBJDIR, obj)]
     res = subprocess.run(full, capture_output=True, text=True)
     if res.returncode != 0:
@@ -74,9 +79,18 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
         subprocess.run(["nvcc", *ARCH, "-shared", "-o", tmp, *objs], check=True)
         os.replace(tmp, LIB)
     cli_src = os.path.join(CSRC, "e2d_solve_main.cpp")
-    if os.path.exists(cli_src) and (force or _stale(CLI, [cli_src, LIB])):
+    if force or _stale(CLI, [cli_src, LIB]):
         subprocess.run(["g++", "-O2", "-std=c++17", f"-I{os.path.join(ROOT, 'include')}", cli_src,
                         "-o", CLI, f"-L{LIBDIR}", "-leuler2d", "-Wl,-rpath,$ORIGIN"], check=True)
+    # the reference's function surface, for linking the reference's gpu_fvm.cu
+    compat_src = os.path.join(CSRC, "compat.cpp")
+    compat_o = os.path.join(OBJDIR, "compat.o")
+    compat_deps = [compat_src, os.path.join(ROOT, "include", "euler2d_compat.h"), *hdrs]
+    if force or _stale(COMPAT, compat_deps):
+        subprocess.run([*GXX, "-I/usr/local/cuda/include", "-c", compat_src, "-o", compat_o], check=True)
+        if os.path.exists(COMPAT):
+            os.remove(COMPAT)
+        subprocess.run(["ar", "rcs", COMPAT, compat_o], check=True)
     return LIB
 
 

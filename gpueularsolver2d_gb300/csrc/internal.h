@@ -25,6 +25,9 @@ struct MeshTopo {
     std::vector<double> area, cx, cy;
     std::vector<int> clog;
     std::vector<int> celledge, neicell;  // [3*ncell], reference ids
+    // edge id before the changeEdge partition (discovery order, as
+    // CalculationMeshGeo leaves it) -> id after it; both 1-based
+    std::vector<int> pre2post;           // [nedge+1]
     // per cell face: 0-based neighbour cell (-1 far, -2 wall), whether this
     // cell is the edge's right cell, and the face slot of the neighbour
     std::vector<int> nb, nb_slot;

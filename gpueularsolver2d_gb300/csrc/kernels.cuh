@@ -26,6 +26,15 @@
 
 namespace e2d {
 
+// Occupancy targets (minimum resident 256-thread blocks per SM) of the two
+// gather kernels; the register budget follows from them.  Build-time knobs.
+#ifndef E2D_MINB_FACES
+#define E2D_MINB_FACES 1
+#endif
+#ifndef E2D_MINB_FLUX
+#define E2D_MINB_FLUX 1
+#endif
+
 template <typename T> __device__ __forceinline__ T tabs(T v) { return fabs(v); }
 template <typename T> __device__ __forceinline__ T tsqrt(T v) { return sqrt(v); }
 template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return fmin(a, b); }
@@ -202,7 +211,7 @@ __device__ __forceinline__ V4<T> roe(const V4<T> &LW, const V4<T> &RW, T nx, T n
 // reconstruction for an interior face, the cell state itself for a boundary
 // face (the reference's boundary faces are first order).
 template <typename T>
-__global__ void __launch_bounds__(256) k_faces(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ W,
+__global__ void __launch_bounds__(256, E2D_MINB_FACES) k_faces(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ W,
                                                V4<T> *__restrict__ FS, T *__restrict__ dt,
                                                const Ctl *__restrict__ ctl) {
     if (ctl->halt) return;
@@ -276,7 +285,7 @@ __global__ void __launch_bounds__(256) k_faces(MeshDev<T> m, Flow<T> f, const V4
 // three faces, summed as gpu_solver.cu:798-825 (+F where the cell is the
 // edge's left cell, -F where it is the right cell, in face order).
 template <typename T>
-__global__ void __launch_bounds__(256) k_flux(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ FS,
+__global__ void __launch_bounds__(256, E2D_MINB_FLUX) k_flux(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ FS,
                                               V4<T> *__restrict__ res, const Ctl *__restrict__ ctl) {
     if (ctl->halt) return;
     const int n = m.n;

@@ -120,6 +120,7 @@ int build_topology(e2d_mesh *m, double wall_box) {
         for (int e = 0; e < NE; e++)
             if (elog[e] == lg) newid[e + 1] = j++;
     t.nedge = NE; t.nwall = nw; t.nfar = nf;
+    t.pre2post = newid;
     for (auto *v : {&t.elog, &t.eleft, &t.eright, &t.efar, &t.ewall, &t.en1, &t.en2}) v->assign(NE, 0);
     for (auto *v : {&t.evn, &t.evx, &t.evy, &t.emx, &t.emy}) v->assign(NE, 0.0);
     for (int e = 0; e < NE; e++) {

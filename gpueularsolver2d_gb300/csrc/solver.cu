@@ -298,6 +298,23 @@ int build_graph(e2d_solver *s) {
     return E2D_OK;
 }
 
+// Copies the residuals of iterations completed since the last call into the
+// host history; with verbose set, prints them as the reference does
+// ("%d,%1.20lf", gpu_solver.cu:2433).  The stream must be synchronised.
+int sync_hist(e2d_solver *s) {
+    const int step = s->ctl_host->step;
+    const int have = (int)s->hist.size();
+    if (step <= have) return E2D_OK;
+    s->hist.resize(step);
+    CK(cudaMemcpy(s->hist.data() + have, s->hist_dev + have, sizeof(double) * (step - have),
+                  cudaMemcpyDeviceToHost));
+    if (s->prm.verbose) {
+        for (int k = have; k < step; k++) std::printf("%d,%1.20lf\n", k + 1, s->hist[k]);
+        std::fflush(stdout);
+    }
+    return E2D_OK;
+}
+
 // Runs up to n iterations (fewer if the residual test stops the loop).
 int run(e2d_solver *s, int n, bool check, double epsl, int poll_every) {
     if (n <= 0) return E2D_OK;
@@ -317,6 +334,7 @@ int run(e2d_solver *s, int n, bool check, double epsl, int poll_every) {
         CK(cudaGraphLaunch(s->gexec, s->stream));
         if (check && poll_every > 0 && (k + 1) % poll_every == 0 && k + 1 < launches) {
             if ((rc = pull_ctl(s))) return rc;
+            if ((rc = sync_hist(s))) return rc;
             if (c.halt) break;
         }
     }
@@ -325,12 +343,7 @@ int run(e2d_solver *s, int n, bool check, double epsl, int poll_every) {
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
     s->last_ms = ms;
-    int have = (int)s->hist.size();
-    if (c.step > have) {
-        s->hist.resize(c.step);
-        CK(cudaMemcpy(s->hist.data() + have, s->hist_dev + have, sizeof(double) * (c.step - have),
-                      cudaMemcpyDeviceToHost));
-    }
+    if ((rc = sync_hist(s))) return rc;
     if (c.halt == 2) {
         set_error("solution diverged: non-positive density or pressure (or NaN) at step " + std::to_string(c.step));
         return E2D_ERR_DIVERGED;
@@ -417,8 +430,6 @@ int e2d_solve(e2d_solver *s, int32_t max_steps, double epsl, double *resid_histo
     const int done = s->ctl_host->step - step0;
     if (nsteps) *nsteps = done;
     if (resid_history) std::memcpy(resid_history, s->hist.data() + step0, sizeof(double) * done);
-    if (s->prm.verbose)
-        for (int k = step0; k < step0 + done; k++) std::printf("%d,%1.20lf\n", k + 1, s->hist[k]);
     return rc;
 }
 
@@ -485,12 +496,7 @@ int e2d_profile_passes(e2d_solver *s, int32_t iters, double *ms, int32_t *launch
     }
     for (auto &e : ev) cudaEventDestroy(e);
     if ((rc = pull_ctl(s))) return rc;
-    int have = (int)s->hist.size();
-    if (c.step > have) {
-        s->hist.resize(c.step);
-        CK(cudaMemcpy(s->hist.data() + have, s->hist_dev + have, sizeof(double) * (c.step - have),
-                      cudaMemcpyDeviceToHost));
-    }
+    if ((rc = sync_hist(s))) return rc;
     return c.halt == 2 ? E2D_ERR_DIVERGED : E2D_OK;
 }
 
@@ -526,6 +532,12 @@ int e2d_write_residual_plt(e2d_solver *s, const char *path) {
     for (int i = 1; i <= step; i++)
         if (i % 100 == 0) std::fprintf(fp, "%d %20.10lf\n", i, s->hist[i - 1]);
     std::fclose(fp);
+    return E2D_OK;
+}
+
+int e2d_get_params(e2d_solver *s, e2d_params *p) {
+    if (!s || !p) { set_error("null argument"); return E2D_ERR_ARG; }
+    *p = s->prm;
     return E2D_OK;
 }
 

@@ -160,6 +160,15 @@ int e2d_forces(e2d_solver *s, double *cl, double *cd);
 /* unresidual.plt as the reference writes it (gpu_fvm.cu:165-175): every
  * 100th step. */
 int e2d_write_residual_plt(e2d_solver *s, const char *path);
+/* unresult.plt (gpu_fvm.cu:143-163): area-weighted node averages of rho,
+ * u, v, P, T and Mach (Node_Computing, gpu_fvm.cu:71-131) of the solver's
+ * current state on mesh m (the mesh the solver was created from). */
+int e2d_write_field_plt(e2d_solver *s, e2d_mesh *m, const char *path);
+/* unairfoilpress.plt (gpu_fvm.cu:177-192): -2 (P - P_inf) at both nodes of
+ * every wall face, in wall-face order. */
+int e2d_write_wall_cp_plt(e2d_solver *s, e2d_mesh *m, const char *path);
+/* Parameters the solver was created with. */
+int e2d_get_params(e2d_solver *s, e2d_params *p);
 /* Device time of the kernels of the last e2d_step/e2d_solve call, ms,
  * measured with CUDA events on the solver's stream. */
 int e2d_last_device_ms(e2d_solver *s, double *ms);

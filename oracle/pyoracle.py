@@ -208,7 +208,8 @@ def run_reference(mode: str, mesh_path: str, input_line: str, w_in: np.ndarray |
                          ("cell_i", np.int32), ("cell_d", np.float64), ("w_init", np.float64),
                          ("pis", np.float64), ("flux_raw", np.float64), ("ghost", np.float64),
                          ("grad", np.float64), ("umm", np.float64), ("sr_sum", np.float64),
-                         ("gpu_counts", np.int32), ("gpu_w", np.float64)]:
+                         ("gpu_counts", np.int32), ("gpu_w", np.float64),
+                         ("wall_i", np.int32), ("nlog", np.int32)]:
             p = os.path.join(d, name + ".bin")
             if os.path.exists(p):
                 out[name] = np.fromfile(p, dt)

@@ -10,6 +10,8 @@
  * mesh under that name.  Outputs are raw little-endian binary files written
  * into the same directory.
  *
+ *   ref_harness geo0  DIR  -- inputMesh, Initialization, CalculationMeshGeo;
+ *                             dump the set-up, WallEdge list and node flags
  *   ref_harness geo   DIR  -- inputMesh, Initialization, CalculationMeshGeo,
  *                             changeEdge; dump the set-up
  *   ref_harness stage DIR  -- geo, then the reference's host Boundary,
@@ -70,7 +72,7 @@ static void dump(const char *name, const void *p, size_t bytes) {
     fclose(f);
 }
 
-static void setup() {
+static void setup(bool partition = true) {
     /* gpu_fvm.cu:31-40 */
     inputMesh(&cell, &node);
     w = (W *)calloc(Ncell + 1, sizeof(W));
@@ -80,7 +82,23 @@ static void setup() {
     WallEdge = (EDGE *)calloc(Ncell + 1, sizeof(EDGE));
     Initialization(w);
     CalculationMeshGeo(cell, node, edge, WallEdge);
-    changeEdge();
+    if (partition) changeEdge();
+}
+
+/* WallEdge list and wall-node flags as CalculationMeshGeo leaves them */
+static void dump_walls() {
+    int *wi = (int *)malloc(sizeof(int) * 7 * (WallBoundNum + 1));
+    for (int k = 1; k <= WallBoundNum; k++) {
+        int *o = wi + 7 * (k - 1);
+        o[0] = WallEdge[k].ELog; o[1] = WallEdge[k].left_cell; o[2] = WallEdge[k].right_cell;
+        o[3] = WallEdge[k].farfieldid; o[4] = WallEdge[k].wallid; o[5] = WallEdge[k].node1;
+        o[6] = WallEdge[k].node2;
+    }
+    dump("wall_i.bin", wi, sizeof(int) * 7 * WallBoundNum);
+    int *nl = (int *)malloc(sizeof(int) * Nnode);
+    for (int n = 1; n <= Nnode; n++) nl[n - 1] = node[n].NLog;
+    dump("nlog.bin", nl, sizeof(int) * Nnode);
+    free(wi); free(nl);
 }
 
 static void dump_setup() {
@@ -170,6 +188,12 @@ static void run_stage() {
 int main(int argc, char **argv) {
     if (argc < 3) { fprintf(stderr, "usage: ref_harness geo|stage|gpu DIR\n"); return 2; }
     if (chdir(argv[2]) != 0) { fprintf(stderr, "cannot enter %s\n", argv[2]); return 2; }
+    if (!strcmp(argv[1], "geo0")) {  /* CalculationMeshGeo without changeEdge */
+        setup(false);
+        dump_setup();
+        dump_walls();
+        return 0;
+    }
     if (!strcmp(argv[1], "geo") || !strcmp(argv[1], "stage")) {
         setup();
         dump_setup();
