@@ -83,6 +83,7 @@ SIGNATURES = {
     "e2d_launches_per_iteration": (_I, [_P, _PI]),
     "e2d_profile_passes": (_I, [_P, _I, _PD, _PI]),
     "e2d_set_stream": (_I, [_P, _P]),
+    "e2d_step_noalloc": (_I, [_I, _P, _P, _P, _P, ctypes.POINTER(Params), _I, _P, _P, _PD, _P]),
 }
 
 _lib = None

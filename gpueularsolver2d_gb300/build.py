@@ -35,6 +35,7 @@ UNITS = {
     "solver.o": ("solver.cu", ["nvcc", *NVCC_COMMON]),
     "resid.o": ("resid.cu", ["nvcc", *NVCC_COMMON]),
     "kernels_f64.o": ("kernels_f64.cu", ["nvcc", *NVCC_COMMON, "--fmad=false"]),
+    "noalloc.o": ("noalloc.cu", ["nvcc", *NVCC_COMMON, "--fmad=false"]),
     "kernels_f32.o": ("kernels_f32.cu", ["nvcc", *NVCC_COMMON, "--fmad=true",
                                           "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
 }
@@ -65,6 +66,13 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     os.makedirs(OBJDIR, exist_ok=True)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "euler2d.h"),
                                                        __file__]
+    # rebuild everything when the extra nvcc flags differ from the last build
+    stamp = os.path.join(OBJDIR, "nvcc_extra.txt")
+    extra = os.environ.get("E2D_NVCC_EXTRA", "")
+    if not os.path.exists(stamp) or open(stamp).read() != extra:
+        force = True
+        with open(stamp, "w") as f:
+            f.write(extra)
     todo = []
     for obj, (src, cmd) in UNITS.items():
         deps = [os.path.join(CSRC, src), *hdrs]

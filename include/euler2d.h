@@ -184,6 +184,47 @@ int e2d_profile_passes(e2d_solver *s, int32_t iters, double *ms, int32_t *launch
 /* Sets the CUDA stream used by the solver (default: a stream it owns). */
 int e2d_set_stream(e2d_solver *s, void *cuda_stream);
 
+/* ---- iterations without allocation ------------------------------------ */
+/* Largest mesh e2d_step_noalloc accepts. */
+#define E2D_NOALLOC_MAX_CELLS 32768
+/* Runs `iterations` FP64 iterations of the solve path, like e2d_step, for a
+ * caller that may not allocate device memory -- for example a plug-in whose
+ * host application owns every device allocation and hands it buffers from its
+ * own pool.  No counterpart in the reference.
+ *
+ * It calls no cudaMalloc / cudaFree and no allocating library routine: the
+ * per-iteration working arrays live in one fixed device array of the library
+ * sized for E2D_NOALLOC_MAX_CELLS cells (about 7.7 MB), which every GPU that
+ * loads the library keeps until the process exits.  Meshes with more cells
+ * are rejected with E2D_ERR_CAPACITY.
+ *
+ * The caller passes, all in device memory, the mesh in the solver's cell-local
+ * layout for some cell order of its choice (n = ncell, cells 0..n-1):
+ *   topo [4n] int32, 16-byte aligned: per cell the three face codes and the
+ *        number of interior neighbours; face k joins Point[(k+1)%3] and
+ *        Point[(k+2)%3]; its code is (nb << 3) | (right << 2) | slot for an
+ *        interior neighbour nb (right = 1 when this cell is the edge's
+ *        right_cell in the reference numbering, slot = the face index of the
+ *        same edge in nb), -1 for a far-field face, -2 for a wall face;
+ *   S    [6n] double, 16-byte aligned: S[2(k n + i) + {0,1}] = (vectory,
+ *        vectorx) of face k in cell i's own node order (gpu_init.cu:153-154);
+ *   R    [6n] double, 16-byte aligned: face midpoint minus cell centroid;
+ *   area [n]  double;
+ * the state w [4n] (rho, rho u, rho v, rho E per cell, 32-byte aligned),
+ * advanced in place, and resid [iterations] receiving Resd of each iteration.
+ * *epsm is the residual normalisation: <= 0 on entry takes drou of this call's
+ * first iteration (gpu_solver.cu:2428); the value used is returned in *epsm,
+ * so passing it back continues one residual history across calls.
+ *
+ * The call is synchronous on `stream` (NULL: the legacy default stream).  The
+ * first call on each device looks up the array's device address (with that
+ * device current) and may load the module; make it before any stream capture.
+ * All calls share the one array and it keeps the last call's contents: calls
+ * whose work overlaps on a GPU race with each other. */
+int e2d_step_noalloc(int32_t ncell, const int32_t *topo, const double *S, const double *R,
+                     const double *area, const e2d_params *p, int32_t iterations, double *w,
+                     double *resid, double *epsm, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
