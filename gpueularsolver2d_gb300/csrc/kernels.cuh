@@ -38,16 +38,15 @@ namespace e2d {
 #ifndef E2D_MINB_FLUX
 #define E2D_MINB_FLUX 6
 #endif
-#if E2D_MINB_FACES > 0
-#define E2D_LB_FACES __launch_bounds__(256, E2D_MINB_FACES)
-#else
-#define E2D_LB_FACES __launch_bounds__(256)
-#endif
-#if E2D_MINB_FLUX > 0
-#define E2D_LB_FLUX __launch_bounds__(256, E2D_MINB_FLUX)
-#else
-#define E2D_LB_FLUX __launch_bounds__(256)
-#endif
+// The targets apply to the FP32 kernels; the FP64 (parity) kernels keep two
+// blocks, enough registers for their ~100 live doubles without spilling.
+template <typename T> struct MinBlocks { static constexpr int faces = 2, flux = 2; };
+template <> struct MinBlocks<float> {
+    static constexpr int faces = E2D_MINB_FACES > 0 ? E2D_MINB_FACES : 1;
+    static constexpr int flux = E2D_MINB_FLUX > 0 ? E2D_MINB_FLUX : 1;
+};
+#define E2D_LB_FACES __launch_bounds__(256, MinBlocks<T>::faces)
+#define E2D_LB_FLUX __launch_bounds__(256, MinBlocks<T>::flux)
 
 template <typename T> __device__ __forceinline__ T tabs(T v) { return fabs(v); }
 template <typename T> __device__ __forceinline__ T tsqrt(T v) { return sqrt(v); }
