@@ -84,6 +84,21 @@ SIGNATURES = {
     "e2d_profile_passes": (_I, [_P, _I, _PD, _PI]),
     "e2d_set_stream": (_I, [_P, _P]),
     "e2d_step_noalloc": (_I, [_I, _P, _P, _P, _P, ctypes.POINTER(Params), _I, _P, _P, _PD, _P]),
+    "e2d_batch_create": (_I, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Params), _I, _PP]),
+    "e2d_batch_destroy": (None, [_P]),
+    "e2d_batch_step": (_I, [_P, _I]),
+    "e2d_batch_solve": (_I, [_P, _I, _D, _PI]),
+    "e2d_batch_info": (_I, [_P, _PI, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
+    "e2d_batch_get_state": (_I, [_P, _I, _PD]),
+    "e2d_batch_set_state": (_I, [_P, _I, _PD]),
+    "e2d_batch_progress": (_I, [_P, _I, _PI, _PD, _PI]),
+    "e2d_batch_residual_history": (_I, [_P, _I, _PD, _I, _PI]),
+    "e2d_batch_forces": (_I, [_P, _I, _PD, _PD]),
+    "e2d_batch_set_launch": (_I, [_P, _I, _I]),
+    "e2d_batch_get_launch": (_I, [_P, _PI, _PI]),
+    "e2d_batch_autotune": (_I, [_P, ctypes.c_char_p, _I, _PI, _PI, _PD]),
+    "e2d_batch_last_device_ms": (_I, [_P, _PD]),
+    "e2d_batch_launches_per_iteration": (_I, [_P, _PI]),
 }
 
 _lib = None

@@ -12,7 +12,7 @@ import numpy as np
 from ._lib import (E2D_FP32, E2D_FP64, E2D_ORDER_FILE, E2D_ORDER_MORTON, MeshInfo, Params,
                    check, load)
 
-__all__ = ["Mesh", "Solver", "Params", "default_params", "read_input", "E2D_FP32", "E2D_FP64",
+__all__ = ["Mesh", "Solver", "Batch", "Params", "default_params", "read_input", "E2D_FP32", "E2D_FP64",
            "E2D_ORDER_FILE", "E2D_ORDER_MORTON"]
 
 
@@ -196,6 +196,103 @@ class Solver:
     def close(self) -> None:
         if self._h:
             load().e2d_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent cases advanced together (e2d_batch_* in include/euler2d.h)."""
+
+    def __init__(self, meshes, params):
+        self.meshes = list(meshes)
+        self.params = list(params)
+        n = len(self.meshes)
+        handles = (ctypes.c_void_p * n)(*[m._h.value for m in self.meshes])
+        parr = (Params * n)(*self.params)
+        h = ctypes.c_void_p()
+        check(load().e2d_batch_create(handles, parr, n, ctypes.byref(h)))
+        self._h = h
+        self.ncells = [m.info(p.wall_box).ncell for m, p in zip(self.meshes, self.params)]
+
+    def step(self, n: int) -> None:
+        check(load().e2d_batch_step(self._h, n))
+
+    def solve(self, max_steps: int, epsl: float) -> np.ndarray:
+        out = np.zeros(len(self.meshes), np.int32)
+        check(load().e2d_batch_solve(self._h, max_steps, epsl, _ip(out)))
+        return out
+
+    def info(self):
+        nc = ctypes.c_int32()
+        nt = ctypes.c_int64()
+        npad = ctypes.c_int64()
+        check(load().e2d_batch_info(self._h, ctypes.byref(nc), ctypes.byref(nt), ctypes.byref(npad)))
+        return nc.value, nt.value, npad.value
+
+    def state(self, c: int) -> np.ndarray:
+        w = np.zeros((self.ncells[c], 4))
+        check(load().e2d_batch_get_state(self._h, c, _dp(w)))
+        return w
+
+    def set_state(self, c: int, w) -> None:
+        w = np.ascontiguousarray(w, np.float64).reshape(self.ncells[c], 4)
+        check(load().e2d_batch_set_state(self._h, c, _dp(w)))
+
+    def progress(self, c: int):
+        st = ctypes.c_int32()
+        r = ctypes.c_double()
+        hl = ctypes.c_int32()
+        check(load().e2d_batch_progress(self._h, c, ctypes.byref(st), ctypes.byref(r), ctypes.byref(hl)))
+        return st.value, r.value, hl.value
+
+    def history(self, c: int) -> np.ndarray:
+        n = ctypes.c_int32()
+        check(load().e2d_batch_residual_history(self._h, c, None, 0, ctypes.byref(n)))
+        out = np.zeros(max(1, n.value))
+        check(load().e2d_batch_residual_history(self._h, c, _dp(out), n.value, ctypes.byref(n)))
+        return out[: n.value]
+
+    def forces(self, c: int):
+        cl = ctypes.c_double()
+        cd = ctypes.c_double()
+        check(load().e2d_batch_forces(self._h, c, ctypes.byref(cl), ctypes.byref(cd)))
+        return cl.value, cd.value
+
+    def set_launch(self, block: int, grid: int = 0) -> None:
+        check(load().e2d_batch_set_launch(self._h, block, grid))
+
+    def launch(self):
+        b = ctypes.c_int32()
+        g = ctypes.c_int32()
+        check(load().e2d_batch_get_launch(self._h, ctypes.byref(b), ctypes.byref(g)))
+        return b.value, g.value
+
+    def autotune(self, cache_path: str | None = None, iters: int = 16):
+        b = ctypes.c_int32()
+        g = ctypes.c_int32()
+        ms = ctypes.c_double()
+        check(load().e2d_batch_autotune(self._h, cache_path.encode() if cache_path else None, iters,
+                                        ctypes.byref(b), ctypes.byref(g), ctypes.byref(ms)))
+        return b.value, g.value, ms.value
+
+    def last_device_ms(self) -> float:
+        v = ctypes.c_double()
+        check(load().e2d_batch_last_device_ms(self._h, ctypes.byref(v)))
+        return v.value
+
+    def launches_per_iteration(self) -> int:
+        v = ctypes.c_int32()
+        check(load().e2d_batch_launches_per_iteration(self._h, ctypes.byref(v)))
+        return v.value
+
+    def close(self) -> None:
+        if self._h:
+            load().e2d_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

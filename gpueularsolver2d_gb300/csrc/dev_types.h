@@ -64,6 +64,48 @@ template <typename T> int launches_per_iteration(const Plan<T> &p) {
     return p.stages * (3 + (p.sweeps > 1 ? p.sweeps - 1 : 0)) + 1;
 }
 
+// Batched cases: the cells of all cases in one array, case c in
+// [off_c, off_c + n_c) with off_c a multiple of kChunk, so that a tile of B
+// cells (B dividing kChunk) lies in one case.  Padding cells are skipped.
+constexpr int kChunk = 256;
+
+template <typename T> struct BatchDev {
+    const Flow<T> *flows;    // [ncase]
+    const int *chunk_case;   // [n / kChunk] case of each chunk
+    const int *case_end;     // [ncase] one past the last real cell
+    Ctl *ctl;                // [ncase]
+};
+
+template <typename T> struct BPlan {
+    MeshDev<T> m;            // concatenated mesh (n includes padding)
+    Flow<T> f;               // parameters shared by all cases (gamma, irs_eps, ...)
+    BatchDev<T> b;
+    V4<T> *W[2];
+    V4<T> *FS;
+    T *dt;
+    V4<T> *res;
+    V4<T> *sm[2];
+    double *part;            // [tiles] one partial per tile
+    int ncase;
+    const int2 *case_tiles;  // [ncase] {first tile, tile count}
+    double *hist;            // [ncase * hist_cap]
+    int hist_cap;
+    int stages;
+    T rk[8];
+    int sweeps;
+    int block;               // cells per tile = threads per CTA
+    int grid;                // CTAs per launch (persistent when < tiles)
+};
+
+template <typename T> int launches_per_iteration(const BPlan<T> &p) {
+    return p.stages * (3 + (p.sweeps > 1 ? p.sweeps - 1 : 0)) + 1;
+}
+
+template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream_t s);
+
+void enqueue_batch_resid(const double *part, const int2 *case_tiles, int ncase, Ctl *ctl, double *hist,
+                         int hist_cap, cudaStream_t s);
+
 // Enqueue one iteration (all RK stages + the residual) on a stream.
 // Instantiated for double in kernels_f64.cu and for float in kernels_f32.cu.
 template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s);

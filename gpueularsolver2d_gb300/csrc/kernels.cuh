@@ -224,13 +224,10 @@ __device__ __forceinline__ V4<T> roe(const V4<T> &LW, const V4<T> &RW, T nx, T n
 // reconstruction for an interior face, the cell state itself for a boundary
 // face (the reference's boundary faces are first order).
 template <typename T>
-__global__ void E2D_LB_FACES k_faces(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ W,
-                                               V4<T> *__restrict__ FS, T *__restrict__ dt,
-                                               const Ctl *__restrict__ ctl) {
-    if (ctl->halt) return;
+__device__ __forceinline__ void faces_cell(const MeshDev<T> &m, const Flow<T> &f, const int i,
+                                           const V4<T> *__restrict__ W, V4<T> *__restrict__ FS,
+                                           T *__restrict__ dt) {
     const int n = m.n;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
     const int4 tp = m.topo[i];
     const int code[3] = {tp.x, tp.y, tp.z};
     const V4<T> U = W[i];
@@ -293,17 +290,24 @@ __global__ void E2D_LB_FACES k_faces(MeshDev<T> m, Flow<T> f, const V4<T> *__res
     dt[i] = tmin(A * f.cfl / Tsum, f.dt_cap);
 }
 
+template <typename T>
+__global__ void E2D_LB_FACES k_faces(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ W,
+                                     V4<T> *__restrict__ FS, T *__restrict__ dt,
+                                     const Ctl *__restrict__ ctl) {
+    if (ctl->halt) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.n) return;
+    faces_cell(m, f, i, W, FS, dt);
+}
+
 // ---------------------------------------------------------------------------
 // Pass B: gpu_solver.cu:651-764 (kernel_Flux2) evaluated per cell for its
 // three faces, summed as gpu_solver.cu:798-825 (+F where the cell is the
 // edge's left cell, -F where it is the right cell, in face order).
 template <typename T>
-__global__ void E2D_LB_FLUX k_flux(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ FS,
-                                              V4<T> *__restrict__ res, const Ctl *__restrict__ ctl) {
-    if (ctl->halt) return;
+__device__ __forceinline__ void flux_cell(const MeshDev<T> &m, const Flow<T> &f, const int i,
+                                          const V4<T> *__restrict__ FS, V4<T> *__restrict__ res) {
     const int n = m.n;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
     const int4 tp = m.topo[i];
     const int code[3] = {tp.x, tp.y, tp.z};
     V4<T> r;
@@ -333,6 +337,15 @@ __global__ void E2D_LB_FLUX k_flux(MeshDev<T> m, Flow<T> f, const V4<T> *__restr
     res[i] = r;
 }
 
+template <typename T>
+__global__ void E2D_LB_FLUX k_flux(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ FS,
+                                   V4<T> *__restrict__ res, const Ctl *__restrict__ ctl) {
+    if (ctl->halt) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.n) return;
+    flux_cell(m, f, i, FS, res);
+}
+
 // Sum of the interior neighbours' values in face order (gpu_solver.cu:1658-1666)
 template <typename T>
 __device__ __forceinline__ V4<T> nb_sum(const int4 tp, const V4<T> *__restrict__ src) {
@@ -352,12 +365,9 @@ __device__ __forceinline__ V4<T> nb_sum(const int4 tp, const V4<T> *__restrict__
 // Pass C: gpu_solver.cu:1635-1673 (kernel_Smooth1): one Jacobi-type sweep
 // dst = (eps * sum_interior src + res) / (1 + eps * CLog).
 template <typename T>
-__global__ void __launch_bounds__(256) k_smooth(MeshDev<T> m, T eps, const V4<T> *__restrict__ src,
-                                                const V4<T> *__restrict__ res, V4<T> *__restrict__ dst,
-                                                const Ctl *__restrict__ ctl) {
-    if (ctl->halt) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.n) return;
+__device__ __forceinline__ void smooth_cell(const MeshDev<T> &m, const T eps, const int i,
+                                            const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
+                                            V4<T> *__restrict__ dst) {
     const int4 tp = m.topo[i];
     const V4<T> d = nb_sum(tp, src);
     const V4<T> r0 = res[i];
@@ -370,20 +380,27 @@ __global__ void __launch_bounds__(256) k_smooth(MeshDev<T> m, T eps, const V4<T>
     dst[i] = o;
 }
 
+template <typename T>
+__global__ void __launch_bounds__(256) k_smooth(MeshDev<T> m, T eps, const V4<T> *__restrict__ src,
+                                                const V4<T> *__restrict__ res, V4<T> *__restrict__ dst,
+                                                const Ctl *__restrict__ ctl) {
+    if (ctl->halt) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.n) return;
+    smooth_cell(m, eps, i, src, res, dst);
+}
+
 // ---------------------------------------------------------------------------
 // Pass D: gpu_solver.cu:1675-1720 (kernel_Smooth2, last sweep + clamp) fused
 // with 938-966 (kernel_RKStep); on the last stage also 968-1020 (kernel_drou)
 // as FP64 block partials and a count of unphysical cells.
 template <typename T>
-__global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, int smooth,
-                                                const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
-                                                const T *__restrict__ dt, const V4<T> *W0, V4<T> *Wout,
-                                                double *__restrict__ part, Ctl *ctl) {
-    if (ctl->halt) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double d2 = 0.0;
-    int bad = 0;
-    if (i < m.n) {
+__device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &f, const T rk,
+                                            const int smooth, const int i, const V4<T> *__restrict__ src,
+                                            const V4<T> *__restrict__ res, const T *__restrict__ dt,
+                                            const V4<T> *W0, V4<T> *Wout, const bool want, double &d2,
+                                            int &bad) {
+    {
         const int4 tp = m.topo[i];
         V4<T> r = res[i];
         if (smooth) {
@@ -407,30 +424,139 @@ __global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, i
         w.z = w0.z - RK * r.z / A;
         w.w = w0.w - RK * r.w / A;
         Wout[i] = w;
-        if (part) {
+        if (want) {
             double dd = (double)w.x - (double)w0.x;
             d2 = dd * dd;
             double q = 0.5 * ((double)w.y * (double)w.y + (double)w.z * (double)w.z) / (double)w.x;
             bad = !(w.x > T(0)) || !((double)w.w - q > 0.0);
         }
     }
-    if (!part) return;
-    // deterministic block reduction: fixed shuffle tree, then warps in order
+}
+
+// Deterministic block sum of d2 (fixed shuffle tree, then the warps in order)
+// into *slot, and the count of unphysical cells added to *nbad.  Every thread
+// of the block must call it.
+__device__ __forceinline__ void block_partial(double d2, int bad, double *slot, int *nbad) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) d2 += __shfl_down_sync(0xffffffffu, d2, o);
     unsigned badmask = __ballot_sync(0xffffffffu, bad);
     __shared__ double ws[32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();  // ws may still be read by the previous use in this block
     if (lane == 0) {
         ws[wid] = d2;
-        if (badmask) atomicAdd(&ctl->nbad, __popc(badmask));
+        if (badmask) atomicAdd(nbad, __popc(badmask));
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         double s = 0.0;
         for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += ws[k];
-        part[blockIdx.x] = s;
+        *slot = s;
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, int smooth,
+                                                const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
+                                                const T *__restrict__ dt, const V4<T> *W0, V4<T> *Wout,
+                                                double *__restrict__ part, Ctl *ctl) {
+    if (ctl->halt) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double d2 = 0.0;
+    int bad = 0;
+    if (i < m.n) update_cell(m, f, rk, smooth, i, src, res, dt, W0, Wout, part != nullptr, d2, bad);
+    if (!part) return;
+    block_partial(d2, bad, part + blockIdx.x, &ctl->nbad);
+}
+
+// ---------------------------------------------------------------------------
+// Batched cases: the same per-cell work as the kernels above, by persistent
+// CTAs that walk the tiles of all cases (tile = blockDim.x consecutive cells,
+// all of one case).  Cells of halted (converged) cases and padding cells are
+// skipped; each cell uses the flow constants of its own case.
+template <typename T>
+__device__ __forceinline__ bool batch_cell(const BatchDev<T> &b, const int n, const int i, int &c) {
+    if (i >= n) return false;
+    c = b.chunk_case[i / kChunk];
+    return i < b.case_end[c] && !b.ctl[c].halt;
+}
+
+template <typename T>
+__global__ void E2D_LB_FACES kb_faces(MeshDev<T> m, BatchDev<T> b, int ntiles, const V4<T> *__restrict__ W,
+                                      V4<T> *__restrict__ FS, T *__restrict__ dt) {
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int i = t * blockDim.x + threadIdx.x;
+        int c;
+        if (batch_cell(b, m.n, i, c)) {
+            const Flow<T> f = b.flows[c];
+            faces_cell(m, f, i, W, FS, dt);
+        }
+    }
+}
+
+template <typename T>
+__global__ void E2D_LB_FLUX kb_flux(MeshDev<T> m, BatchDev<T> b, int ntiles, const V4<T> *__restrict__ FS,
+                                    V4<T> *__restrict__ res) {
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int i = t * blockDim.x + threadIdx.x;
+        int c;
+        if (batch_cell(b, m.n, i, c)) {
+            const Flow<T> f = b.flows[c];
+            flux_cell(m, f, i, FS, res);
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) kb_smooth(MeshDev<T> m, BatchDev<T> b, int ntiles, T eps,
+                                                 const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
+                                                 V4<T> *__restrict__ dst) {
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int i = t * blockDim.x + threadIdx.x;
+        int c;
+        if (batch_cell(b, m.n, i, c)) smooth_cell(m, eps, i, src, res, dst);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) kb_update(MeshDev<T> m, BatchDev<T> b, int ntiles, T rk, int smooth,
+                                                 const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
+                                                 const T *__restrict__ dt, const V4<T> *W0, V4<T> *Wout,
+                                                 double *__restrict__ part) {
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int tc = b.chunk_case[(t * blockDim.x) / kChunk];  // the tile's case
+        if (b.ctl[tc].halt) continue;                             // uniform over the block
+        const int i = t * blockDim.x + threadIdx.x;
+        double d2 = 0.0;
+        int bad = 0, c;
+        if (batch_cell(b, m.n, i, c)) {
+            const Flow<T> f = b.flows[c];
+            update_cell(m, f, rk, smooth, i, src, res, dt, W0, Wout, part != nullptr, d2, bad);
+        }
+        if (part) block_partial(d2, bad, part + t, &b.ctl[tc].nbad);
+    }
+}
+
+// One iteration of every case that has not halted; the same stage / buffer
+// sequence as enqueue_iteration.
+template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream_t s) {
+    const int B = p.block, NT = (p.m.n + B - 1) / B, G = p.grid;
+    for (int st = 0; st < p.stages; st++) {
+        const bool last = st == p.stages - 1;
+        V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
+        V4<T> *Wout = last ? p.W[0] : p.W[1];
+        kb_faces<T><<<G, B, 0, s>>>(p.m, p.b, NT, Wcur, p.FS, p.dt);
+        kb_flux<T><<<G, B, 0, s>>>(p.m, p.b, NT, p.FS, p.res);
+        const V4<T> *src = p.res;
+        for (int sw = 0; sw + 1 < p.sweeps; sw++) {
+            V4<T> *dst = p.sm[sw & 1];
+            kb_smooth<T><<<G, B, 0, s>>>(p.m, p.b, NT, p.f.irs_eps, src, p.res, dst);
+            src = dst;
+        }
+        kb_update<T><<<G, B, 0, s>>>(p.m, p.b, NT, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt, p.W[0],
+                                     Wout, last ? p.part : nullptr);
+    }
+    enqueue_batch_resid(p.part, p.case_tiles, p.ncase, p.b.ctl, p.hist, p.hist_cap, s);
 }
 
 // ---------------------------------------------------------------------------

@@ -8,9 +8,8 @@ namespace e2d {
 // the caller fixed it.  Sets halt when the loop condition of
 // gpu_solver.cu:2200 (step < MAXSTEP && Resd > EPSL) fails or the state went
 // unphysical.  One block of 256 threads.
-__global__ void __launch_bounds__(256) k_resid(const double *__restrict__ part, int nparts, Ctl *ctl,
-                                               double *hist, int hist_cap) {
-    if (ctl->halt) return;
+__device__ __forceinline__ void resid_block(const double *__restrict__ part, int nparts, Ctl *ctl,
+                                            double *hist, int hist_cap) {
     __shared__ double sh[256];
     double s = 0.0;
     for (int k = threadIdx.x; k < nparts; k += 256) s += part[k];
@@ -33,9 +32,31 @@ __global__ void __launch_bounds__(256) k_resid(const double *__restrict__ part, 
     else if (step >= ctl->target) ctl->halt = 1;
 }
 
+__global__ void __launch_bounds__(256) k_resid(const double *__restrict__ part, int nparts, Ctl *ctl,
+                                               double *hist, int hist_cap) {
+    if (ctl->halt) return;
+    resid_block(part, nparts, ctl, hist, hist_cap);
+}
+
+// Batched cases: one block per case over that case's tile partials (each
+// case's tiles are numbered from a multiple of the chunk, so the grouping of
+// its partials is the one a single-case run of the same block size uses).
+__global__ void __launch_bounds__(256) kb_resid(const double *__restrict__ part, const int2 *case_tiles,
+                                                Ctl *ctl, double *hist, int hist_cap) {
+    const int c = blockIdx.x;
+    if (ctl[c].halt) return;
+    const int2 ct = case_tiles[c];
+    resid_block(part + ct.x, ct.y, ctl + c, hist + (size_t)c * hist_cap, hist_cap);
+}
+
 void enqueue_resid(const double *part, int nparts, Ctl *ctl, double *hist, int hist_cap,
                    cudaStream_t s) {
     k_resid<<<1, 256, 0, s>>>(part, nparts, ctl, hist, hist_cap);
+}
+
+void enqueue_batch_resid(const double *part, const int2 *case_tiles, int ncase, Ctl *ctl, double *hist,
+                         int hist_cap, cudaStream_t s) {
+    kb_resid<<<ncase, 256, 0, s>>>(part, case_tiles, ctl, hist, hist_cap);
 }
 
 }  // namespace e2d

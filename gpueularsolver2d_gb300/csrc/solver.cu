@@ -14,7 +14,7 @@
 #include <vector>
 
 #include "dev_types.h"
-#include "internal.h"
+#include "solver_internal.h"
 
 using namespace e2d;
 
@@ -33,12 +33,6 @@ namespace e2d {
 static const double kR = 287.06;
 static const double kPi = 3.14159265358979;
 
-// Free-stream constants exactly as Initialization computes them
-// (gpu_init.cu:63-93), including PIS = P of the free-stream cell state.
-struct FreeStream {
-    double alpha, ain, vin, ui, vi, rho_e, pis;
-};
-
 FreeStream free_stream(const e2d_params &p) {
     FreeStream s;
     const double g = p.gamma;
@@ -55,16 +49,6 @@ FreeStream free_stream(const e2d_params &p) {
     s.pis = (g - 1.0) * d * E;
     return s;
 }
-
-// Cell-local layout in FP64, internal order.
-struct HostLayout {
-    int n = 0;
-    std::vector<int> perm, iperm;        // internal -> file, file -> internal
-    std::vector<int32_t> topo;           // [4n]
-    std::vector<double> S, R;            // [3n*2] each
-    std::vector<double> area;            // [n]
-    std::vector<int> wall_cell, wall_k;  // internal cell and face of every wall face
-};
 
 int build_layout(e2d_mesh *m, const e2d_params &p, HostLayout &L) {
     int rc = build_topology(m, p.wall_box);
@@ -102,14 +86,31 @@ int build_layout(e2d_mesh *m, const e2d_params &p, HostLayout &L) {
     return E2D_OK;
 }
 
-// Device arena: one cudaMalloc carved into 256-byte aligned pieces.
-struct Arena {
-    char *base = nullptr;
-    size_t cap = 0, used = 0;
-    ~Arena() { if (base) cudaFree(base); }
-    static size_t up(size_t b) { return (b + 255) & ~(size_t)255; }
-    void *take(size_t b) { void *p = base + used; used += up(b); return p; }
-};
+void forces_from_state(const HostLayout &L, const FreeStream &fs, double gamma, const double *w,
+                       double *cl, double *cd) {
+    double fx = 0.0, fy = 0.0;
+    const int n = L.n;
+    for (size_t q = 0; q < L.wall_cell.size(); q++) {
+        const int i = L.wall_cell[q], k = L.wall_k[q];
+        const double *u = &w[4 * (size_t)L.perm[i]];
+        const double p = (gamma - 1.0) * (u[3] - 0.5 * (u[1] * u[1] + u[2] * u[2]) / u[0]);
+        fx += (p - fs.pis) * L.S[2 * ((size_t)k * n + i)];
+        fy += (p - fs.pis) * L.S[2 * ((size_t)k * n + i) + 1];
+    }
+    const double ca = std::cos(fs.alpha), sa = std::sin(fs.alpha);
+    if (cd) *cd = (fx * ca + fy * sa) / 0.5;
+    if (cl) *cl = (-fx * sa + fy * ca) / 0.5;
+}
+
+bool valid_params(const e2d_params *p) {
+    if (!(p->gamma > 1.0) || !(p->ma > 0.0) || !(p->tin > 0.0) || !(p->cfl > 0.0)) return false;
+    if (p->rk_stages < 1 || p->rk_stages > 8 || p->irs_sweeps < 0 || p->irs_sweeps > 16) return false;
+    if (p->precision != E2D_FP64 && p->precision != E2D_FP32) return false;
+    if (p->ordering != E2D_ORDER_FILE && p->ordering != E2D_ORDER_MORTON) return false;
+    if (p->block_size != 0 && (p->block_size < 32 || p->block_size > 256 || p->block_size % 32)) return false;
+    if (p->graph_iters < 0 || p->graph_iters > 256) return false;
+    return true;
+}
 
 struct SolverBase {
     virtual ~SolverBase() {}
@@ -351,16 +352,6 @@ int run(e2d_solver *s, int n, bool check, double epsl, int poll_every) {
     return E2D_OK;
 }
 
-bool valid_params(const e2d_params *p) {
-    if (!(p->gamma > 1.0) || !(p->ma > 0.0) || !(p->tin > 0.0) || !(p->cfl > 0.0)) return false;
-    if (p->rk_stages < 1 || p->rk_stages > 8 || p->irs_sweeps < 0 || p->irs_sweeps > 16) return false;
-    if (p->precision != E2D_FP64 && p->precision != E2D_FP32) return false;
-    if (p->ordering != E2D_ORDER_FILE && p->ordering != E2D_ORDER_MORTON) return false;
-    if (p->block_size != 0 && (p->block_size < 32 || p->block_size > 256 || p->block_size % 32)) return false;
-    if (p->graph_iters < 0 || p->graph_iters > 256) return false;
-    return true;
-}
-
 }  // namespace
 
 extern "C" {
@@ -505,19 +496,7 @@ int e2d_forces(e2d_solver *s, double *cl, double *cd) {
     std::vector<double> w(4 * (size_t)s->L.n);
     int rc = e2d_get_state(s, w.data());
     if (rc) return rc;
-    const double g = s->prm.gamma, pinf = s->fs.pis;
-    double fx = 0.0, fy = 0.0;
-    const int n = s->L.n;
-    for (size_t q = 0; q < s->L.wall_cell.size(); q++) {
-        const int i = s->L.wall_cell[q], k = s->L.wall_k[q];
-        const double *u = &w[4 * (size_t)s->L.perm[i]];
-        const double p = (g - 1.0) * (u[3] - 0.5 * (u[1] * u[1] + u[2] * u[2]) / u[0]);
-        fx += (p - pinf) * s->L.S[2 * ((size_t)k * n + i)];
-        fy += (p - pinf) * s->L.S[2 * ((size_t)k * n + i) + 1];
-    }
-    const double ca = std::cos(s->fs.alpha), sa = std::sin(s->fs.alpha);
-    if (cd) *cd = (fx * ca + fy * sa) / 0.5;
-    if (cl) *cl = (-fx * sa + fy * ca) / 0.5;
+    forces_from_state(s->L, s->fs, s->prm.gamma, w.data(), cl, cd);
     return E2D_OK;
 }
 

@@ -184,6 +184,44 @@ int e2d_profile_passes(e2d_solver *s, int32_t iters, double *ms, int32_t *launch
 /* Sets the CUDA stream used by the solver (default: a stream it owns). */
 int e2d_set_stream(e2d_solver *s, void *cuda_stream);
 
+/* ---- batched cases ------------------------------------------------------
+ * Many independent flow cases on meshes of uneven size advanced together on
+ * one GPU: every pass is one launch over all cases, one CUDA graph covers
+ * several iterations of all of them, and each case keeps its own residual
+ * history and convergence test (a converged case stops while the others go
+ * on).  Each case gives the same result, bit for bit, as a single-case solver
+ * with the same parameters and block size.  No reference counterpart. */
+
+/* params[c] of each case; cases must share precision, RK scheme, smoothing,
+ * gamma, entropy fix and dt cap (per case: Mach, alpha, CFL, p, T, mesh).
+ * The residual history holds max(params[].maxstep, 1024) iterations. */
+int e2d_batch_create(e2d_mesh **meshes, const e2d_params *params, int32_t ncase, e2d_batch **out);
+void e2d_batch_destroy(e2d_batch *b);
+/* Exactly n iterations for every case that has not stopped. */
+int e2d_batch_step(e2d_batch *b, int32_t n);
+/* Each case iterates until its Resd <= epsl or max_steps more iterations;
+ * nsteps[c] (may be NULL) receives the iterations each case ran. */
+int e2d_batch_solve(e2d_batch *b, int32_t max_steps, double epsl, int32_t *nsteps);
+int e2d_batch_info(e2d_batch *b, int32_t *ncase, int64_t *ncell_total, int64_t *ncell_padded);
+int e2d_batch_get_state(e2d_batch *b, int32_t icase, double *w);
+int e2d_batch_set_state(e2d_batch *b, int32_t icase, const double *w);
+/* halted: 0 running, 1 stopped (converged / iteration target), 2 diverged. */
+int e2d_batch_progress(e2d_batch *b, int32_t icase, int32_t *step, double *resd, int32_t *halted);
+int e2d_batch_residual_history(e2d_batch *b, int32_t icase, double *out, int32_t cap, int32_t *n);
+int e2d_batch_forces(e2d_batch *b, int32_t icase, double *cl, double *cd);
+/* Launch shape: threads per CTA (a divisor of 256, >= 32) and CTAs per launch
+ * (0: one per tile; fewer: persistent CTAs walking the tiles). */
+int e2d_batch_set_launch(e2d_batch *b, int32_t block, int32_t grid);
+int e2d_batch_get_launch(e2d_batch *b, int32_t *block, int32_t *grid);
+/* Autotuner: times the candidate launch shapes on `iters` iterations each,
+ * keeps the fastest, and restores the state.  cache_path (may be NULL) is a
+ * JSON file of earlier results keyed by GPU, cell count, case count and
+ * scheme; a hit is applied without timing, a new result is added. */
+int e2d_batch_autotune(e2d_batch *b, const char *cache_path, int32_t iters, int32_t *block, int32_t *grid,
+                       double *ms_per_iter);
+int e2d_batch_last_device_ms(e2d_batch *b, double *ms);
+int e2d_batch_launches_per_iteration(e2d_batch *b, int32_t *n);
+
 /* ---- iterations without allocation ------------------------------------ */
 /* Largest mesh e2d_step_noalloc accepts. */
 #define E2D_NOALLOC_MAX_CELLS 32768
