@@ -33,7 +33,7 @@ class Params(ctypes.Structure):
         ("dt_cap", ctypes.c_double), ("entropy_eps", ctypes.c_double),
         ("wall_box", ctypes.c_double), ("ordering", ctypes.c_int32),
         ("block_size", ctypes.c_int32), ("graph_iters", ctypes.c_int32),
-        ("verbose", ctypes.c_int32),
+        ("verbose", ctypes.c_int32), ("limiter_freeze", ctypes.c_int32),
     ]
 
 

@@ -62,12 +62,14 @@ template <typename T> struct BatchT : BatchBase {
              double *hist, int hist_cap) {
         ntot = ntot_;
         const int n = ntot, ncase = (int)L->size();
+        bool freeze = false;
+        for (auto &p : P) freeze = freeze || p.limiter_freeze > 0;
         int nmax = 0;
         for (auto &l : *L) nmax = std::max(nmax, l.n);
         const int maxtiles = (n + 31) / 32;
         size_t bytes = Arena::up(sizeof(int4) * n) + 2 * Arena::up(sizeof(V2<T>) * 3 * n) +
                        2 * Arena::up(sizeof(T) * n) + 6 * Arena::up(sizeof(V4<T>) * n) +
-                       Arena::up(sizeof(V4<T>) * 3 * n) + Arena::up(sizeof(double) * maxtiles) +
+                       Arena::up(sizeof(V4<T>) * 3 * n) * (freeze ? 2 : 1) + Arena::up(sizeof(double) * maxtiles) +
                        Arena::up(sizeof(int) * n) + Arena::up(sizeof(double) * 4 * nmax) +
                        Arena::up(sizeof(Flow<T>) * ncase) + Arena::up(sizeof(int) * (n / kChunk + 1)) +
                        2 * Arena::up(sizeof(int2) * ncase);
@@ -80,6 +82,7 @@ template <typename T> struct BatchT : BatchBase {
         plan.W[0] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
         plan.W[1] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
         plan.FS = (V4<T> *)arena.take(sizeof(V4<T>) * 3 * n);
+        plan.phi = freeze ? (V4<T> *)arena.take(sizeof(V4<T>) * 3 * n) : nullptr;
         plan.dt = (T *)arena.take(sizeof(T) * n);
         plan.res = (V4<T> *)arena.take(sizeof(V4<T>) * n);
         plan.sm[0] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
@@ -373,7 +376,10 @@ int e2d_batch_create(e2d_mesh **meshes, const e2d_params *params, int32_t ncase,
     CK(cudaMalloc((void **)&b->ctl_dev, sizeof(Ctl) * ncase));
     CK(cudaMallocHost((void **)&b->ctl_host, sizeof(Ctl) * ncase));
     std::memset(b->ctl_host, 0, sizeof(Ctl) * ncase);
-    for (int c = 0; c < ncase; c++) b->ctl_host[c].resd = 100.0;
+    for (int c = 0; c < ncase; c++) {
+        b->ctl_host[c].resd = 100.0;
+        b->ctl_host[c].freeze_after = params[c].limiter_freeze > 0 ? params[c].limiter_freeze : 0;
+    }
     CK(cudaMemcpy(b->ctl_dev, b->ctl_host, sizeof(Ctl) * ncase, cudaMemcpyHostToDevice));
     // the history buffer is sized once here: its pointer is captured in the graph
     int maxstep = 0;

@@ -19,6 +19,8 @@ struct Ctl {
     int nbad;        // cells with rho <= 0, p <= 0 or NaN after the last iteration
     int fixed_norm;  // epsm given by the caller
     double epsl, epsm, resd;
+    int freeze_after;  // > 0: freeze the limiter once step reaches this (option; 0 = reference)
+    int frozen;        // limiter values are frozen (set by the residual kernel)
 };
 
 // Flow constants of one case (gpu_init.cu:63-93).
@@ -47,6 +49,7 @@ template <typename T> struct Plan {
     Flow<T> f;
     V4<T> *W[2];   // W[0] holds the iteration's start state and its result
     V4<T> *FS;     // [3n] face-side states
+    V4<T> *phi;    // [3n] limiter values (limiter-freeze option), else null
     T *dt;         // [n]
     V4<T> *res;    // [n]
     V4<T> *sm[2];  // [n] smoothing sweeps (ping-pong)
@@ -82,6 +85,7 @@ template <typename T> struct BPlan {
     BatchDev<T> b;
     V4<T> *W[2];
     V4<T> *FS;
+    V4<T> *phi;              // [3n] limiter values (limiter-freeze option), else null
     T *dt;
     V4<T> *res;
     V4<T> *sm[2];

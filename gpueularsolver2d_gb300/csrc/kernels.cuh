@@ -223,10 +223,16 @@ __device__ __forceinline__ V4<T> roe(const V4<T> &LW, const V4<T> &RW, T nx, T n
 // FS[k*n+i] receives the state on the cell's own side of face k: the limited
 // reconstruction for an interior face, the cell state itself for a boundary
 // face (the reference's boundary faces are first order).
+//
+// Limiter freezing (an option with no reference counterpart, off when phi is
+// null): while not frozen the limiter values of every face are recorded in
+// phi; once frozen they are reused instead of re-evaluated, which makes the
+// residual a smooth function of the state so that it can converge below the
+// limiter's chatter floor.
 template <typename T>
 __device__ __forceinline__ void faces_cell(const MeshDev<T> &m, const Flow<T> &f, const int i,
                                            const V4<T> *__restrict__ W, V4<T> *__restrict__ FS,
-                                           T *__restrict__ dt) {
+                                           T *__restrict__ dt, V4<T> *__restrict__ phi, const int frozen) {
     const int n = m.n;
     const int4 tp = m.topo[i];
     const int code[3] = {tp.x, tp.y, tp.z};
@@ -272,18 +278,30 @@ __device__ __forceinline__ void faces_cell(const MeshDev<T> &m, const Flow<T> &f
         V4<T> o = U;
         if (code[k] >= 0) {
             const V2<T> r = m.R[k * n + i];
-            T fi = T(1.0), d[4];
+            const bool reuse = phi && frozen;
+            V4<T> pf;
+            if (reuse) pf = phi[k * n + i];
+            T fi = T(1.0), d[4], ph[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 T delt2 = gx[q] * r.x + gy[q] * r.y;
                 T u = comp(U, q);
-                if (delt2 > T(0)) fi = tmin((umax[q] - u) / delt2, T(1.0));
-                if (delt2 < T(0)) fi = tmin((umin[q] - u) / delt2, T(1.0));
-                if (delt2 == T(0)) fi = T(1.0);
+                if (reuse) fi = comp(pf, q);
+                else {
+                    if (delt2 > T(0)) fi = tmin((umax[q] - u) / delt2, T(1.0));
+                    if (delt2 < T(0)) fi = tmin((umin[q] - u) / delt2, T(1.0));
+                    if (delt2 == T(0)) fi = T(1.0);
+                }
+                ph[q] = fi;
                 delt2 *= fi;
                 d[q] = u + delt2;
             }
             o.x = d[0]; o.y = d[1]; o.z = d[2]; o.w = d[3];
+            if (phi && !frozen) {
+                V4<T> pw;
+                pw.x = ph[0]; pw.y = ph[1]; pw.z = ph[2]; pw.w = ph[3];
+                phi[k * n + i] = pw;
+            }
         }
         FS[k * n + i] = o;
     }
@@ -293,11 +311,11 @@ __device__ __forceinline__ void faces_cell(const MeshDev<T> &m, const Flow<T> &f
 template <typename T>
 __global__ void E2D_LB_FACES k_faces(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ W,
                                      V4<T> *__restrict__ FS, T *__restrict__ dt,
-                                     const Ctl *__restrict__ ctl) {
+                                     const Ctl *__restrict__ ctl, V4<T> *__restrict__ phi) {
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.n) return;
-    faces_cell(m, f, i, W, FS, dt);
+    faces_cell(m, f, i, W, FS, dt, phi, phi ? ctl->frozen : 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -483,13 +501,13 @@ __device__ __forceinline__ bool batch_cell(const BatchDev<T> &b, const int n, co
 
 template <typename T>
 __global__ void E2D_LB_FACES kb_faces(MeshDev<T> m, BatchDev<T> b, int ntiles, const V4<T> *__restrict__ W,
-                                      V4<T> *__restrict__ FS, T *__restrict__ dt) {
+                                      V4<T> *__restrict__ FS, T *__restrict__ dt, V4<T> *__restrict__ phi) {
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int i = t * blockDim.x + threadIdx.x;
         int c;
         if (batch_cell(b, m.n, i, c)) {
             const Flow<T> f = b.flows[c];
-            faces_cell(m, f, i, W, FS, dt);
+            faces_cell(m, f, i, W, FS, dt, phi, phi ? b.ctl[c].frozen : 0);
         }
     }
 }
@@ -545,7 +563,7 @@ template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream
         const bool last = st == p.stages - 1;
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
-        kb_faces<T><<<G, B, 0, s>>>(p.m, p.b, NT, Wcur, p.FS, p.dt);
+        kb_faces<T><<<G, B, 0, s>>>(p.m, p.b, NT, Wcur, p.FS, p.dt, p.phi);
         kb_flux<T><<<G, B, 0, s>>>(p.m, p.b, NT, p.FS, p.res);
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
@@ -604,7 +622,7 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
         const bool last = st == p.stages - 1;
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
-        k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl);
+        k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi);
         k_flux<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
@@ -631,7 +649,7 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
         const bool last = st == p.stages - 1;
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
-        mark(0); k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl); done();
+        mark(0); k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi); done();
         mark(1); k_flux<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl); done();
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {

@@ -48,6 +48,8 @@ __global__ void k_noalloc_ctl(Ctl *ctl, int target, double epsm) {
     ctl->epsl = 0.0;
     ctl->epsm = epsm > 0.0 ? epsm : 0.0;
     ctl->resd = 100.0;
+    ctl->freeze_after = 0;
+    ctl->frozen = 0;
 }
 
 size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }

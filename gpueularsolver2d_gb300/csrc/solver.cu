@@ -109,6 +109,7 @@ bool valid_params(const e2d_params *p) {
     if (p->ordering != E2D_ORDER_FILE && p->ordering != E2D_ORDER_MORTON) return false;
     if (p->block_size != 0 && (p->block_size < 32 || p->block_size > 256 || p->block_size % 32)) return false;
     if (p->graph_iters < 0 || p->graph_iters > 256) return false;
+    if (p->limiter_freeze < 0) return false;
     return true;
 }
 
@@ -137,7 +138,8 @@ template <typename T> struct SolverT : SolverBase {
         const int G = (n + block - 1) / block;
         size_t bytes = Arena::up(sizeof(int4) * n) + 2 * Arena::up(sizeof(V2<T>) * 3 * n) +
                        Arena::up(sizeof(T) * n) * 2 + Arena::up(sizeof(V4<T>) * n) * 5 +
-                       Arena::up(sizeof(V4<T>) * 3 * n) + Arena::up(sizeof(double) * G) +
+                       Arena::up(sizeof(V4<T>) * 3 * n) * (p.limiter_freeze > 0 ? 2 : 1) +
+                       Arena::up(sizeof(double) * G) +
                        Arena::up(sizeof(int) * n) + Arena::up(sizeof(double) * 4 * n);
         CK(cudaMalloc((void **)&arena.base, bytes));
         arena.cap = bytes;
@@ -148,6 +150,7 @@ template <typename T> struct SolverT : SolverBase {
         plan.W[0] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
         plan.W[1] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
         plan.FS = (V4<T> *)arena.take(sizeof(V4<T>) * 3 * n);
+        plan.phi = p.limiter_freeze > 0 ? (V4<T> *)arena.take(sizeof(V4<T>) * 3 * n) : nullptr;
         plan.dt = (T *)arena.take(sizeof(T) * n);
         plan.res = (V4<T> *)arena.take(sizeof(V4<T>) * n);
         plan.sm[0] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
@@ -379,6 +382,7 @@ int e2d_solver_create(e2d_mesh *m, const e2d_params *p, e2d_solver **out) {
     CK(cudaMallocHost((void **)&s->ctl_host, sizeof(Ctl)));
     std::memset(s->ctl_host, 0, sizeof(Ctl));
     s->ctl_host->resd = 100.0;  // gpu_solver.cu:2185 Resd[0]=100
+    s->ctl_host->freeze_after = p->limiter_freeze > 0 ? p->limiter_freeze : 0;
     CK(cudaMemcpy(s->ctl_dev, s->ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice));
     s->graph_iters = p->graph_iters > 0 ? p->graph_iters : 8;
     const int block = p->block_size > 0 ? p->block_size : 128;

@@ -75,6 +75,11 @@ typedef struct e2d_params {
     int32_t graph_iters; /* iterations captured per CUDA graph, 0 = default */
     int32_t verbose;     /* e2d_solve prints "step,resid" lines like the
                             reference (gpu_solver.cu:2433) when nonzero     */
+    int32_t limiter_freeze; /* option, no reference counterpart: 0 (default,
+                            reference) re-evaluates the limiter every stage;
+                            k > 0 freezes the per-face limiter values from
+                            iteration k on, so the residual can fall below
+                            the limiter's chatter floor                     */
 } e2d_params;
 
 typedef struct e2d_mesh_info {

@@ -49,6 +49,8 @@ struct or_case {
     double *dtel, *dter;    /* [nedge+1] deltT_e left/right */
     double *res, *r1, *r2;  /* [(ncell+1)*4] */
     double *dt;             /* [ncell+1] */
+    double *phil, *phir;    /* [(nedge+1)*4] limiter values (freeze option) */
+    int frozen;
     int step;
     double epsm, last_resd;
 };
@@ -445,6 +447,10 @@ static or_case *finish_create(or_case *c) {
     c->r1 = xcalloc((size_t)(N + 1) * 4, sizeof(double));
     c->r2 = xcalloc((size_t)(N + 1) * 4, sizeof(double));
     c->dt = xcalloc(N + 1, sizeof(double));
+    if (c->p.limiter_freeze > 0) {
+        c->phil = xcalloc((size_t)(c->nedge + 1) * 4, sizeof(double));
+        c->phir = xcalloc((size_t)(c->nedge + 1) * 4, sizeof(double));
+    }
     initialise(c);
     return c;
 }
@@ -490,7 +496,7 @@ void or_destroy(or_case *c) {
                     c->neicell, c->elog, c->eleft, c->eright, c->efar, c->ewall, c->en1,
                     c->en2, c->evn, c->evx, c->evy, c->emx, c->emy, c->w, c->w0,
                     c->farw, c->wallw, c->du, c->umax, c->umin, c->rel, c->rer,
-                    c->dtel, c->dter, c->res, c->r1, c->r2, c->dt};
+                    c->dtel, c->dter, c->res, c->r1, c->r2, c->dt, c->phil, c->phir};
     for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++) free(ptrs[i]);
     free(c);
 }
@@ -611,8 +617,10 @@ static void stage_gradient(or_case *c) {
 }
 
 /* gpu_solver.cu:456-494 (kernel_Limiter) and 496-549 (kernel_LBJinterpolate):
- * one side of an interior face, limited per face and per component. */
-static void reconstruct(const or_case *c, int cell, double midx, double midy, wst *out) {
+ * one side of an interior face, limited per face and per component.
+ * phi: with the limiter-freeze option, the 4 stored limiter values of this
+ * face side (recorded while not frozen, reused once frozen); NULL otherwise. */
+static void reconstruct(const or_case *c, int cell, double midx, double midy, wst *out, double *phi) {
     const wst *w = &c->w[cell];
     double UI[4] = {w->d, w->du, w->dv, w->de};
     double r0 = midx - c->cx[cell], r1 = midy - c->cy[cell];
@@ -620,9 +628,13 @@ static void reconstruct(const or_case *c, int cell, double midx, double midy, ws
     double delt2[4], fi = 1.0;
     for (int k = 0; k < 4; k++) delt2[k] = du[k] * r0 + du[4 + k] * r1;
     for (int k = 0; k < 4; k++) {
-        if (delt2[k] > 0) fi = fmin((c->umax[4 * (size_t)cell + k] - UI[k]) / delt2[k], 1.0);
-        if (delt2[k] < 0) fi = fmin((c->umin[4 * (size_t)cell + k] - UI[k]) / delt2[k], 1.0);
-        if (delt2[k] == 0) fi = 1.0;
+        if (phi && c->frozen) fi = phi[k];
+        else {
+            if (delt2[k] > 0) fi = fmin((c->umax[4 * (size_t)cell + k] - UI[k]) / delt2[k], 1.0);
+            if (delt2[k] < 0) fi = fmin((c->umin[4 * (size_t)cell + k] - UI[k]) / delt2[k], 1.0);
+            if (delt2[k] == 0) fi = 1.0;
+            if (phi) phi[k] = fi;
+        }
         delt2[k] *= fi;
     }
     memset(out, 0, sizeof *out);
@@ -639,8 +651,8 @@ static void stage_flux(or_case *c) {
         wst LW, RW;
         const wst *G = NULL;
         if (lg == 0) {
-            reconstruct(c, L, c->emx[e], c->emy[e], &LW);
-            reconstruct(c, R, c->emx[e], c->emy[e], &RW);
+            reconstruct(c, L, c->emx[e], c->emy[e], &LW, c->phil ? c->phil + 4 * (size_t)e : NULL);
+            reconstruct(c, R, c->emx[e], c->emy[e], &RW, c->phir ? c->phir + 4 * (size_t)e : NULL);
         } else {
             G = lg == 1 ? &c->farw[c->efar[e]] : &c->wallw[c->ewall[e]];
             LW = c->w[L];
@@ -818,6 +830,7 @@ int or_run(or_case *c, int nsteps, double *resid) {
         }
         if (c->step == 1) c->epsm = drou;
         c->last_resd = sqrt((drou + 1.0E-32) / c->epsm);
+        if (c->p.limiter_freeze > 0 && c->step >= c->p.limiter_freeze) c->frozen = 1;
         if (resid) resid[done] = c->last_resd;
         done++;
     }

@@ -36,6 +36,9 @@ typedef struct or_params {
     double dt_cap;            /* gpu_solver.cu:831 fmin(..., 0.1)          */
     double entropy_eps;       /* gpu_solver.cu:603 epsilon=0.05            */
     double wall_box;          /* gpu_init.cu:190 |mid|<2.0                 */
+    int limiter_freeze;       /* option without reference counterpart: > 0
+                                 reuses the limiter values of the last stage
+                                 of iteration k from iteration k+1 on      */
 } or_params;
 
 typedef struct or_case or_case;

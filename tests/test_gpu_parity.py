@@ -29,6 +29,7 @@ def run_pair(mesh, oracle, nsteps, **kw):
     dict(ma=0.8, alpha_deg=1.25, cfl=2.0, irs_eps=0.6, rk_stages=5, rk_coef=BLAZEK5),
     dict(ma=0.5, alpha_deg=-2.0, cfl=1.0, irs_sweeps=0),
     dict(ma=0.7, alpha_deg=3.0, cfl=1.5, irs_sweeps=3, ordering=e2d.E2D_ORDER_MORTON),
+    dict(ma=0.6, alpha_deg=1.0, cfl=1.5, limiter_freeze=12, ordering=e2d.E2D_ORDER_MORTON),
 ])
 def test_fp64_bit_exact_vs_oracle(lib, oracle, kw):
     mesh = e2d.Mesh.ogrid(48, 12, seed=7)
