@@ -125,3 +125,27 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
 def check(rc: int) -> None:
     if rc != 0:
         raise E2DError(rc, load().e2d_last_error().decode())
+
+
+class MLPConfig(ctypes.Structure):
+    """Mirror of ``e2d_mlp_config`` in include/euler2d.h."""
+    _fields_ = [("nhidden", ctypes.c_int32), ("batch", ctypes.c_int32), ("seed", ctypes.c_uint64),
+                ("lr", ctypes.c_double), ("beta1", ctypes.c_double), ("beta2", ctypes.c_double),
+                ("eps", ctypes.c_double)]
+
+
+_PF = ctypes.POINTER(ctypes.c_float)
+SIGNATURES.update({
+    "e2d_mlp_config_default": (_I, [ctypes.POINTER(MLPConfig)]),
+    "e2d_mlp_create": (_I, [ctypes.POINTER(MLPConfig), _PP]),
+    "e2d_mlp_destroy": (None, [_P]),
+    "e2d_mlp_param_count": (_I, [_P, ctypes.POINTER(ctypes.c_int64)]),
+    "e2d_mlp_get_params": (_I, [_P, _PF]),
+    "e2d_mlp_set_params": (_I, [_P, _PF]),
+    "e2d_mlp_set_data": (_I, [_P, ctypes.c_int64, _PF, _PF]),
+    "e2d_mlp_train": (_I, [_P, _I, _PD]),
+    "e2d_mlp_forward": (_I, [_P, ctypes.c_int64, _PF, _PF]),
+    "e2d_mlp_gradient": (_I, [_P, _PF, _PF, _PD, _PF]),
+    "e2d_mlp_features": (_I, [_P, _D, _D, _D, ctypes.c_uint64, _D, _PF]),
+    "e2d_wall_distance": (_I, [_P, _D, _PD]),
+})

@@ -12,7 +12,7 @@ import numpy as np
 from ._lib import (E2D_FP32, E2D_FP64, E2D_ORDER_FILE, E2D_ORDER_MORTON, MeshInfo, Params,
                    check, load)
 
-__all__ = ["Mesh", "Solver", "Batch", "Params", "default_params", "read_input", "E2D_FP32", "E2D_FP64",
+__all__ = ["Mesh", "Solver", "Batch", "MLP", "Params", "default_params", "read_input", "E2D_FP32", "E2D_FP64",
            "E2D_ORDER_FILE", "E2D_ORDER_MORTON"]
 
 
@@ -293,6 +293,84 @@ class Batch:
     def close(self) -> None:
         if self._h:
             load().e2d_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _fp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class MLP:
+    """The warm-start coordinate MLP (e2d_mlp_* in include/euler2d.h)."""
+
+    INPUTS = 32
+    FEATURES = 22
+
+    def __init__(self, nhidden: int = 5, batch: int = 65536, seed: int = 3, lr: float = 1e-3):
+        from ._lib import MLPConfig
+        c = MLPConfig()
+        check(load().e2d_mlp_config_default(ctypes.byref(c)))
+        c.nhidden, c.batch, c.seed, c.lr = nhidden, batch, seed, lr
+        self.config = c
+        h = ctypes.c_void_p()
+        check(load().e2d_mlp_create(ctypes.byref(c), ctypes.byref(h)))
+        self._h = h
+
+    def param_count(self) -> int:
+        n = ctypes.c_int64()
+        check(load().e2d_mlp_param_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.param_count(), np.float32)
+        check(load().e2d_mlp_get_params(self._h, _fp(p)))
+        return p
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        check(load().e2d_mlp_set_params(self._h, _fp(p)))
+
+    def set_data(self, x, t) -> None:
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, self.INPUTS)
+        t = np.ascontiguousarray(t, np.float32).reshape(-1, 4)
+        check(load().e2d_mlp_set_data(self._h, x.shape[0], _fp(x), _fp(t)))
+
+    def train(self, steps: int, record_loss: bool = True) -> np.ndarray:
+        loss = np.zeros(steps)
+        check(load().e2d_mlp_train(self._h, steps, _dp(loss) if record_loss else None))
+        return loss
+
+    def forward(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, self.INPUTS)
+        y = np.zeros((x.shape[0], 4), np.float32)
+        check(load().e2d_mlp_forward(self._h, x.shape[0], _fp(x), _fp(y)))
+        return y
+
+    def gradient(self, x, t):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, self.INPUTS)
+        t = np.ascontiguousarray(t, np.float32).reshape(-1, 4)
+        g = np.zeros(self.param_count(), np.float32)
+        loss = ctypes.c_double()
+        check(load().e2d_mlp_gradient(self._h, _fp(x), _fp(t), ctypes.byref(loss), _fp(g)))
+        return loss.value, g
+
+    @staticmethod
+    def features(mesh: "Mesh", mach: float, alpha_deg: float, seed: int = 3, sigma: float = 1.0,
+                 wall_box: float = 2.0) -> np.ndarray:
+        n = mesh.info(wall_box).ncell
+        out = np.zeros((n, MLP.INPUTS), np.float32)
+        check(load().e2d_mlp_features(mesh._h, wall_box, mach, alpha_deg, seed, sigma, _fp(out)))
+        return out
+
+    def close(self) -> None:
+        if self._h:
+            load().e2d_mlp_destroy(self._h)
             self._h = None
 
     def __del__(self):

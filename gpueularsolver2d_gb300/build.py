@@ -34,13 +34,14 @@ UNITS = {
     "output.o": ("output.cpp", GXX),
     "solver.o": ("solver.cu", ["nvcc", *NVCC_COMMON]),
     "batch.o": ("batch.cu", ["nvcc", *NVCC_COMMON]),
+    "mlp.o": ("mlp.cu", ["nvcc", *NVCC_COMMON]),
     "resid.o": ("resid.cu", ["nvcc", *NVCC_COMMON]),
     "kernels_f64.o": ("kernels_f64.cu", ["nvcc", *NVCC_COMMON, "--fmad=false"]),
     "noalloc.o": ("noalloc.cu", ["nvcc", *NVCC_COMMON, "--fmad=false"]),
     "kernels_f32.o": ("kernels_f32.cu", ["nvcc", *NVCC_COMMON, "--fmad=true",
                                           "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
 }
-HEADERS = ["internal.h", "dev_types.h", "kernels.cuh", "solver_internal.h"]
+HEADERS = ["internal.h", "dev_types.h", "kernels.cuh", "solver_internal.h", "mlp_kernels.cuh"]
 
 
 def _stale(target: str, deps: list[str]) -> bool:

@@ -1,0 +1,520 @@
+// mlp.cu -- the coordinate MLP of the learned warm start, trained on the GPU
+// by the kernels of mlp_kernels.cuh.  No reference counterpart.
+//
+// Network: 32 inputs (22 features, zero padded) -> H -> ... -> H (nhidden
+// layers, GELU) -> 4 outputs.  Weights are kept in FP32 (Adam master copy) and
+// used in BF16; activations and their gradients are BF16; every product
+// accumulates in FP32.  The output layer (H -> 4) runs on the CUDA cores.
+// One training step (batch gather, forward, MSE loss, backward, Adam) is one
+// CUDA graph; the step counter lives in device memory so the graph is static.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "mlp_kernels.cuh"
+#include "solver_internal.h"
+
+using namespace e2d;
+using namespace e2d::mlp;
+
+#define CK(call)                                                                       \
+    do {                                                                               \
+        cudaError_t err_ = (call);                                                     \
+        if (err_ != cudaSuccess) {                                                     \
+            set_error(std::string("CUDA: ") + #call + ": " + cudaGetErrorString(err_)); \
+            return E2D_ERR_CUDA;                                                       \
+        }                                                                              \
+    } while (0)
+
+namespace {
+
+constexpr int NIN = E2D_MLP_INPUTS;  // padded input width
+constexpr int NOUT = 4;
+constexpr int H = 256;
+constexpr int kSplits = 64;          // split-K over the batch for weight gradients
+
+__global__ void k_step_update(int *step, float beta1, float beta2, float *bc) {
+    const int s = ++*step;
+    bc[0] = 1.f - powf(beta1, (float)s);
+    bc[1] = 1.f - powf(beta2, (float)s);
+}
+
+__global__ void __launch_bounds__(256) k_adam_dev(int count, const float *__restrict__ part, int nparts,
+                                                  size_t pstride, float *__restrict__ w32, bf16 *__restrict__ wbf,
+                                                  float *__restrict__ m, float *__restrict__ v, float lr,
+                                                  float beta1, float beta2, float eps, const float *__restrict__ bc,
+                                                  float *__restrict__ grad_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    float g = 0.f;
+    for (int p = 0; p < nparts; p++) g += part[(size_t)p * pstride + i];
+    if (grad_out) grad_out[i] = g;
+    if (lr == 0.f) return;
+    const float mi = beta1 * m[i] + (1.f - beta1) * g;
+    const float vi = beta2 * v[i] + (1.f - beta2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    const float w = w32[i] - lr * (mi / bc[0]) / (sqrtf(vi / bc[1]) + eps);
+    w32[i] = w;
+    if (wbf) wbf[i] = __float2bfloat16_rn(w);
+}
+
+__global__ void k_to_bf16(int n, const float *__restrict__ a, bf16 *__restrict__ b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = __float2bfloat16_rn(a[i]);
+}
+
+// Minimum distance from each point to a set of segments (wall faces).
+__global__ void __launch_bounds__(256) k_wall_distance(int n, const double *__restrict__ px,
+                                                       const double *__restrict__ py, int nseg,
+                                                       const double4 *__restrict__ seg, double *__restrict__ d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double4 s[256];
+    double best = 1e300;
+    const double x = i < n ? px[i] : 0.0, y = i < n ? py[i] : 0.0;
+    for (int base = 0; base < nseg; base += 256) {
+        __syncthreads();
+        if (base + (int)threadIdx.x < nseg) s[threadIdx.x] = seg[base + threadIdx.x];
+        __syncthreads();
+        const int cnt = min(256, nseg - base);
+        for (int k = 0; k < cnt; k++) {
+            const double4 q = s[k];
+            const double ex = q.z - q.x, ey = q.w - q.y;
+            const double L2 = ex * ex + ey * ey;
+            double t = L2 > 0 ? ((x - q.x) * ex + (y - q.y) * ey) / L2 : 0.0;
+            t = fmin(1.0, fmax(0.0, t));
+            const double dx = x - (q.x + t * ex), dy = y - (q.y + t * ey);
+            best = fmin(best, dx * dx + dy * dy);
+        }
+    }
+    if (i < n) d[i] = sqrt(best);
+}
+
+struct Tensor {
+    int rows, cols;
+    float *w32 = nullptr, *m = nullptr, *v = nullptr;
+    bf16 *wbf = nullptr;
+    int count() const { return rows * cols; }
+};
+
+}  // namespace
+
+struct e2d_mlp {
+    e2d_mlp_config cfg;
+    int nhidden = 5;
+    std::vector<Tensor> W, b;  // hidden layers (W: H x in, b: H x 1) then the output layer
+    // batch buffers
+    int B = 0;
+    bf16 *xb = nullptr;
+    float *tb = nullptr, *y = nullptr, *dy = nullptr;
+    std::vector<bf16 *> Z, Hh;  // [nhidden] of [B][H]
+    bf16 *dz[2] = {nullptr, nullptr};
+    float *part = nullptr;      // weight-gradient partials (largest tensor x kSplits)
+    float *bpart = nullptr;     // bias-gradient partials
+    double *loss_part = nullptr;
+    int *step_dev = nullptr;
+    float *bc_dev = nullptr;
+    float *grad = nullptr;      // flat gradient of all parameters (gradient probe)
+    // training set
+    bf16 *X = nullptr;
+    float *T = nullptr;
+    long long nsamples = 0, cap_samples = 0;
+    std::vector<void *> allocs;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<double> loss_host;
+
+    ~e2d_mlp() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (stream) cudaStreamDestroy(stream);
+        for (void *p : allocs) cudaFree(p);
+        if (X) cudaFree(X);
+        if (T) cudaFree(T);
+    }
+    template <typename P> int alloc(P **p, size_t bytes) {
+        CK(cudaMalloc((void **)p, bytes));
+        CK(cudaMemset(*p, 0, bytes));
+        allocs.push_back(*p);
+        return E2D_OK;
+    }
+};
+
+namespace {
+
+size_t param_count(const e2d_mlp *m) {
+    size_t c = 0;
+    for (size_t l = 0; l < m->W.size(); l++) c += m->W[l].count() + m->b[l].count();
+    return c;
+}
+
+int ensure_batch(e2d_mlp *m, int B) {
+    if (m->B == B) return E2D_OK;
+    if (m->B != 0) { set_error("batch size is fixed at the first use"); return E2D_ERR_ARG; }
+    if (B < 2048 || B % 2048 != 0) {  // split-K slices of the batch are multiples of BK
+        set_error("batch must be a positive multiple of 2048");
+        return E2D_ERR_ARG;
+    }
+    m->B = B;
+    int rc;
+    if ((rc = m->alloc(&m->xb, sizeof(bf16) * (size_t)B * NIN))) return rc;
+    if ((rc = m->alloc(&m->tb, sizeof(float) * (size_t)B * NOUT))) return rc;
+    if ((rc = m->alloc(&m->y, sizeof(float) * (size_t)B * NOUT))) return rc;
+    if ((rc = m->alloc(&m->dy, sizeof(float) * (size_t)B * NOUT))) return rc;
+    m->Z.resize(m->nhidden);
+    m->Hh.resize(m->nhidden);
+    for (int l = 0; l < m->nhidden; l++) {
+        if ((rc = m->alloc(&m->Z[l], sizeof(bf16) * (size_t)B * H))) return rc;
+        if ((rc = m->alloc(&m->Hh[l], sizeof(bf16) * (size_t)B * H))) return rc;
+    }
+    for (int k = 0; k < 2; k++)
+        if ((rc = m->alloc(&m->dz[k], sizeof(bf16) * (size_t)B * H))) return rc;
+    if ((rc = m->alloc(&m->part, sizeof(float) * (size_t)kSplits * H * H))) return rc;
+    if ((rc = m->alloc(&m->bpart, sizeof(float) * (size_t)kSplits * (NOUT * H + NOUT + H)))) return rc;
+    if ((rc = m->alloc(&m->loss_part, sizeof(double) * (B / 256)))) return rc;
+    return E2D_OK;
+}
+
+void adam(e2d_mlp *m, cudaStream_t s, Tensor &t, const float *part, int nparts, size_t pstride, float lr,
+          float *grad_out) {
+    const auto &c = m->cfg;
+    k_adam_dev<<<(t.count() + 255) / 256, 256, 0, s>>>(t.count(), part, nparts, pstride, t.w32, t.wbf, t.m, t.v,
+                                                        lr, (float)c.beta1, (float)c.beta2, (float)c.eps, m->bc_dev,
+                                                        grad_out);
+}
+
+// Forward on the batch in xb (rows B); with targets, the loss partials and dy.
+void forward(e2d_mlp *m, cudaStream_t s, bool with_loss) {
+    const int B = m->B;
+    for (int l = 0; l < m->nhidden; l++) {
+        GemmArgs g{};
+        g.M = B; g.N = H; g.K = l == 0 ? NIN : H;
+        g.A = l == 0 ? m->xb : m->Hh[l - 1];
+        g.lda = g.K;
+        g.B = m->W[l].wbf; g.ldb = g.K;
+        g.bias = m->b[l].w32; g.out = m->Hh[l]; g.zout = m->Z[l]; g.ldc = H;
+        k_gemm<false, false, EPI_BIAS_GELU><<<dim3(H / BN, (B + BM - 1) / BM, 1), 256, 0, s>>>(g);
+    }
+    const Tensor &Wo = m->W[m->nhidden], &bo = m->b[m->nhidden];
+    k_out_fwd_loss<H, NOUT><<<(B + 255) / 256, 256, 0, s>>>(B, m->Hh[m->nhidden - 1], Wo.w32, bo.w32,
+                                                            with_loss ? m->tb : nullptr, m->y, m->dy,
+                                                            with_loss ? m->loss_part : nullptr);
+}
+
+// Backward + Adam (lr = 0: gradient only, written to m->grad in parameter order).
+void backward(e2d_mlp *m, cudaStream_t s, float lr, bool want_grad) {
+    const int B = m->B, L = m->nhidden;
+    const int rows = B / kSplits;
+    size_t goff = param_count(m);
+    auto gslot = [&](const Tensor &t) -> float * {
+        if (!want_grad) return nullptr;
+        goff -= t.count();
+        return m->grad + goff;
+    };
+    // output layer: weight / bias partials, then the gradient at the last pre-activation
+    Tensor &Wo = m->W[L], &bo = m->b[L];
+    k_out_bwd_weight<H, NOUT><<<kSplits, 256, 0, s>>>(B, rows, m->dy, m->Hh[L - 1], m->bpart);
+    k_out_bwd_data<H, NOUT><<<(B * (H / 2) + 255) / 256, 256, 0, s>>>(B, m->dy, Wo.w32, m->Z[L - 1], m->dz[0]);
+    const size_t ostride = NOUT * H + NOUT;
+    float *gbo = gslot(bo);
+    float *gWo = gslot(Wo);
+    adam(m, s, bo, m->bpart + NOUT * H, kSplits, ostride, lr, gbo);
+    adam(m, s, Wo, m->bpart, kSplits, ostride, lr, gWo);
+    int cur = 0;
+    for (int l = L - 1; l >= 0; l--) {
+        const int kin = l == 0 ? NIN : H;
+        const bf16 *hin = l == 0 ? m->xb : m->Hh[l - 1];
+        // dW_l = dz^T hin (split over the batch), db_l = column sums of dz
+        GemmArgs gw{};
+        gw.M = H; gw.N = kin; gw.K = B;
+        gw.A = m->dz[cur]; gw.lda = H;
+        gw.B = hin; gw.ldb = kin;
+        gw.part = m->part;
+        k_gemm<true, true, EPI_PARTIAL><<<dim3((kin + BN - 1) / BN, H / BM, kSplits), 256, 0, s>>>(gw);
+        k_colsum<<<kSplits, 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart);
+        // gradient at the previous pre-activation (before this layer's weights change)
+        if (l > 0) {
+            GemmArgs gd{};
+            gd.M = B; gd.N = H; gd.K = H;
+            gd.A = m->dz[cur]; gd.lda = H;
+            gd.B = m->W[l].wbf; gd.ldb = H;
+            gd.zin = m->Z[l - 1]; gd.out = m->dz[cur ^ 1]; gd.ldc = H;
+            k_gemm<false, true, EPI_GELU_BWD><<<dim3(H / BN, (B + BM - 1) / BM, 1), 256, 0, s>>>(gd);
+        }
+        float *gb = gslot(m->b[l]);
+        float *gW = gslot(m->W[l]);
+        adam(m, s, m->b[l], m->bpart, kSplits, H, lr, gb);
+        adam(m, s, m->W[l], m->part, kSplits, (size_t)H * kin, lr, gW);
+        cur ^= 1;
+    }
+}
+
+int build_train_graph(e2d_mlp *m) {
+    if (m->gexec) return E2D_OK;
+    cudaGraph_t g = nullptr;
+    cudaStream_t s = m->stream;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    k_step_update<<<1, 1, 0, s>>>(m->step_dev, (float)m->cfg.beta1, (float)m->cfg.beta2, m->bc_dev);
+    // the gather reads the step from device memory through its seed argument
+    k_gather<<<(m->B + 255) / 256, 256, 0, s>>>(m->B, NIN, NOUT, m->cfg.seed, m->step_dev, m->nsamples, m->X,
+                                                  m->T, m->xb, m->tb);
+    forward(m, s, true);
+    backward(m, s, (float)m->cfg.lr, false);
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (e != cudaSuccess) { set_error(std::string("graph capture: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
+    e = cudaGraphInstantiate(&m->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { m->gexec = nullptr; set_error(std::string("graph instantiate: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
+    return E2D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int e2d_mlp_config_default(e2d_mlp_config *c) {
+    if (!c) { set_error("null argument"); return E2D_ERR_ARG; }
+    std::memset(c, 0, sizeof *c);
+    c->nhidden = 5;
+    c->lr = 1e-3;
+    c->beta1 = 0.9;
+    c->beta2 = 0.999;
+    c->eps = 1e-8;
+    c->batch = 65536;
+    c->seed = 3;
+    return E2D_OK;
+}
+
+int e2d_mlp_create(const e2d_mlp_config *cfg, e2d_mlp **out) {
+    if (!cfg || !out) { set_error("null argument"); return E2D_ERR_ARG; }
+    *out = nullptr;
+    if (cfg->nhidden < 1 || cfg->nhidden > 16) { set_error("nhidden must be 1..16"); return E2D_ERR_ARG; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        set_error("no CUDA device: the MLP trains on the GPU only");
+        return E2D_ERR_CUDA;
+    }
+    auto m = std::make_unique<e2d_mlp>();
+    m->cfg = *cfg;
+    m->nhidden = cfg->nhidden;
+    CK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+    // He-style initialisation from a fixed-seed generator
+    uint64_t st = cfg->seed * 0x9e3779b97f4a7c15ULL + 12345;
+    auto rnd = [&]() {
+        st ^= st >> 12; st ^= st << 25; st ^= st >> 27;
+        return ((st * 0x2545F4914F6CDD1DULL) >> 11) * (1.0 / 9007199254740992.0);
+    };
+    auto normal = [&]() {
+        double u1 = rnd() + 1e-300, u2 = rnd();
+        return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+    };
+    for (int l = 0; l <= m->nhidden; l++) {
+        const bool last = l == m->nhidden;
+        const int rows = last ? NOUT : H, cols = l == 0 ? NIN : H;
+        const int fan_in = l == 0 ? E2D_MLP_FEATURES : H;
+        Tensor W{rows, cols}, b{rows, 1};
+        std::vector<float> hw((size_t)rows * cols, 0.f), hb(rows, 0.f);
+        const double sd = std::sqrt((last ? 1.0 : 2.0) / fan_in);
+        for (int r = 0; r < rows; r++)
+            for (int c = 0; c < cols; c++)
+                hw[(size_t)r * cols + c] = (l == 0 && c >= E2D_MLP_FEATURES) ? 0.f : (float)(sd * normal());
+        int rc;
+        for (Tensor *t : {&W, &b}) {
+            const size_t n = t->count();
+            if ((rc = m->alloc(&t->w32, sizeof(float) * n))) return rc;
+            if ((rc = m->alloc(&t->m, sizeof(float) * n))) return rc;
+            if ((rc = m->alloc(&t->v, sizeof(float) * n))) return rc;
+            if (!last && t == &W && (rc = m->alloc(&t->wbf, sizeof(bf16) * n))) return rc;
+        }
+        CK(cudaMemcpy(W.w32, hw.data(), sizeof(float) * hw.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(b.w32, hb.data(), sizeof(float) * hb.size(), cudaMemcpyHostToDevice));
+        if (W.wbf) k_to_bf16<<<(W.count() + 255) / 256, 256, 0, m->stream>>>(W.count(), W.w32, W.wbf);
+        m->W.push_back(W);
+        m->b.push_back(b);
+    }
+    int rc;
+    if ((rc = m->alloc(&m->step_dev, sizeof(int)))) return rc;
+    if ((rc = m->alloc(&m->bc_dev, 2 * sizeof(float)))) return rc;
+    if ((rc = m->alloc(&m->grad, sizeof(float) * param_count(m.get())))) return rc;
+    CK(cudaStreamSynchronize(m->stream));
+    *out = m.release();
+    return E2D_OK;
+}
+
+void e2d_mlp_destroy(e2d_mlp *m) { delete m; }
+
+int e2d_mlp_param_count(e2d_mlp *m, int64_t *n) {
+    if (!m || !n) { set_error("null argument"); return E2D_ERR_ARG; }
+    *n = (int64_t)param_count(m);
+    return E2D_OK;
+}
+
+int e2d_mlp_get_params(e2d_mlp *m, float *out) {
+    if (!m || !out) { set_error("null argument"); return E2D_ERR_ARG; }
+    size_t off = 0;
+    for (size_t l = 0; l < m->W.size(); l++)
+        for (Tensor *t : {&m->W[l], &m->b[l]}) {
+            CK(cudaMemcpy(out + off, t->w32, sizeof(float) * t->count(), cudaMemcpyDeviceToHost));
+            off += t->count();
+        }
+    return E2D_OK;
+}
+
+int e2d_mlp_set_params(e2d_mlp *m, const float *in) {
+    if (!m || !in) { set_error("null argument"); return E2D_ERR_ARG; }
+    size_t off = 0;
+    for (size_t l = 0; l < m->W.size(); l++)
+        for (Tensor *t : {&m->W[l], &m->b[l]}) {
+            CK(cudaMemcpy(t->w32, in + off, sizeof(float) * t->count(), cudaMemcpyHostToDevice));
+            if (t->wbf) k_to_bf16<<<(t->count() + 255) / 256, 256, 0, m->stream>>>(t->count(), t->w32, t->wbf);
+            off += t->count();
+        }
+    CK(cudaStreamSynchronize(m->stream));
+    return E2D_OK;
+}
+
+int e2d_mlp_set_data(e2d_mlp *m, int64_t nsamples, const float *x, const float *t) {
+    if (!m || !x || !t || nsamples < 1) { set_error("bad argument"); return E2D_ERR_ARG; }
+    if (m->X) { cudaFree(m->X); m->X = nullptr; }
+    if (m->T) { cudaFree(m->T); m->T = nullptr; }
+    std::vector<bf16> xb((size_t)nsamples * NIN);
+    for (size_t i = 0; i < xb.size(); i++) xb[i] = __float2bfloat16_rn(x[i]);
+    CK(cudaMalloc((void **)&m->X, sizeof(bf16) * xb.size()));
+    CK(cudaMalloc((void **)&m->T, sizeof(float) * (size_t)nsamples * NOUT));
+    CK(cudaMemcpy(m->X, xb.data(), sizeof(bf16) * xb.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(m->T, t, sizeof(float) * (size_t)nsamples * NOUT, cudaMemcpyHostToDevice));
+    m->nsamples = nsamples;
+    if (m->gexec) { cudaGraphExecDestroy(m->gexec); m->gexec = nullptr; }
+    return E2D_OK;
+}
+
+int e2d_mlp_train(e2d_mlp *m, int32_t steps, double *loss) {
+    if (!m || steps < 1 || !m->X) { set_error("bad argument or no training data"); return E2D_ERR_ARG; }
+    int rc = ensure_batch(m, m->cfg.batch);
+    if (rc) return rc;
+    if ((rc = build_train_graph(m))) return rc;
+    const int nlp = m->B / 256;
+    std::vector<double> lp(nlp);
+    for (int k = 0; k < steps; k++) {
+        CK(cudaGraphLaunch(m->gexec, m->stream));
+        if (loss) {
+            CK(cudaMemcpyAsync(lp.data(), m->loss_part, sizeof(double) * nlp, cudaMemcpyDeviceToHost, m->stream));
+            CK(cudaStreamSynchronize(m->stream));
+            double s = 0.0;
+            for (double v : lp) s += v;
+            loss[k] = s / ((double)m->B * NOUT);
+        }
+    }
+    CK(cudaStreamSynchronize(m->stream));
+    return E2D_OK;
+}
+
+int e2d_mlp_forward(e2d_mlp *m, int64_t n, const float *x, float *y) {
+    if (!m || !x || !y || n < 1) { set_error("bad argument"); return E2D_ERR_ARG; }
+    int rc = ensure_batch(m, m->cfg.batch);
+    if (rc) return rc;
+    std::vector<bf16> xb((size_t)m->B * NIN);
+    for (int64_t r0 = 0; r0 < n; r0 += m->B) {
+        const int64_t cnt = std::min<int64_t>(m->B, n - r0);
+        for (size_t i = 0; i < xb.size(); i++)
+            xb[i] = __float2bfloat16_rn(i < (size_t)cnt * NIN ? x[(size_t)r0 * NIN + i] : 0.f);
+        CK(cudaMemcpyAsync(m->xb, xb.data(), sizeof(bf16) * xb.size(), cudaMemcpyHostToDevice, m->stream));
+        forward(m, m->stream, false);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(y + (size_t)r0 * NOUT, m->y, sizeof(float) * cnt * NOUT, cudaMemcpyDeviceToHost, m->stream));
+        CK(cudaStreamSynchronize(m->stream));
+    }
+    return E2D_OK;
+}
+
+int e2d_mlp_gradient(e2d_mlp *m, const float *x, const float *t, double *loss, float *grad) {
+    if (!m || !x || !t || !grad) { set_error("bad argument"); return E2D_ERR_ARG; }
+    int rc = ensure_batch(m, m->cfg.batch);
+    if (rc) return rc;
+    std::vector<bf16> xb((size_t)m->B * NIN);
+    for (size_t i = 0; i < xb.size(); i++) xb[i] = __float2bfloat16_rn(x[i]);
+    CK(cudaMemcpy(m->xb, xb.data(), sizeof(bf16) * xb.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(m->tb, t, sizeof(float) * (size_t)m->B * NOUT, cudaMemcpyHostToDevice));
+    forward(m, m->stream, true);
+    backward(m, m->stream, 0.f, true);
+    CK(cudaGetLastError());
+    const int nlp = m->B / 256;
+    std::vector<double> lp(nlp);
+    CK(cudaMemcpyAsync(lp.data(), m->loss_part, sizeof(double) * nlp, cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaMemcpyAsync(grad, m->grad, sizeof(float) * param_count(m), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    double s = 0.0;
+    for (double v : lp) s += v;
+    if (loss) *loss = s / ((double)m->B * NOUT);
+    return E2D_OK;
+}
+
+int e2d_wall_distance(e2d_mesh *mesh, double wall_box, double *d) {
+    if (!mesh || !d) { set_error("null argument"); return E2D_ERR_ARG; }
+    int rc = build_topology(mesh, wall_box);
+    if (rc) return rc;
+    const MeshTopo &t = mesh->topo;
+    std::vector<double4> seg;
+    for (int e = 0; e < t.nedge; e++)
+        if (t.elog[e] == 2)
+            seg.push_back(make_double4(mesh->x[t.en1[e] - 1], mesh->y[t.en1[e] - 1], mesh->x[t.en2[e] - 1],
+                                       mesh->y[t.en2[e] - 1]));
+    const int n = mesh->ncell;
+    if (seg.empty()) { for (int i = 0; i < n; i++) d[i] = 1e300; return E2D_OK; }
+    double *px, *py, *dd;
+    double4 *sg;
+    CK(cudaMalloc((void **)&px, sizeof(double) * n));
+    CK(cudaMalloc((void **)&py, sizeof(double) * n));
+    CK(cudaMalloc((void **)&dd, sizeof(double) * n));
+    CK(cudaMalloc((void **)&sg, sizeof(double4) * seg.size()));
+    CK(cudaMemcpy(px, t.cx.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(py, t.cy.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(sg, seg.data(), sizeof(double4) * seg.size(), cudaMemcpyHostToDevice));
+    k_wall_distance<<<(n + 255) / 256, 256>>>(n, px, py, (int)seg.size(), sg, dd);
+    cudaError_t e = cudaMemcpy(d, dd, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    cudaFree(px); cudaFree(py); cudaFree(dd); cudaFree(sg);
+    if (e != cudaSuccess) { set_error(std::string("wall distance: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
+    return E2D_OK;
+}
+
+// Features per cell: x, y, log(d_wall + 1e-3), Mach, sin a, cos a, then for
+// j = 0..7: sin(2 pi f_j . (x, y)), cos(2 pi f_j . (x, y)), f_j ~ N(0, sigma^2).
+int e2d_mlp_features(e2d_mesh *mesh, double wall_box, double mach, double alpha_deg, uint64_t seed, double sigma,
+                     float *out) {
+    if (!mesh || !out) { set_error("null argument"); return E2D_ERR_ARG; }
+    const int n = mesh->ncell;
+    std::vector<double> d(n);
+    int rc = e2d_wall_distance(mesh, wall_box, d.data());
+    if (rc) return rc;
+    uint64_t st = seed * 0x9e3779b97f4a7c15ULL + 777;
+    auto rnd = [&]() {
+        st ^= st >> 12; st ^= st << 25; st ^= st >> 27;
+        return ((st * 0x2545F4914F6CDD1DULL) >> 11) * (1.0 / 9007199254740992.0);
+    };
+    double f[8][2];
+    for (auto &fj : f)
+        for (double &c : fj) {
+            double u1 = rnd() + 1e-300, u2 = rnd();
+            c = sigma * std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+        }
+    const double a = alpha_deg * 3.14159265358979 / 180.0, sa = std::sin(a), ca = std::cos(a);
+    const MeshTopo &t = mesh->topo;
+    for (int i = 0; i < n; i++) {
+        float *o = out + (size_t)i * NIN;
+        const double x = t.cx[i], y = t.cy[i];
+        o[0] = (float)x; o[1] = (float)y; o[2] = (float)std::log(d[i] + 1e-3);
+        o[3] = (float)mach; o[4] = (float)sa; o[5] = (float)ca;
+        for (int j = 0; j < 8; j++) {
+            const double ph = 6.283185307179586 * (f[j][0] * x + f[j][1] * y);
+            o[6 + 2 * j] = (float)std::sin(ph);
+            o[7 + 2 * j] = (float)std::cos(ph);
+        }
+        for (int k = E2D_MLP_FEATURES; k < NIN; k++) o[k] = 0.f;
+    }
+    return E2D_OK;
+}
+
+}  // extern "C"

@@ -227,6 +227,49 @@ int e2d_batch_autotune(e2d_batch *b, const char *cache_path, int32_t iters, int3
 int e2d_batch_last_device_ms(e2d_batch *b, double *ms);
 int e2d_batch_launches_per_iteration(e2d_batch *b, int32_t *n);
 
+/* ---- learned warm start ------------------------------------------------
+ * A coordinate MLP maps per-cell features (x, y, log wall distance, Mach,
+ * sin alpha, cos alpha and 16 random Fourier features of (x, y)) to the
+ * conserved state; it is trained on steady solutions of this solver and its
+ * prediction is an initial state for e2d_set_state.  Training runs on the GPU
+ * in hand-written kernels: BF16 tensor-core GEMMs with FP32 accumulation
+ * (forward, backward), and Adam on FP32 master weights.  No reference
+ * counterpart. */
+#define E2D_MLP_FEATURES 22   /* feature count */
+#define E2D_MLP_INPUTS 32     /* padded input width (features, then zeros) */
+
+typedef struct e2d_mlp e2d_mlp;
+typedef struct e2d_mlp_config {
+    int32_t nhidden;  /* hidden layers of width 256 (default 5)         */
+    int32_t batch;    /* training batch, a multiple of 2048 (65536)     */
+    uint64_t seed;    /* initial weights and batch sampling             */
+    double lr, beta1, beta2, eps;  /* Adam (1e-3, 0.9, 0.999, 1e-8)     */
+} e2d_mlp_config;
+
+int e2d_mlp_config_default(e2d_mlp_config *c);
+int e2d_mlp_create(const e2d_mlp_config *c, e2d_mlp **out);
+void e2d_mlp_destroy(e2d_mlp *m);
+/* Parameters in order W0, b0, W1, b1, ..., W_out, b_out (row-major W[out][in]). */
+int e2d_mlp_param_count(e2d_mlp *m, int64_t *n);
+int e2d_mlp_get_params(e2d_mlp *m, float *p);
+int e2d_mlp_set_params(e2d_mlp *m, const float *p);
+/* Training set: x [n * E2D_MLP_INPUTS] normalised inputs, t [n * 4] targets. */
+int e2d_mlp_set_data(e2d_mlp *m, int64_t n, const float *x, const float *t);
+/* steps Adam steps on random batches; loss[k] (may be NULL) = batch MSE. */
+int e2d_mlp_train(e2d_mlp *m, int32_t steps, double *loss);
+/* y [n * 4] = network(x [n * E2D_MLP_INPUTS]). */
+int e2d_mlp_forward(e2d_mlp *m, int64_t n, const float *x, float *y);
+/* MSE loss and its gradient (parameter order as e2d_mlp_get_params) on one
+ * batch x [batch * E2D_MLP_INPUTS], t [batch * 4]; parameters unchanged. */
+int e2d_mlp_gradient(e2d_mlp *m, const float *x, const float *t, double *loss, float *grad);
+/* Raw features of every cell of a mesh for one flow condition, [ncell *
+ * E2D_MLP_INPUTS] (before normalisation; padding zero).  Fourier
+ * frequencies are N(0, sigma^2) per chord, drawn from `seed`. */
+int e2d_mlp_features(e2d_mesh *m, double wall_box, double mach, double alpha_deg, uint64_t seed,
+                     double sigma, float *out);
+/* Distance from every cell centroid to the nearest wall face. */
+int e2d_wall_distance(e2d_mesh *m, double wall_box, double *d);
+
 /* ---- iterations without allocation ------------------------------------ */
 /* Largest mesh e2d_step_noalloc accepts. */
 #define E2D_NOALLOC_MAX_CELLS 32768

@@ -1,0 +1,59 @@
+"""The warm-start MLP's GPU kernels (BF16 tensor-core GEMMs, FP32 accumulation,
+Adam) against the CPU restatement in oracle/mlp_oracle.py.
+
+The GPU rounds activations and their gradients to BF16 (8-bit mantissa); the
+oracle works in FP64 on the same BF16-rounded weights and inputs.  Tolerances,
+written per check: loss to 1e-2 relative, every parameter tensor's gradient
+to 5e-2 relative in the 2-norm with cosine similarity above 0.998."""
+import numpy as np
+import pytest
+
+import gpueularsolver2d_gb300 as e2d
+
+pytestmark = pytest.mark.gpu
+
+
+def test_gradient_matches_cpu_oracle(lib, oracle):
+    import mlp_oracle
+    B, L = 2048, 3
+    net = e2d.MLP(nhidden=L, batch=B, seed=11)
+    rng = np.random.default_rng(5)
+    x = np.zeros((B, 32), np.float32)
+    x[:, :22] = rng.normal(size=(B, 22)).astype(np.float32)
+    t = rng.normal(size=(B, 4)).astype(np.float32) * 0.3
+    loss, g = net.gradient(x, t)
+    p = net.params()
+    loss_ref, g_ref = mlp_oracle.loss_and_grad(p, x, t, L)
+    assert abs(loss - loss_ref) / loss_ref < 1e-2
+    off = 0
+    for l in range(L + 1):
+        rows = 4 if l == L else 256
+        cols = 32 if l == 0 else 256
+        for size in (rows * cols, rows):
+            a, b = g[off:off + size].astype(np.float64), g_ref[off:off + size]
+            off += size
+            if l == 0 and size == rows * cols:  # padding inputs have zero gradient
+                a = a.reshape(rows, cols)[:, :22].ravel()
+                b = b.reshape(rows, cols)[:, :22].ravel()
+            rel = np.linalg.norm(a - b) / np.linalg.norm(b)
+            cos = a @ b / (np.linalg.norm(a) * np.linalg.norm(b))
+            assert rel < 5e-2 and cos > 0.998, (l, size, rel, cos)
+    assert off == len(g)
+
+
+def test_training_reduces_loss_and_forward_agrees(lib):
+    B = 4096
+    net = e2d.MLP(nhidden=3, batch=B, seed=2, lr=2e-3)
+    rng = np.random.default_rng(0)
+    n = 40000
+    x = np.zeros((n, 32), np.float32)
+    x[:, :22] = rng.uniform(-1, 1, size=(n, 22)).astype(np.float32)
+    t = np.stack([np.sin(2 * x[:, 0]) * x[:, 1], np.cos(x[:, 2] + x[:, 3]), x[:, 4] ** 2 - 0.3,
+                  0.5 * np.tanh(3 * x[:, 5])], axis=1).astype(np.float32)
+    net.set_data(x, t)
+    loss = net.train(400)
+    assert np.all(np.isfinite(loss))
+    assert loss[-20:].mean() < 0.1 * loss[:5].mean(), (loss[:5].mean(), loss[-20:].mean())
+    y = net.forward(x[:5000])
+    mse = float(np.mean((y - t[:5000]) ** 2))
+    assert mse < 2.0 * loss[-20:].mean() + 1e-4
