@@ -1,0 +1,220 @@
+"""Learned warm start: a coordinate MLP trained on steady solutions of the
+solver predicts the initial conserved field of a new flow condition.
+
+Pipeline (no reference counterpart; the plain solver stays the oracle):
+
+1. ``generate``: steady solutions for sampled (Mach, alpha) on one mesh,
+   computed by the batched solver (FP32 stencil) with the limiter-freeze
+   option, the same settings for every case.
+2. ``Dataset``: per-cell features (x, y, log wall distance, Mach, sin a, cos a,
+   16 random Fourier features of (x, y); e2d_mlp_features) normalised to zero
+   mean / unit variance for the first six, and targets W - W_inf(M, a) scaled
+   per component.
+3. ``train``: Adam on random batches, all on the GPU (e2d_mlp_train).
+4. ``predict``: W_inf + scale * MLP(features) for a new condition.
+5. ``evaluate``: for held-out conditions, iterations and wall time to the
+   target drop from the free stream and from the prediction, with the same
+   solver settings and the same residual normalisation (the free-stream run's
+   first-iteration density change), and the converged CL / CD of both.
+
+Run ``python -m gpueularsolver2d_gb300.warmstart --help``.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import sys
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import api as e2d
+from ._lib import E2DError
+
+GAMMA = 1.4
+
+
+def conditions(n: int, seed: int, mach=(0.5, 0.7), alpha=(-1.0, 3.0)):
+    rng = np.random.default_rng(seed)
+    return [(float(m), float(a)) for m, a in zip(rng.uniform(*mach, n), rng.uniform(*alpha, n))]
+
+
+def freestream(mach: float, alpha_deg: float, ncell: int) -> np.ndarray:
+    """The reference's free-stream state (gpu_init.cu:79-86), non-dimensional."""
+    a = alpha_deg * 3.14159265358979 / 180.0
+    rho_e = 1.0 / (GAMMA * (GAMMA - 1.0) * mach * mach) + 0.5
+    w = np.empty((ncell, 4))
+    w[:, 0] = 1.0
+    w[:, 1] = math.cos(a)
+    w[:, 2] = math.sin(a)
+    w[:, 3] = rho_e
+    return w
+
+
+@dataclass
+class SolverSettings:
+    cfl: float = 3.0
+    freeze: int = 1500
+    precision: int = e2d.E2D_FP32
+
+    def params(self, mach, alpha, maxstep=100000):
+        return e2d.default_params(ma=mach, alpha_deg=alpha, cfl=self.cfl, precision=self.precision,
+                                  ordering=e2d.E2D_ORDER_MORTON, limiter_freeze=self.freeze, maxstep=maxstep)
+
+
+def generate(mesh, conds, settings: SolverSettings, iters: int, chunk: int = 128, log=print):
+    """Steady states for every condition (batched solves of `iters` iterations)."""
+    states, info = [], []
+    for c0 in range(0, len(conds), chunk):
+        part = conds[c0:c0 + chunk]
+        params = [settings.params(m, a, maxstep=iters) for m, a in part]
+        b = e2d.Batch([mesh] * len(part), params)
+        t0 = time.perf_counter()
+        b.step(iters)
+        dt = time.perf_counter() - t0
+        for c in range(len(part)):
+            states.append(b.state(c))
+            h = b.history(c)
+            info.append({"mach": part[c][0], "alpha": part[c][1], "resd": float(h[-1])})
+        log(f"generate: cases {c0}..{c0 + len(part) - 1}: {iters} iterations in {dt:.1f} s, "
+            f"Resd median {np.median([i['resd'] for i in info[c0:]]):.2e}")
+        b.close()
+    return states, info
+
+
+class Dataset:
+    """Normalised features and targets of a set of solutions on one mesh."""
+
+    def __init__(self, mesh, conds, states, fourier_seed: int = 3, sigma: float = 1.0):
+        self.fourier_seed, self.sigma = fourier_seed, sigma
+        feats = [e2d.MLP.features(mesh, m, a, fourier_seed, sigma) for m, a in conds]
+        x = np.concatenate(feats)
+        self.x_mean = np.zeros(32, np.float32)
+        self.x_std = np.ones(32, np.float32)
+        self.x_mean[:6] = x[:, :6].mean(axis=0)
+        self.x_std[:6] = np.maximum(x[:, :6].std(axis=0), 1e-6)
+        tgt = np.concatenate([s - freestream(m, a, s.shape[0]) for (m, a), s in zip(conds, states)])
+        self.t_scale = np.maximum(tgt.std(axis=0), 1e-6)
+        self.x = self.normalise(x)
+        self.t = (tgt / self.t_scale).astype(np.float32)
+
+    def normalise(self, x):
+        return ((x - self.x_mean) / self.x_std).astype(np.float32)
+
+    def to_json(self):
+        return {"x_mean": self.x_mean.tolist(), "x_std": self.x_std.tolist(), "t_scale": self.t_scale.tolist(),
+                "fourier_seed": self.fourier_seed, "sigma": self.sigma}
+
+
+def train(ds: Dataset, steps: int, batch: int = 65536, nhidden: int = 5, lr: float = 1e-3, seed: int = 3,
+          log=print):
+    net = e2d.MLP(nhidden=nhidden, batch=batch, seed=seed, lr=lr)
+    net.set_data(ds.x, ds.t)
+    t0 = time.perf_counter()
+    loss = net.train(steps)
+    dt = time.perf_counter() - t0
+    log(f"train: {steps} steps of batch {batch} in {dt:.1f} s, loss {loss[:10].mean():.3e} -> {loss[-100:].mean():.3e}")
+    return net, loss, dt
+
+
+def predict(net, ds: Dataset, mesh, mach, alpha):
+    x = ds.normalise(e2d.MLP.features(mesh, mach, alpha, ds.fourier_seed, ds.sigma))
+    y = net.forward(x).astype(np.float64) * ds.t_scale
+    return freestream(mach, alpha, x.shape[0]) + y
+
+
+def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=None, epsm=None):
+    s = e2d.Solver(mesh, settings.params(mach, alpha, maxstep=maxit))
+    if w0 is not None:
+        s.set_state(w0)
+    if epsm is not None:
+        s.set_residual_norm(epsm)
+    t0 = time.perf_counter()
+    try:
+        h = s.solve(maxit, target)
+        ok = bool(len(h) and h[-1] <= target)
+    except E2DError:
+        h, ok = s.history(), False
+    wall = time.perf_counter() - t0
+    cl, cd = s.forces() if ok else (float("nan"), float("nan"))
+    out = {"iterations": int(len(h)), "wall_s": wall, "converged": ok, "cl": cl, "cd": cd,
+           "first_resd": float(h[0]) if len(h) else float("nan"), "epsm": s.residual_norm()}
+    s.close()
+    return out
+
+
+def evaluate(net, ds, mesh, conds, settings: SolverSettings, target: float, maxit: int, log=print):
+    rows = []
+    for m, a in conds:
+        free = run_to_drop(mesh, m, a, settings, target, maxit)
+        warm_state = predict(net, ds, mesh, m, a)
+        warm = run_to_drop(mesh, m, a, settings, target, maxit, w0=warm_state, epsm=free["epsm"])
+        r = {"mach": m, "alpha": a, "free": free, "warm": warm,
+             "speedup_wall": free["wall_s"] / warm["wall_s"] if warm["converged"] else float("nan"),
+             "speedup_iter": free["iterations"] / max(1, warm["iterations"]) if warm["converged"] else float("nan"),
+             "dcl": abs(warm["cl"] - free["cl"]), "dcd": abs(warm["cd"] - free["cd"])}
+        rows.append(r)
+        log(f"eval M{m:.3f} a{a:+.2f}: free {free['iterations']} its {free['wall_s']:.2f} s | warm "
+            f"{warm['iterations']} its {warm['wall_s']:.2f} s (first Resd {warm['first_resd']:.2e}) | "
+            f"x{r['speedup_wall']:.2f} wall, dCL {r['dcl']:.1e} dCD {r['dcd']:.1e}")
+    return rows
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--ni", type=int, default=256)
+    ap.add_argument("--nj", type=int, default=64)
+    ap.add_argument("--ntrain", type=int, default=256)
+    ap.add_argument("--nheld", type=int, default=32)
+    ap.add_argument("--neval", type=int, default=8, help="held-out conditions timed one by one")
+    ap.add_argument("--gen-iters", type=int, default=20000)
+    ap.add_argument("--steps", type=int, default=20000)
+    ap.add_argument("--batch", type=int, default=65536)
+    ap.add_argument("--target", type=float, default=1e-6)
+    ap.add_argument("--maxit", type=int, default=60000)
+    ap.add_argument("--mach", type=float, nargs=2, default=(0.5, 0.7))
+    ap.add_argument("--alpha", type=float, nargs=2, default=(-1.0, 3.0))
+    ap.add_argument("--json", default=None)
+    args = ap.parse_args(argv)
+    log = lambda s: print(s, file=sys.stderr, flush=True)  # noqa: E731
+    mesh = e2d.Mesh.ogrid(args.ni, args.nj, seed=1)
+    train_c = conditions(args.ntrain, 3, tuple(args.mach), tuple(args.alpha))
+    held_c = conditions(args.nheld, 4, tuple(args.mach), tuple(args.alpha))
+    gen = SolverSettings(precision=e2d.E2D_FP32)
+    states, info = generate(mesh, train_c, gen, args.gen_iters, log=log)
+    ds = Dataset(mesh, train_c, states)
+    net, loss, t_train = train(ds, args.steps, args.batch, log=log)
+    # prediction error on the held-out conditions against their FP32 solutions
+    held_states, _ = generate(mesh, held_c, gen, args.gen_iters, log=log)
+    errs = []
+    for (m, a), w in zip(held_c, held_states):
+        p = predict(net, ds, mesh, m, a)
+        errs.append(float(np.sqrt(np.mean((p - w) ** 2, axis=0)).max() / np.abs(w).max()))
+    log(f"held-out prediction RMS error (max over components, rel. to max |W|): median {np.median(errs):.2e}")
+    ev = SolverSettings(precision=e2d.E2D_FP64)
+    rows = evaluate(net, ds, mesh, held_c[:args.neval], ev, args.target, args.maxit, log=log)
+    conv = [r for r in rows if r["warm"]["converged"] and r["free"]["converged"]]
+    summary = {
+        "mesh": f"{args.ni}x{args.nj}", "ntrain": args.ntrain, "nheld": args.nheld, "mach": list(args.mach),
+        "alpha": list(args.alpha), "gen_iters": args.gen_iters, "train_steps": args.steps, "batch": args.batch,
+        "train_seconds": t_train, "final_loss": float(loss[-100:].mean()),
+        "heldout_pred_err_median": float(np.median(errs)), "target_drop": args.target,
+        "eval_precision": "fp64", "evaluated": len(rows), "both_converged": len(conv),
+        "speedup_wall_median": float(np.median([r["speedup_wall"] for r in conv])) if conv else None,
+        "speedup_iter_median": float(np.median([r["speedup_iter"] for r in conv])) if conv else None,
+        "max_dcl": float(max(r["dcl"] for r in conv)) if conv else None,
+        "max_dcd": float(max(r["dcd"] for r in conv)) if conv else None,
+        "rows": rows,
+    }
+    text = json.dumps(summary)
+    print(text, flush=True)
+    if args.json:
+        with open(args.json, "w") as f:
+            f.write(text + "\n")
+    return summary
+
+
+if __name__ == "__main__":
+    main()
