@@ -125,6 +125,22 @@ def measured_peak_hbm() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
+def max_over_ranks(t: float, dist, device: str) -> float:
+    """The slowest rank's time (the job's time); t itself without a process group."""
+    if dist is None:
+        return t
+    import torch
+    v = torch.tensor([t], dtype=torch.float64, device=device)
+    dist.all_reduce(v, op=dist.ReduceOp.MAX)
+    return float(v.item())
+
+
+def replica_rate(world: int, ncell: int, stages: int, steps: int, t_max: float) -> float:
+    """Whole-job cell-stage updates/s of `world` replicas that each ran `steps`
+    iterations of an ncell-cell mesh, timed by the slowest one."""
+    return world * ncell * stages * steps / t_max
+
+
 def make_params(e2d, wl, precision, block=0):
     return e2d.default_params(ma=wl["ma"], alpha_deg=wl["alpha"], cfl=wl["cfl"], precision=precision,
                               ordering=e2d.E2D_ORDER_MORTON, maxstep=1000000, block_size=block)
@@ -228,13 +244,8 @@ def run_gpu(args, rank: int, world: int):
     barrier()
     clocks = sampler.stop()
     t_local = dev_ms / 1e3
-    if dist is not None:
-        t = torch.tensor([t_local], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    else:
-        t_max = t_local
-    value = world * ncell * stages * args.steps / t_max
+    t_max = max_over_ranks(t_local, dist, "cuda")
+    value = replica_rate(world, ncell, stages, args.steps, t_max)
 
     # per-pass device time inside the same iteration sequence (events around every launch)
     prof_iters = 3
@@ -274,12 +285,8 @@ def run_gpu(args, rank: int, world: int):
         solver.step(1)
         solver.state_into(pin_out)
     torch.cuda.synchronize()
-    e2e_t = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_t], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_t = float(t.item())
-    e2e_rate = world * ncell * stages * e2e_steps / e2e_t
+    e2e_t = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
+    e2e_rate = replica_rate(world, ncell, stages, e2e_steps, e2e_t)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -311,6 +318,51 @@ def run_gpu(args, rank: int, world: int):
         dist.destroy_process_group()
 
 
+def run_batch64(args):
+    """Batched sweep: 64 cases on O-grids of sizes drawn from {64..512}x{16..128}
+    (seed 2), Mach U[0.3, 0.85], alpha U[-2, 4] deg, FP32, one launch per pass
+    over all cases with the autotuned launch shape, against the same 64 cases
+    solved one after the other by the single-case solver."""
+    import numpy as np
+    import torch
+    import gpueularsolver2d_gb300 as e2d
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    rng = np.random.default_rng(2)
+    ni = rng.choice([64, 128, 256, 512], 64)
+    nj = rng.choice([16, 32, 64, 128], 64)
+    mach = rng.uniform(0.3, 0.85, 64)
+    alpha = rng.uniform(-2.0, 4.0, 64)
+    meshes = [e2d.Mesh.ogrid(int(a), int(b), seed=10 + k) for k, (a, b) in enumerate(zip(ni, nj))]
+    params = [e2d.default_params(ma=float(m), alpha_deg=float(a), cfl=2.0, precision=e2d.E2D_FP32,
+                                 ordering=e2d.E2D_ORDER_MORTON, maxstep=args.steps + args.warmup + 64)
+              for m, a in zip(mach, alpha)]
+    cells = sum(2 * int(a) * int(b) for a, b in zip(ni, nj))
+    b = e2d.Batch(meshes, params)
+    block, grid, ms_tune = b.autotune(None, iters=16)
+    b.step(args.warmup)
+    b.step(args.steps)
+    t_batch = b.last_device_ms() / 1e3
+    stages = params[0].rk_stages
+    agg = cells * stages * args.steps / t_batch
+    t_seq = 0.0
+    for m, p in zip(meshes, params):
+        s = e2d.Solver(m, p)
+        s.step(args.warmup)
+        s.step(args.steps)
+        t_seq += s.last_device_ms() / 1e3
+        s.close()
+    seq = cells * stages * args.steps / t_seq
+    line = {"metric": "cell-stage updates/s (64-case batched sweep)", "value": agg, "unit": "cell-stage/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_batch / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded NACA0012 O-grids)",
+            "config": {"workload": "64 cases, O-grids {64..512}x{16..128} (seed 2), M U[0.3,0.85], a U[-2,4]",
+                       "cells": cells, "stages": stages, "autotuned_block": block, "autotuned_grid": grid},
+            "sequential_value": seq, "speedup_vs_sequential": agg / seq,
+            "gpu_launches": b.launches_per_iteration() * args.steps}
+    print(json.dumps(line), flush=True)
+
+
 def args_sweeps_count(params) -> int:
     return max(0, params.irs_sweeps - 1)
 
@@ -333,7 +385,7 @@ def main():
     ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="large")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch64"], default="large")
     ap.add_argument("--fp64", action="store_true")
     ap.add_argument("--block", type=int, default=0, help="threads per CTA (0: library default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -342,7 +394,13 @@ def main():
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    if args.impl == "reference":
+    if args.workload == "batch64":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference solves one case per run; "
+                              "the batched sweep has no reference arm"}))
+        elif rank == 0:
+            run_batch64(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_gpu(args, rank, world)
