@@ -39,6 +39,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 REF_FILES = ["gpu_fvm.cuh", "gpu_fvm.cu", "gpu_init.cu", "gpu_solver.cu", "cuPrintf.cu",
              "cuPrintf.cuh"]
+# the reference's RAE2822 meshes, staged beside the sources for machines without the checkout
+REF_MESHES = ["2822-3k.dat", "2822-1w.dat", "2822-5w.dat"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -47,10 +49,10 @@ def _source_dir() -> str | None:
     if all(os.path.exists(os.path.join(ref, f)) for f in REF_FILES):
         stage = os.path.join(OUT, "src")
         os.makedirs(stage, exist_ok=True)
-        for f in REF_FILES:
+        for f in REF_FILES + REF_MESHES:
             dst = os.path.join(stage, f)
             src = os.path.join(ref, f)
-            if not os.path.exists(dst) or os.path.getmtime(dst) < os.path.getmtime(src):
+            if os.path.exists(src) and (not os.path.exists(dst) or os.path.getmtime(dst) < os.path.getmtime(src)):
                 shutil.copyfile(src, dst)
         return ref
     stage = os.path.join(OUT, "src")

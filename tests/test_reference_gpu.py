@@ -43,3 +43,41 @@ def test_reference_gpu_program_matches(lib, oracle):
     # the reference prints "step,resid" per iteration (gpu_solver.cu:2433)
     lines = [l for l in out["stdout"].splitlines() if l.count(",") == 1 and l.split(",")[0].isdigit()]
     assert len(lines) == steps
+
+
+def test_reference_kernels_timed_on_this_gpu(lib, oracle):
+    """The reference's Fermi-era kernels run on this GPU on its own 51,800-cell
+    RAE2822 mesh (the size of its published per-kernel timings), beside this
+    library's FP64 and FP32 paths on the same mesh and settings.  Records the
+    times (gpurun_out/reference_gpu_timing.json when that directory exists)."""
+    import json
+    import time
+    from conftest import reference_mesh, ROOT
+    mesh_path = reference_mesh("2822-5w.dat")
+    if mesh_path is None or oracle.ref_harness_path() is None:
+        pytest.skip("reference sources or meshes not available")
+    steps = 300
+    line = f"0.73 2.0 1.4 101325 288.15 1.5 1e-12 {steps}"
+    t0 = time.perf_counter()
+    out = oracle.run_reference("gpu", mesh_path, line)
+    t_prog = time.perf_counter() - t0
+    tot = [l for l in out["stdout"].splitlines() if l.startswith("total time:")]
+    assert tot, out["stdout"][-500:]
+    ref_s = float(tot[-1].split(":")[1])
+    mesh = e2d.Mesh.read(mesh_path)
+    res = {"mesh": "2822-5w.dat", "cells": mesh.info().ncell, "iterations": steps,
+           "reference_ms_per_iteration": ref_s / steps * 1e3, "reference_program_seconds": t_prog}
+    for name, prec in (("fp64", e2d.E2D_FP64), ("fp32", e2d.E2D_FP32)):
+        s = e2d.Solver(mesh, e2d.default_params(ma=0.73, alpha_deg=2.0, cfl=1.5, precision=prec,
+                                                ordering=e2d.E2D_ORDER_MORTON))
+        s.step(10)
+        s.step(steps)
+        res[f"{name}_ms_per_iteration"] = s.last_device_ms() / steps
+    res["speedup_fp64"] = res["reference_ms_per_iteration"] / res["fp64_ms_per_iteration"]
+    res["speedup_fp32"] = res["reference_ms_per_iteration"] / res["fp32_ms_per_iteration"]
+    out_dir = os.path.join(ROOT, "gpurun_out")
+    if os.path.isdir(out_dir):
+        with open(os.path.join(out_dir, "reference_gpu_timing.json"), "w") as f:
+            json.dump(res, f)
+    print(res)
+    assert res["fp64_ms_per_iteration"] < res["reference_ms_per_iteration"]
