@@ -34,6 +34,7 @@ class Params(ctypes.Structure):
         ("wall_box", ctypes.c_double), ("ordering", ctypes.c_int32),
         ("block_size", ctypes.c_int32), ("graph_iters", ctypes.c_int32),
         ("verbose", ctypes.c_int32), ("limiter_freeze", ctypes.c_int32),
+        ("limiter", ctypes.c_int32), ("limiter_k", ctypes.c_double),
     ]
 
 

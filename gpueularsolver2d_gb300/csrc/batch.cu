@@ -124,6 +124,7 @@ template <typename T> struct BatchT : BatchBase {
             f.gamma = (T)p.gamma; f.ui = (T)FS[c].ui; f.vi = (T)FS[c].vi; f.ain = (T)FS[c].ain;
             f.tin = (T)p.tin; f.vin = (T)FS[c].vin; f.R = (T)287.06; f.pis = (T)FS[c].pis; f.cfl = (T)p.cfl;
             f.dt_cap = (T)p.dt_cap; f.eps_entropy = (T)p.entropy_eps; f.irs_eps = (T)p.irs_eps;
+            f.venk_k3 = (T)(p.limiter_k * p.limiter_k * p.limiter_k); f.limiter = p.limiter;
         }
         CK(cudaMemcpy(topo, ht.data(), sizeof(int4) * n, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(S, hS.data(), sizeof(T) * hS.size(), cudaMemcpyHostToDevice));

@@ -26,6 +26,8 @@ struct Ctl {
 // Flow constants of one case (gpu_init.cu:63-93).
 template <typename T> struct Flow {
     T gamma, ui, vi, ain, tin, vin, R, pis, cfl, dt_cap, eps_entropy, irs_eps;
+    T venk_k3;    // K^3 of the Venkatakrishnan option
+    int limiter;  // 0 reference, 1 Venkatakrishnan
 };
 
 // Cell-local mesh data in internal order (n cells).

@@ -287,7 +287,14 @@ __device__ __forceinline__ void faces_cell(const MeshDev<T> &m, const Flow<T> &f
                 T delt2 = gx[q] * r.x + gy[q] * r.y;
                 T u = comp(U, q);
                 if (reuse) fi = comp(pf, q);
-                else {
+                else if (f.limiter == 1) {
+                    // Venkatakrishnan on the per-face differences (option)
+                    const T e2 = f.venk_k3 * A * tsqrt(A);
+                    const T d1 = delt2 > T(0) ? umax[q] - u : umin[q] - u;
+                    fi = delt2 == T(0) ? T(1.0)
+                                       : (d1 * d1 + e2 + T(2) * delt2 * d1) /
+                                             (d1 * d1 + T(2) * delt2 * delt2 + d1 * delt2 + e2);
+                } else {
                     if (delt2 > T(0)) fi = tmin((umax[q] - u) / delt2, T(1.0));
                     if (delt2 < T(0)) fi = tmin((umin[q] - u) / delt2, T(1.0));
                     if (delt2 == T(0)) fi = T(1.0);

@@ -424,6 +424,7 @@ int e2d_params_default(e2d_params *p) {
     p->irs_eps = 0.8; p->irs_sweeps = 2; p->precision = E2D_FP64;
     p->dt_cap = 0.1; p->entropy_eps = 0.05; p->wall_box = 2.0;
     p->ordering = E2D_ORDER_FILE; p->block_size = 0; p->graph_iters = 0; p->verbose = 0;
+    p->limiter_freeze = 0; p->limiter = E2D_LIMITER_REFERENCE; p->limiter_k = 5.0;
     return E2D_OK;
 }
 

@@ -123,6 +123,7 @@ extern "C" int e2d_step_noalloc(int32_t ncell, const int32_t *topo, const double
     f.gamma = g; f.ui = std::cos(alpha); f.vi = std::sin(alpha); f.ain = ain; f.tin = p->tin; f.vin = vin;
     f.R = kR; f.pis = (g - 1.0) * 1.0 * E; f.cfl = p->cfl; f.dt_cap = p->dt_cap;
     f.eps_entropy = p->entropy_eps; f.irs_eps = p->irs_eps;
+    f.venk_k3 = p->limiter_k * p->limiter_k * p->limiter_k; f.limiter = p->limiter;
     plan.hist = resid;
     plan.hist_cap = iterations;
     plan.stages = p->rk_stages;

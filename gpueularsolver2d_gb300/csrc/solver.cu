@@ -110,6 +110,8 @@ bool valid_params(const e2d_params *p) {
     if (p->block_size != 0 && (p->block_size < 32 || p->block_size > 256 || p->block_size % 32)) return false;
     if (p->graph_iters < 0 || p->graph_iters > 256) return false;
     if (p->limiter_freeze < 0) return false;
+    if (p->limiter != E2D_LIMITER_REFERENCE && p->limiter != E2D_LIMITER_VENKAT) return false;
+    if (p->limiter == E2D_LIMITER_VENKAT && !(p->limiter_k > 0.0)) return false;
     return true;
 }
 
@@ -174,6 +176,7 @@ template <typename T> struct SolverT : SolverBase {
         f.gamma = (T)p.gamma; f.ui = (T)fs.ui; f.vi = (T)fs.vi; f.ain = (T)fs.ain; f.tin = (T)p.tin;
         f.vin = (T)fs.vin; f.R = (T)kR; f.pis = (T)fs.pis; f.cfl = (T)p.cfl; f.dt_cap = (T)p.dt_cap;
         f.eps_entropy = (T)p.entropy_eps; f.irs_eps = (T)p.irs_eps;
+        f.venk_k3 = (T)(p.limiter_k * p.limiter_k * p.limiter_k); f.limiter = p.limiter;
         plan.ctl = ctl;
         plan.hist = nullptr;
         plan.hist_cap = 0;

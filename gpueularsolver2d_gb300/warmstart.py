@@ -55,13 +55,21 @@ def freestream(mach: float, alpha_deg: float, ncell: int) -> np.ndarray:
 
 @dataclass
 class SolverSettings:
+    """Solver settings shared by every run of the pipeline.  The default is the
+    smooth (Venkatakrishnan-type) limiter option: unlike the reference limiter
+    it lets the residual fall to 1e-6, and unlike a frozen limiter its
+    converged state does not depend on the starting state, so warm and
+    free-stream runs converge to the same solution."""
     cfl: float = 3.0
-    freeze: int = 1500
+    freeze: int = 0
     precision: int = e2d.E2D_FP32
+    limiter: int = 1
+    limiter_k: float = 5.0
 
     def params(self, mach, alpha, maxstep=100000):
         return e2d.default_params(ma=mach, alpha_deg=alpha, cfl=self.cfl, precision=self.precision,
-                                  ordering=e2d.E2D_ORDER_MORTON, limiter_freeze=self.freeze, maxstep=maxstep)
+                                  ordering=e2d.E2D_ORDER_MORTON, limiter_freeze=self.freeze, maxstep=maxstep,
+                                  limiter=self.limiter, limiter_k=self.limiter_k)
 
 
 def generate(mesh, conds, settings: SolverSettings, iters: int, chunk: int = 128, log=print):

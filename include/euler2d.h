@@ -80,7 +80,17 @@ typedef struct e2d_params {
                             k > 0 freezes the per-face limiter values from
                             iteration k on, so the residual can fall below
                             the limiter's chatter floor                     */
+    int32_t limiter;     /* E2D_LIMITER_REFERENCE (default): the reference's
+                            per-face min((Umax-U)/d, 1) (gpu_solver.cu:456-494);
+                            E2D_LIMITER_VENKAT: option, no reference
+                            counterpart -- the smooth Venkatakrishnan form on
+                            the same per-face differences, eps^2 = (K h)^3,
+                            h = sqrt(cell area)                              */
+    double limiter_k;    /* K of E2D_LIMITER_VENKAT (default 5)              */
 } e2d_params;
+
+#define E2D_LIMITER_REFERENCE 0
+#define E2D_LIMITER_VENKAT 1
 
 typedef struct e2d_mesh_info {
     int32_t ncell, nnode, nedge, nwall, nfar;

@@ -72,6 +72,7 @@ void or_params_default(or_params *p) {
     p->dt_cap = 0.1;       /* gpu_solver.cu:831 */
     p->entropy_eps = 0.05; /* gpu_solver.cu:603 */
     p->wall_box = 2.0;     /* gpu_init.cu:190 */
+    p->limiter_k = 5.0;
 }
 
 /* gpu_init.cu:34-42: "%lf %lf %lf %lf %lf %lf %lf %d" */
@@ -629,7 +630,17 @@ static void reconstruct(const or_case *c, int cell, double midx, double midy, ws
     for (int k = 0; k < 4; k++) delt2[k] = du[k] * r0 + du[4 + k] * r1;
     for (int k = 0; k < 4; k++) {
         if (phi && c->frozen) fi = phi[k];
-        else {
+        else if (c->p.limiter == 1) {
+            /* Venkatakrishnan form on the same per-face differences (option) */
+            double K3 = c->p.limiter_k * c->p.limiter_k * c->p.limiter_k;
+            double A = c->area[cell];
+            double e2 = K3 * A * sqrt(A);
+            double d1 = delt2[k] > 0 ? c->umax[4 * (size_t)cell + k] - UI[k] : c->umin[4 * (size_t)cell + k] - UI[k];
+            fi = delt2[k] == 0 ? 1.0
+                               : (d1 * d1 + e2 + 2 * delt2[k] * d1) /
+                                     (d1 * d1 + 2 * delt2[k] * delt2[k] + d1 * delt2[k] + e2);
+            if (phi) phi[k] = fi;
+        } else {
             if (delt2[k] > 0) fi = fmin((c->umax[4 * (size_t)cell + k] - UI[k]) / delt2[k], 1.0);
             if (delt2[k] < 0) fi = fmin((c->umin[4 * (size_t)cell + k] - UI[k]) / delt2[k], 1.0);
             if (delt2[k] == 0) fi = 1.0;

@@ -39,6 +39,8 @@ typedef struct or_params {
     int limiter_freeze;       /* option without reference counterpart: > 0
                                  reuses the limiter values of the last stage
                                  of iteration k from iteration k+1 on      */
+    int limiter;              /* 0 reference; 1 Venkatakrishnan option     */
+    double limiter_k;         /* K of the Venkatakrishnan option           */
 } or_params;
 
 typedef struct or_case or_case;

@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 def test_warm_start_small(lib):
     mesh = e2d.Mesh.ogrid(64, 16, seed=1)
-    gen = ws.SolverSettings(cfl=3.0, freeze=400, precision=e2d.E2D_FP32)
+    gen = ws.SolverSettings(cfl=3.0, precision=e2d.E2D_FP32)
     train_c = ws.conditions(16, 3, (0.5, 0.65), (-1.0, 3.0))
     held = ws.conditions(1, 4, (0.5, 0.65), (-1.0, 3.0))
     states, _ = ws.generate(mesh, train_c + held, gen, 3000, log=lambda s: None)
@@ -26,7 +26,7 @@ def test_warm_start_small(lib):
     err_pred = np.abs(p - w_true).mean()
     err_free = np.abs(ws.freestream(m, a, p.shape[0]) - w_true).mean()
     assert err_pred < 0.5 * err_free, (err_pred, err_free)
-    ev = ws.SolverSettings(cfl=3.0, freeze=400, precision=e2d.E2D_FP32)
+    ev = ws.SolverSettings(cfl=3.0, precision=e2d.E2D_FP32)
     free = ws.run_to_drop(mesh, m, a, ev, 1e-4, 20000)
     warm = ws.run_to_drop(mesh, m, a, ev, 1e-4, 20000, w0=p, epsm=free["epsm"])
     assert free["converged"] and warm["converged"]
