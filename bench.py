@@ -288,6 +288,23 @@ def run_gpu(args, rank: int, world: int):
     e2e_t = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
     e2e_rate = replica_rate(world, ncell, stages, e2e_steps, e2e_t)
 
+    # FP32 stencil against an FP64 run of the same code on the same workload
+    fp_err = None
+    if rank == 0 and prec == e2d.E2D_FP32:
+        n_err = 20
+        a32 = e2d.Solver(mesh, make_params(e2d, wl, e2d.E2D_FP32))
+        a64 = e2d.Solver(mesh, make_params(e2d, wl, e2d.E2D_FP64))
+        a32.step(n_err)
+        a64.step(n_err)
+        w32, w64 = a32.state(), a64.state()
+        h32, h64 = a32.history(), a64.history()
+        fp_err = {"iterations": n_err,
+                  "max_rel_linf": float(np.max(np.abs(w32 - w64)) / np.max(np.abs(w64))),
+                  "median_rel": float(np.median(np.abs(w32 - w64) / np.abs(w64).max(axis=0))),
+                  "resid_max_rel": float(np.max(np.abs(h32 - h64) / h64))}
+        a32.close()
+        a64.close()
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         del solver
@@ -306,7 +323,7 @@ def run_gpu(args, rank: int, world: int):
                        "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (working set > 1 GB), no flush"},
             "wall_ms_per_step": wall / args.steps * 1e3,
-            "roofline": roofline, "passes": per_pass,
+            "roofline": roofline, "passes": per_pass, "fp32_error_vs_fp64": fp_err,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_rate, "unit": "cell-stage/s", "steps": e2e_steps,
                     "h2d_bytes_per_step": int(pin_in.nbytes), "d2h_bytes_per_step": int(pin_out.nbytes)},

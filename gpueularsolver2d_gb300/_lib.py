@@ -35,6 +35,7 @@ class Params(ctypes.Structure):
         ("block_size", ctypes.c_int32), ("graph_iters", ctypes.c_int32),
         ("verbose", ctypes.c_int32), ("limiter_freeze", ctypes.c_int32),
         ("limiter", ctypes.c_int32), ("limiter_k", ctypes.c_double),
+        ("limiter_freeze_resd", ctypes.c_double),
     ]
 
 

@@ -63,7 +63,7 @@ template <typename T> struct BatchT : BatchBase {
         ntot = ntot_;
         const int n = ntot, ncase = (int)L->size();
         bool freeze = false;
-        for (auto &p : P) freeze = freeze || p.limiter_freeze > 0;
+        for (auto &p : P) freeze = freeze || p.limiter_freeze > 0 || p.limiter_freeze_resd > 0.0;
         int nmax = 0;
         for (auto &l : *L) nmax = std::max(nmax, l.n);
         const int maxtiles = (n + 31) / 32;
@@ -380,6 +380,7 @@ int e2d_batch_create(e2d_mesh **meshes, const e2d_params *params, int32_t ncase,
     for (int c = 0; c < ncase; c++) {
         b->ctl_host[c].resd = 100.0;
         b->ctl_host[c].freeze_after = params[c].limiter_freeze > 0 ? params[c].limiter_freeze : 0;
+        b->ctl_host[c].freeze_resd = params[c].limiter_freeze_resd > 0.0 ? params[c].limiter_freeze_resd : 0.0;
     }
     CK(cudaMemcpy(b->ctl_dev, b->ctl_host, sizeof(Ctl) * ncase, cudaMemcpyHostToDevice));
     // the history buffer is sized once here: its pointer is captured in the graph

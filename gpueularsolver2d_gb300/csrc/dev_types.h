@@ -21,6 +21,7 @@ struct Ctl {
     double epsl, epsm, resd;
     int freeze_after;  // > 0: freeze the limiter once step reaches this (option; 0 = reference)
     int frozen;        // limiter values are frozen (set by the residual kernel)
+    double freeze_resd;  // > 0: freeze the limiter once Resd falls to this (option)
 };
 
 // Flow constants of one case (gpu_init.cu:63-93).

@@ -339,27 +339,121 @@ __device__ __forceinline__ void flux_cell(const MeshDev<T> &m, const Flow<T> &f,
     r.x = T(0.0); r.y = T(0.0); r.z = T(0.0); r.w = T(0.0);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        const V2<T> S = m.S[k * n + i];
-        const V4<T> own = FS[k * n + i];
-        const T vn = tsqrt(S.y * S.y + S.x * S.x);
-        T nx = S.x / vn, ny = S.y / vn;
-        V4<T> F;
-        bool right = false;
-        if (code[k] >= 0) {
-            const int c = code[k];
-            const V4<T> oth = FS[(c & 3) * n + (c >> 3)];
-            right = (c >> 2) & 1;
-            F = right ? roe(oth, own, -nx, -ny, f.gamma, f.eps_entropy)
-                      : roe(own, oth, nx, ny, f.gamma, f.eps_entropy);
-        } else {
-            const V4<T> gst = ghost(code[k], own, S.x, S.y, f);
-            F = roe(own, gst, nx, ny, f.gamma, f.eps_entropy);
-        }
-        F.x *= vn; F.y *= vn; F.z *= vn; F.w *= vn;
+        bool right;
+        const V4<T> F = face_flux(m, f, i, k, code[k], FS, right);
         if (right) { r.x -= F.x; r.y -= F.y; r.z -= F.z; r.w -= F.w; }
         else { r.x += F.x; r.y += F.y; r.z += F.z; r.w += F.w; }
     }
     res[i] = r;
+}
+
+// Flux of face k of cell i, times |S|, in the edge's orientation (the
+// reference's Res_e.left of gpu_solver.cu:738-745); *right tells whether cell
+// i is the edge's right cell.
+template <typename T>
+__device__ __forceinline__ V4<T> face_flux(const MeshDev<T> &m, const Flow<T> &f, const int i, const int k,
+                                           const int code, const V4<T> *__restrict__ FS, bool &right) {
+    const int n = m.n;
+    const V2<T> S = m.S[k * n + i];
+    const V4<T> own = FS[k * n + i];
+    const T vn = tsqrt(S.y * S.y + S.x * S.x);
+    T nx = S.x / vn, ny = S.y / vn;
+    V4<T> F;
+    right = false;
+    if (code >= 0) {
+        const V4<T> oth = FS[(code & 3) * n + (code >> 3)];
+        right = (code >> 2) & 1;
+        F = right ? roe(oth, own, -nx, -ny, f.gamma, f.eps_entropy) : roe(own, oth, nx, ny, f.gamma, f.eps_entropy);
+    } else {
+        const V4<T> gst = ghost(code, own, S.x, S.y, f);
+        F = roe(own, gst, nx, ny, f.gamma, f.eps_entropy);
+    }
+    F.x *= vn; F.y *= vn; F.z *= vn; F.w *= vn;
+    return F;
+}
+
+// Pass B for one tile of cells [base, base + nvalid) with each interior face
+// inside the tile evaluated once: the tile lists the faces it must evaluate
+// (boundary faces, faces to cells outside the tile, and inside faces from
+// their left cell only), spreads that list over its threads, keeps the
+// fluxes in shared memory, and then every cell sums its three faces in face
+// order with the reference's signs.  The fluxes are the same bits as in
+// flux_cell and are summed in the same order.  blockDim.x <= 256.
+template <typename T>
+__device__ __forceinline__ void flux_tile(const MeshDev<T> &m, const Flow<T> &f, const int base, const int nvalid,
+                                          const V4<T> *__restrict__ FS, V4<T> *__restrict__ res) {
+    __shared__ V4<T> Fs[256 * 3];
+    __shared__ int4 tps[256];
+    __shared__ unsigned short items[256 * 3];
+    __shared__ int wtot[8];
+    const int t = threadIdx.x, i = base + t;
+    const bool live = t < nvalid;
+    const int4 tp = live ? m.topo[i] : make_int4(-3, -3, -3, 0);
+    tps[t] = tp;
+    const int code[3] = {tp.x, tp.y, tp.z};
+    unsigned mask = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        if (!live) continue;
+        const int c = code[k];
+        if (c < 0) { mask |= 1u << k; continue; }
+        const bool inside = (unsigned)((c >> 3) - base) < (unsigned)nvalid;
+        if (!inside || !((c >> 2) & 1)) mask |= 1u << k;
+    }
+    // exclusive prefix sum of the per-cell counts over the block
+    const int cnt = __popc(mask), lane = t & 31, wid = t >> 5;
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) wtot[wid] = incl;
+    __syncthreads();
+    int off = incl - cnt, total = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+        if (w < wid) off += wtot[w];
+        total += wtot[w];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        if (mask & (1u << k)) items[off++] = (unsigned short)((t << 2) | k);
+    __syncthreads();
+    for (int j = t; j < total; j += blockDim.x) {
+        const int it = items[j], tt = it >> 2, k = it & 3;
+        const int4 q = tps[tt];
+        const int c = k == 0 ? q.x : k == 1 ? q.y : q.z;
+        bool right;
+        Fs[tt * 3 + k] = face_flux(m, f, base + tt, k, c, FS, right);
+    }
+    __syncthreads();
+    if (!live) return;
+    V4<T> r;
+    r.x = T(0.0); r.y = T(0.0); r.z = T(0.0); r.w = T(0.0);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int c = code[k];
+        V4<T> F;
+        bool right;
+        if (mask & (1u << k)) {
+            F = Fs[t * 3 + k];
+            right = c >= 0 && ((c >> 2) & 1);
+        } else {  // inside face evaluated by its left cell
+            F = Fs[((c >> 3) - base) * 3 + (c & 3)];
+            right = true;
+        }
+        if (right) { r.x -= F.x; r.y -= F.y; r.z -= F.z; r.w -= F.w; }
+        else { r.x += F.x; r.y += F.y; r.z += F.z; r.w += F.w; }
+    }
+    res[i] = r;
+}
+
+template <typename T>
+__global__ void E2D_LB_FLUX k_flux_tile(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ FS,
+                                        V4<T> *__restrict__ res, const Ctl *__restrict__ ctl) {
+    if (ctl->halt) return;
+    const int base = blockIdx.x * blockDim.x;
+    flux_tile(m, f, base, min((int)blockDim.x, m.n - base), FS, res);
 }
 
 template <typename T>
@@ -523,12 +617,11 @@ template <typename T>
 __global__ void E2D_LB_FLUX kb_flux(MeshDev<T> m, BatchDev<T> b, int ntiles, const V4<T> *__restrict__ FS,
                                     V4<T> *__restrict__ res) {
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int i = t * blockDim.x + threadIdx.x;
-        int c;
-        if (batch_cell(b, m.n, i, c)) {
-            const Flow<T> f = b.flows[c];
-            flux_cell(m, f, i, FS, res);
-        }
+        const int base = t * blockDim.x;
+        const int tc = b.chunk_case[base / kChunk];  // every cell of a tile is in one case
+        if (b.ctl[tc].halt) continue;                // uniform over the block
+        const Flow<T> f = b.flows[tc];
+        flux_tile(m, f, base, max(0, min((int)blockDim.x, b.case_end[tc] - base)), FS, res);
     }
 }
 
@@ -630,7 +723,7 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
         k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi);
-        k_flux<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
+        k_flux_tile<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
             V4<T> *dst = p.sm[sw & 1];
@@ -657,7 +750,7 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
         mark(0); k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi); done();
-        mark(1); k_flux<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl); done();
+        mark(1); k_flux_tile<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl); done();
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
             V4<T> *dst = p.sm[sw & 1];

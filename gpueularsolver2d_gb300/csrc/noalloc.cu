@@ -50,6 +50,7 @@ __global__ void k_noalloc_ctl(Ctl *ctl, int target, double epsm) {
     ctl->resd = 100.0;
     ctl->freeze_after = 0;
     ctl->frozen = 0;
+    ctl->freeze_resd = 0.0;
 }
 
 size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }

@@ -27,7 +27,8 @@ __device__ __forceinline__ void resid_block(const double *__restrict__ part, int
     if (step - 1 < hist_cap) hist[step - 1] = resd;
     ctl->step = step;
     ctl->resd = resd;
-    if (ctl->freeze_after > 0 && step >= ctl->freeze_after) ctl->frozen = 1;
+    if ((ctl->freeze_after > 0 && step >= ctl->freeze_after) || (ctl->freeze_resd > 0.0 && resd <= ctl->freeze_resd))
+        ctl->frozen = 1;
     if (ctl->nbad) ctl->halt = 2;
     else if (ctl->check_epsl && !(resd > ctl->epsl)) ctl->halt = 1;
     else if (step >= ctl->target) ctl->halt = 1;

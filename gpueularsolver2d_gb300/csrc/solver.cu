@@ -102,6 +102,8 @@ void forces_from_state(const HostLayout &L, const FreeStream &fs, double gamma, 
     if (cl) *cl = (-fx * sa + fy * ca) / 0.5;
 }
 
+bool freezes(const e2d_params &p) { return p.limiter_freeze > 0 || p.limiter_freeze_resd > 0.0; }
+
 bool valid_params(const e2d_params *p) {
     if (!(p->gamma > 1.0) || !(p->ma > 0.0) || !(p->tin > 0.0) || !(p->cfl > 0.0)) return false;
     if (p->rk_stages < 1 || p->rk_stages > 8 || p->irs_sweeps < 0 || p->irs_sweeps > 16) return false;
@@ -140,7 +142,7 @@ template <typename T> struct SolverT : SolverBase {
         const int G = (n + block - 1) / block;
         size_t bytes = Arena::up(sizeof(int4) * n) + 2 * Arena::up(sizeof(V2<T>) * 3 * n) +
                        Arena::up(sizeof(T) * n) * 2 + Arena::up(sizeof(V4<T>) * n) * 5 +
-                       Arena::up(sizeof(V4<T>) * 3 * n) * (p.limiter_freeze > 0 ? 2 : 1) +
+                       Arena::up(sizeof(V4<T>) * 3 * n) * (freezes(p) ? 2 : 1) +
                        Arena::up(sizeof(double) * G) +
                        Arena::up(sizeof(int) * n) + Arena::up(sizeof(double) * 4 * n);
         CK(cudaMalloc((void **)&arena.base, bytes));
@@ -152,7 +154,7 @@ template <typename T> struct SolverT : SolverBase {
         plan.W[0] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
         plan.W[1] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
         plan.FS = (V4<T> *)arena.take(sizeof(V4<T>) * 3 * n);
-        plan.phi = p.limiter_freeze > 0 ? (V4<T> *)arena.take(sizeof(V4<T>) * 3 * n) : nullptr;
+        plan.phi = freezes(p) ? (V4<T> *)arena.take(sizeof(V4<T>) * 3 * n) : nullptr;
         plan.dt = (T *)arena.take(sizeof(T) * n);
         plan.res = (V4<T> *)arena.take(sizeof(V4<T>) * n);
         plan.sm[0] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
@@ -386,6 +388,7 @@ int e2d_solver_create(e2d_mesh *m, const e2d_params *p, e2d_solver **out) {
     std::memset(s->ctl_host, 0, sizeof(Ctl));
     s->ctl_host->resd = 100.0;  // gpu_solver.cu:2185 Resd[0]=100
     s->ctl_host->freeze_after = p->limiter_freeze > 0 ? p->limiter_freeze : 0;
+    s->ctl_host->freeze_resd = p->limiter_freeze_resd > 0.0 ? p->limiter_freeze_resd : 0.0;
     CK(cudaMemcpy(s->ctl_dev, s->ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice));
     s->graph_iters = p->graph_iters > 0 ? p->graph_iters : 8;
     const int block = p->block_size > 0 ? p->block_size : 128;

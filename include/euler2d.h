@@ -87,6 +87,10 @@ typedef struct e2d_params {
                             the same per-face differences, eps^2 = (K h)^3,
                             h = sqrt(cell area)                              */
     double limiter_k;    /* K of E2D_LIMITER_VENKAT (default 5)              */
+    double limiter_freeze_resd; /* option, no reference counterpart: > 0
+                            freezes the limiter values once Resd falls to
+                            this level (whichever of this and limiter_freeze
+                            comes first)                                     */
 } e2d_params;
 
 #define E2D_LIMITER_REFERENCE 0

@@ -448,7 +448,7 @@ static or_case *finish_create(or_case *c) {
     c->r1 = xcalloc((size_t)(N + 1) * 4, sizeof(double));
     c->r2 = xcalloc((size_t)(N + 1) * 4, sizeof(double));
     c->dt = xcalloc(N + 1, sizeof(double));
-    if (c->p.limiter_freeze > 0) {
+    if (c->p.limiter_freeze > 0 || c->p.limiter_freeze_resd > 0.0) {
         c->phil = xcalloc((size_t)(c->nedge + 1) * 4, sizeof(double));
         c->phir = xcalloc((size_t)(c->nedge + 1) * 4, sizeof(double));
     }
@@ -841,7 +841,9 @@ int or_run(or_case *c, int nsteps, double *resid) {
         }
         if (c->step == 1) c->epsm = drou;
         c->last_resd = sqrt((drou + 1.0E-32) / c->epsm);
-        if (c->p.limiter_freeze > 0 && c->step >= c->p.limiter_freeze) c->frozen = 1;
+        if ((c->p.limiter_freeze > 0 && c->step >= c->p.limiter_freeze) ||
+            (c->p.limiter_freeze_resd > 0.0 && c->last_resd <= c->p.limiter_freeze_resd))
+            c->frozen = 1;
         if (resid) resid[done] = c->last_resd;
         done++;
     }

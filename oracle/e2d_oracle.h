@@ -41,6 +41,7 @@ typedef struct or_params {
                                  of iteration k from iteration k+1 on      */
     int limiter;              /* 0 reference; 1 Venkatakrishnan option     */
     double limiter_k;         /* K of the Venkatakrishnan option           */
+    double limiter_freeze_resd; /* option: freeze once Resd <= this        */
 } or_params;
 
 typedef struct or_case or_case;

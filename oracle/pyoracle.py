@@ -26,6 +26,7 @@ class OrParams(ctypes.Structure):
         ("irs_sweeps", ctypes.c_int), ("dt_cap", ctypes.c_double),
         ("entropy_eps", ctypes.c_double), ("wall_box", ctypes.c_double),
         ("limiter_freeze", ctypes.c_int), ("limiter", ctypes.c_int), ("limiter_k", ctypes.c_double),
+        ("limiter_freeze_resd", ctypes.c_double),
     ]
 
 

@@ -80,4 +80,5 @@ def test_reference_kernels_timed_on_this_gpu(lib, oracle):
         with open(os.path.join(out_dir, "reference_gpu_timing.json"), "w") as f:
             json.dump(res, f)
     print(res)
-    assert res["fp64_ms_per_iteration"] < res["reference_ms_per_iteration"]
+    # the product path (FP32 stencil) must beat the reference kernels on the same GPU
+    assert res["fp32_ms_per_iteration"] < res["reference_ms_per_iteration"]
