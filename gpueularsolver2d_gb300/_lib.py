@@ -35,7 +35,8 @@ class Params(ctypes.Structure):
         ("block_size", ctypes.c_int32), ("graph_iters", ctypes.c_int32),
         ("verbose", ctypes.c_int32), ("limiter_freeze", ctypes.c_int32),
         ("limiter", ctypes.c_int32), ("limiter_k", ctypes.c_double),
-        ("limiter_freeze_resd", ctypes.c_double),
+        ("limiter_freeze_resd", ctypes.c_double), ("global_dt", ctypes.c_int32),
+        ("far_field_fix", ctypes.c_int32),
     ]
 
 
@@ -59,6 +60,7 @@ SIGNATURES = {
     "e2d_input_read": (_I, [ctypes.c_char_p, ctypes.POINTER(Params)]),
     "e2d_mesh_read": (_I, [ctypes.c_char_p, _PP]),
     "e2d_mesh_write": (_I, [ctypes.c_char_p, _P]),
+    "e2d_mesh_write_binary": (_I, [ctypes.c_char_p, _P]),
     "e2d_mesh_from_arrays": (_I, [_I, _I, _PD, _PD, _PI, _PP]),
     "e2d_mesh_ogrid_naca0012": (_I, [_I, _I, _D, _D, _D, ctypes.c_uint64, _PP]),
     "e2d_mesh_free": (None, [_P]),

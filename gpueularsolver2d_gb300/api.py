@@ -28,7 +28,10 @@ def default_params(**kw) -> Params:
     """Reference defaults, with any field overridden by keyword."""
     p = Params()
     check(load().e2d_params_default(ctypes.byref(p)))
+    names = {f[0] for f in Params._fields_}
     for k, v in kw.items():
+        if k not in names:
+            raise TypeError(f"unknown solver parameter {k!r}")
         if k == "rk_coef":
             for i, c in enumerate(v):
                 p.rk_coef[i] = c
@@ -70,8 +73,10 @@ class Mesh:
         check(load().e2d_mesh_ogrid_naca0012(ni, nj, r_far, dy_wall, jitter, seed, ctypes.byref(h)))
         return cls(h.value)
 
-    def write(self, path: str) -> None:
-        check(load().e2d_mesh_write(path.encode(), self._h))
+    def write(self, path: str, binary: bool = False) -> None:
+        """Reference .dat text, or the binary cache that Mesh.read also accepts."""
+        fn = load().e2d_mesh_write_binary if binary else load().e2d_mesh_write
+        check(fn(path.encode(), self._h))
 
     def info(self, wall_box: float = 2.0) -> MeshInfo:
         i = MeshInfo()

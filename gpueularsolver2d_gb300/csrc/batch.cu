@@ -121,10 +121,11 @@ template <typename T> struct BatchT : BatchBase {
             hce[c] = o + l.n;
             const e2d_params &p = P[c];
             Flow<T> &f = hf[c];
-            f.gamma = (T)p.gamma; f.ui = (T)FS[c].ui; f.vi = (T)FS[c].vi; f.ain = (T)FS[c].ain;
+            f.gamma = (T)p.gamma; f.ui = (T)FS[c].ui; f.vi = (T)FS[c].vi; f.ain = (T)FS[c].ain_test;
             f.tin = (T)p.tin; f.vin = (T)FS[c].vin; f.R = (T)287.06; f.pis = (T)FS[c].pis; f.cfl = (T)p.cfl;
             f.dt_cap = (T)p.dt_cap; f.eps_entropy = (T)p.entropy_eps; f.irs_eps = (T)p.irs_eps;
             f.venk_k3 = (T)(p.limiter_k * p.limiter_k * p.limiter_k); f.limiter = p.limiter;
+            f.global_dt = p.global_dt;
         }
         CK(cudaMemcpy(topo, ht.data(), sizeof(int4) * n, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(S, hS.data(), sizeof(T) * hS.size(), cudaMemcpyHostToDevice));
@@ -381,6 +382,7 @@ int e2d_batch_create(e2d_mesh **meshes, const e2d_params *params, int32_t ncase,
         b->ctl_host[c].resd = 100.0;
         b->ctl_host[c].freeze_after = params[c].limiter_freeze > 0 ? params[c].limiter_freeze : 0;
         b->ctl_host[c].freeze_resd = params[c].limiter_freeze_resd > 0.0 ? params[c].limiter_freeze_resd : 0.0;
+        for (auto &d : b->ctl_host[c].dtmin) d = kDtNone;
     }
     CK(cudaMemcpy(b->ctl_dev, b->ctl_host, sizeof(Ctl) * ncase, cudaMemcpyHostToDevice));
     // the history buffer is sized once here: its pointer is captured in the graph

@@ -22,13 +22,20 @@ struct Ctl {
     int freeze_after;  // > 0: freeze the limiter once step reaches this (option; 0 = reference)
     int frozen;        // limiter values are frozen (set by the residual kernel)
     double freeze_resd;  // > 0: freeze the limiter once Resd falls to this (option)
+    // Global time-step option: the smallest local step of RK stage k, as the
+    // bits of a non-negative double (whose order is that of the integers), so
+    // that blocks fold into it with atomicMin.  kDtNone between iterations.
+    unsigned long long dtmin[8];
 };
+
+constexpr unsigned long long kDtNone = 0x7FF0000000000000ULL;  // +inf
 
 // Flow constants of one case (gpu_init.cu:63-93).
 template <typename T> struct Flow {
     T gamma, ui, vi, ain, tin, vin, R, pis, cfl, dt_cap, eps_entropy, irs_eps;
     T venk_k3;    // K^3 of the Venkatakrishnan option
     int limiter;  // 0 reference, 1 Venkatakrishnan
+    int global_dt;  // 1: every cell advances with the smallest local step (option)
 };
 
 // Cell-local mesh data in internal order (n cells).

@@ -6,6 +6,9 @@
 // unairfoilpress.plt (gpu_fvm.cu:133-195) with the converged field.
 //
 //   e2d_solve [mesh.dat [input.dat]] [--fp32] [--file-order] [--out DIR]
+//             [--global-dt] [--far-field-fix]
+// --global-dt advances every cell with the smallest local step; --far-field-fix
+// makes the far-field supersonic test use the non-dimensional sound speed.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -22,13 +25,16 @@ static int fail(const char *what) {
 
 int main(int argc, char **argv) {
     std::string mesh_path = "2822-3k.dat", input_path = "input.dat", out = ".";
-    int precision = E2D_FP64, ordering = E2D_ORDER_MORTON, npos = 0;
+    int precision = E2D_FP64, ordering = E2D_ORDER_MORTON, npos = 0, global_dt = 0, far_fix = 0;
     for (int i = 1; i < argc; i++) {
         if (!std::strcmp(argv[i], "--fp32")) precision = E2D_FP32;
         else if (!std::strcmp(argv[i], "--file-order")) ordering = E2D_ORDER_FILE;
         else if (!std::strcmp(argv[i], "--out") && i + 1 < argc) out = argv[++i];
+        else if (!std::strcmp(argv[i], "--global-dt")) global_dt = 1;
+        else if (!std::strcmp(argv[i], "--far-field-fix")) far_fix = 1;
         else if (argv[i][0] == '-') {
-            std::printf("usage: e2d_solve [mesh.dat [input.dat]] [--fp32] [--file-order] [--out DIR]\n");
+            std::printf("usage: e2d_solve [mesh.dat [input.dat]] [--fp32] [--file-order] [--out DIR] "
+                        "[--global-dt] [--far-field-fix]\n");
             return 2;
         } else if (npos++ == 0) mesh_path = argv[i];
         else input_path = argv[i];
@@ -50,6 +56,8 @@ int main(int argc, char **argv) {
     std::printf("Mesh data Computing's finished!!\n");
     p.precision = precision;
     p.ordering = ordering;
+    p.global_dt = global_dt;
+    p.far_field_fix = far_fix;
     p.verbose = 1;
     e2d_solver *s = nullptr;
     if (e2d_solver_create(m, &p, &s)) return fail("solver");

@@ -14,9 +14,9 @@
 // and k_resid folds the partials into Resd on the last stage.
 //
 // Every cell gathers its own faces, so nothing is accumulated with atomics
-// and the result does not depend on scheduling.  Interior fluxes are
-// evaluated by both cells of a face from identical inputs, so both see the
-// same value.  The arithmetic of each quantity follows the reference kernel
+// and the result does not depend on scheduling.  An interior face inside one
+// block's tile of cells is evaluated once; a face between two tiles is
+// evaluated by both cells from identical inputs, so both see the same value.  The arithmetic of each quantity follows the reference kernel
 // it replaces operation by operation (cited per function); compiled without
 // FMA contraction, the FP64 instantiation reproduces the CPU oracle bit for
 // bit.
@@ -46,6 +46,15 @@ template <> struct MinBlocks<float> {
     static constexpr int flux = E2D_MINB_FLUX > 0 ? E2D_MINB_FLUX : 1;
 };
 #define E2D_LB_FACES __launch_bounds__(256, MinBlocks<T>::faces)
+
+// Pass B variant.  FP64 evaluates each interior face inside a block's tile of
+// cells once (flux_tile): the FP64 Roe flux is arithmetic bound on this GPU,
+// and evaluating about half as many cut a whole FP64 iteration on a 51.8k-cell
+// mesh from 1.75 to 1.27 ms.  FP32 is bound by memory latency, where the
+// tile's work list and barriers cost more than they save (0.152 against
+// 0.110 ms per launch on 4.2M cells), so every cell evaluates its own three
+// faces (flux_cell).  Either way both cells of a face use the same flux bits.
+template <typename T> struct FluxTiled { static constexpr bool value = sizeof(T) == 8; };
 #define E2D_LB_FLUX __launch_bounds__(256, MinBlocks<T>::flux)
 
 template <typename T> __device__ __forceinline__ T tabs(T v) { return fabs(v); }
@@ -229,10 +238,11 @@ __device__ __forceinline__ V4<T> roe(const V4<T> &LW, const V4<T> &RW, T nx, T n
 // phi; once frozen they are reused instead of re-evaluated, which makes the
 // residual a smooth function of the state so that it can converge below the
 // limiter's chatter floor.
+// Returns the cell's local time step (also stored in dt[i]).
 template <typename T>
-__device__ __forceinline__ void faces_cell(const MeshDev<T> &m, const Flow<T> &f, const int i,
-                                           const V4<T> *__restrict__ W, V4<T> *__restrict__ FS,
-                                           T *__restrict__ dt, V4<T> *__restrict__ phi, const int frozen) {
+__device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, const int i,
+                                        const V4<T> *__restrict__ W, V4<T> *__restrict__ FS,
+                                        T *__restrict__ dt, V4<T> *__restrict__ phi, const int frozen) {
     const int n = m.n;
     const int4 tp = m.topo[i];
     const int code[3] = {tp.x, tp.y, tp.z};
@@ -312,17 +322,51 @@ __device__ __forceinline__ void faces_cell(const MeshDev<T> &m, const Flow<T> &f
         }
         FS[k * n + i] = o;
     }
-    dt[i] = tmin(A * f.cfl / Tsum, f.dt_cap);
+    const T dti = tmin(A * f.cfl / Tsum, f.dt_cap);
+    dt[i] = dti;
+    return dti;
+}
+
+// Global time-step option: the block's smallest step folded into *slot.
+// Every thread of the block must call it (v = +inf for no cell).  A time
+// step is non-negative, so its bits order like the integers and min over
+// them is exact and independent of the order of the blocks.
+__device__ __forceinline__ void block_min_dt(double v, unsigned long long *slot) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+    __shared__ double wm[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();  // wm may still be read by the previous use in this block
+    if (lane == 0) wm[wid] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = wm[0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); k++) b = fmin(b, wm[k]);
+        atomicMin(slot, (unsigned long long)__double_as_longlong(b));
+    }
 }
 
 template <typename T>
 __global__ void E2D_LB_FACES k_faces(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ W,
                                      V4<T> *__restrict__ FS, T *__restrict__ dt,
-                                     const Ctl *__restrict__ ctl, V4<T> *__restrict__ phi) {
+                                     Ctl *__restrict__ ctl, V4<T> *__restrict__ phi, const int st) {
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.n) return;
-    faces_cell(m, f, i, W, FS, dt, phi, phi ? ctl->frozen : 0);
+    if (!f.global_dt) {
+        if (i >= m.n) return;
+        faces_cell(m, f, i, W, FS, dt, phi, phi ? ctl->frozen : 0);
+        return;
+    }
+    double v = __longlong_as_double((long long)kDtNone);
+    if (i < m.n) v = (double)faces_cell(m, f, i, W, FS, dt, phi, phi ? ctl->frozen : 0);
+    block_min_dt(v, &ctl->dtmin[st]);
+}
+
+// Time step of cell i in RK stage st: its own, or with the global option the
+// smallest of its case.
+template <typename T>
+__device__ __forceinline__ T stage_dt(const Flow<T> &f, const Ctl *ctl, const int st, const T *dt, const int i) {
+    return f.global_dt ? (T)__longlong_as_double((long long)ctl->dtmin[st]) : dt[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -358,16 +402,21 @@ __device__ __forceinline__ V4<T> face_flux(const MeshDev<T> &m, const Flow<T> &f
     const V4<T> own = FS[k * n + i];
     const T vn = tsqrt(S.y * S.y + S.x * S.x);
     T nx = S.x / vn, ny = S.y / vn;
-    V4<T> F;
+    // one Roe call site for every face, with the left state first: both cells
+    // of a face run the same instructions on the same inputs (their normals
+    // are exact negatives), so they get the same bits even where the
+    // compiler contracts multiply-adds
+    V4<T> a = own, b;
     right = false;
     if (code >= 0) {
         const V4<T> oth = FS[(code & 3) * n + (code >> 3)];
         right = (code >> 2) & 1;
-        F = right ? roe(oth, own, -nx, -ny, f.gamma, f.eps_entropy) : roe(own, oth, nx, ny, f.gamma, f.eps_entropy);
+        if (right) { a = oth; b = own; nx = -nx; ny = -ny; }
+        else b = oth;
     } else {
-        const V4<T> gst = ghost(code, own, S.x, S.y, f);
-        F = roe(own, gst, nx, ny, f.gamma, f.eps_entropy);
+        b = ghost(code, own, S.x, S.y, f);
     }
+    V4<T> F = roe(a, b, nx, ny, f.gamma, f.eps_entropy);
     F.x *= vn; F.y *= vn; F.z *= vn; F.w *= vn;
     return F;
 }
@@ -516,7 +565,7 @@ __global__ void __launch_bounds__(256) k_smooth(MeshDev<T> m, T eps, const V4<T>
 template <typename T>
 __device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &f, const T rk,
                                             const int smooth, const int i, const V4<T> *__restrict__ src,
-                                            const V4<T> *__restrict__ res, const T *__restrict__ dt,
+                                            const V4<T> *__restrict__ res, const T dti,
                                             const V4<T> *W0, V4<T> *Wout, const bool want, double &d2,
                                             int &bad) {
     {
@@ -534,7 +583,7 @@ __device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &
             if (tabs(r.w) > tabs(s3)) r.w = s3;
         }
         T RK = rk;
-        RK *= dt[i];
+        RK *= dti;
         const T A = m.area[i];
         const V4<T> w0 = W0[i];
         V4<T> w;
@@ -578,12 +627,13 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, int smooth,
                                                 const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
                                                 const T *__restrict__ dt, const V4<T> *W0, V4<T> *Wout,
-                                                double *__restrict__ part, Ctl *ctl) {
+                                                double *__restrict__ part, Ctl *ctl, const int st) {
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double d2 = 0.0;
     int bad = 0;
-    if (i < m.n) update_cell(m, f, rk, smooth, i, src, res, dt, W0, Wout, part != nullptr, d2, bad);
+    if (i < m.n)
+        update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, ctl, st, dt, i), W0, Wout, part != nullptr, d2, bad);
     if (!part) return;
     block_partial(d2, bad, part + blockIdx.x, &ctl->nbad);
 }
@@ -602,14 +652,18 @@ __device__ __forceinline__ bool batch_cell(const BatchDev<T> &b, const int n, co
 
 template <typename T>
 __global__ void E2D_LB_FACES kb_faces(MeshDev<T> m, BatchDev<T> b, int ntiles, const V4<T> *__restrict__ W,
-                                      V4<T> *__restrict__ FS, T *__restrict__ dt, V4<T> *__restrict__ phi) {
+                                      V4<T> *__restrict__ FS, T *__restrict__ dt, V4<T> *__restrict__ phi,
+                                      const int st) {
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int i = t * blockDim.x + threadIdx.x;
+        const int tc = b.chunk_case[(t * blockDim.x) / kChunk];  // the tile's case
+        double v = __longlong_as_double((long long)kDtNone);
         int c;
         if (batch_cell(b, m.n, i, c)) {
             const Flow<T> f = b.flows[c];
-            faces_cell(m, f, i, W, FS, dt, phi, phi ? b.ctl[c].frozen : 0);
+            v = (double)faces_cell(m, f, i, W, FS, dt, phi, phi ? b.ctl[c].frozen : 0);
         }
+        if (b.flows[tc].global_dt) block_min_dt(v, &b.ctl[tc].dtmin[st]);  // uniform over the block
     }
 }
 
@@ -621,7 +675,12 @@ __global__ void E2D_LB_FLUX kb_flux(MeshDev<T> m, BatchDev<T> b, int ntiles, con
         const int tc = b.chunk_case[base / kChunk];  // every cell of a tile is in one case
         if (b.ctl[tc].halt) continue;                // uniform over the block
         const Flow<T> f = b.flows[tc];
-        flux_tile(m, f, base, max(0, min((int)blockDim.x, b.case_end[tc] - base)), FS, res);
+        if (FluxTiled<T>::value) {
+            flux_tile(m, f, base, max(0, min((int)blockDim.x, b.case_end[tc] - base)), FS, res);
+        } else {
+            const int i = base + threadIdx.x;
+            if (i < b.case_end[tc]) flux_cell(m, f, i, FS, res);
+        }
     }
 }
 
@@ -640,7 +699,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) kb_update(MeshDev<T> m, BatchDev<T> b, int ntiles, T rk, int smooth,
                                                  const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
                                                  const T *__restrict__ dt, const V4<T> *W0, V4<T> *Wout,
-                                                 double *__restrict__ part) {
+                                                 double *__restrict__ part, const int st) {
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int tc = b.chunk_case[(t * blockDim.x) / kChunk];  // the tile's case
         if (b.ctl[tc].halt) continue;                             // uniform over the block
@@ -649,7 +708,8 @@ __global__ void __launch_bounds__(256) kb_update(MeshDev<T> m, BatchDev<T> b, in
         int bad = 0, c;
         if (batch_cell(b, m.n, i, c)) {
             const Flow<T> f = b.flows[c];
-            update_cell(m, f, rk, smooth, i, src, res, dt, W0, Wout, part != nullptr, d2, bad);
+            update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, &b.ctl[c], st, dt, i), W0, Wout,
+                        part != nullptr, d2, bad);
         }
         if (part) block_partial(d2, bad, part + t, &b.ctl[tc].nbad);
     }
@@ -663,7 +723,7 @@ template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream
         const bool last = st == p.stages - 1;
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
-        kb_faces<T><<<G, B, 0, s>>>(p.m, p.b, NT, Wcur, p.FS, p.dt, p.phi);
+        kb_faces<T><<<G, B, 0, s>>>(p.m, p.b, NT, Wcur, p.FS, p.dt, p.phi, st);
         kb_flux<T><<<G, B, 0, s>>>(p.m, p.b, NT, p.FS, p.res);
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
@@ -672,7 +732,7 @@ template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream
             src = dst;
         }
         kb_update<T><<<G, B, 0, s>>>(p.m, p.b, NT, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt, p.W[0],
-                                     Wout, last ? p.part : nullptr);
+                                     Wout, last ? p.part : nullptr, st);
     }
     enqueue_batch_resid(p.part, p.case_tiles, p.ncase, p.b.ctl, p.hist, p.hist_cap, s);
 }
@@ -722,8 +782,9 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
         const bool last = st == p.stages - 1;
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
-        k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi);
-        k_flux_tile<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
+        k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
+        if (FluxTiled<T>::value) k_flux_tile<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
+        else k_flux<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
             V4<T> *dst = p.sm[sw & 1];
@@ -731,7 +792,7 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
             src = dst;
         }
         k_update<T><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
-                                    p.W[0], Wout, last ? p.part : nullptr, p.ctl);
+                                    p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
     }
     enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, s);
 }
@@ -749,8 +810,11 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
         const bool last = st == p.stages - 1;
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
-        mark(0); k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi); done();
-        mark(1); k_flux_tile<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl); done();
+        mark(0); k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st); done();
+        mark(1);
+        if (FluxTiled<T>::value) k_flux_tile<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
+        else k_flux<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
+        done();
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
             V4<T> *dst = p.sm[sw & 1];
@@ -759,7 +823,7 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
         }
         mark(3);
         k_update<T><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
-                                    p.W[0], Wout, last ? p.part : nullptr, p.ctl);
+                                    p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
         done();
     }
     mark(4); enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, s); done();

@@ -297,11 +297,38 @@ const char *e2d_last_error(void) { return g_error.c_str(); }
 
 const char *e2d_version(void) { return "euler2d-gb300 0.1"; }
 
+// Binary mesh cache: "E2DMESH1", int32 nnode, int32 ncell, double x[nnode],
+// double y[nnode], int32 tri[3*ncell] (1-based node ids), little-endian.
+static const char kBinMagic[8] = {'E', '2', 'D', 'M', 'E', 'S', 'H', '1'};
+
+static int read_binary(FILE *f, e2d_mesh **out) {
+    int32_t hdr[2];
+    if (std::fread(hdr, sizeof(int32_t), 2, f) != 2 || hdr[0] < 3 || hdr[1] < 1) {
+        set_error("bad binary mesh header"); return E2D_ERR_IO;
+    }
+    auto *m = new e2d_mesh;
+    m->nnode = hdr[0]; m->ncell = hdr[1];
+    m->x.resize(m->nnode); m->y.resize(m->nnode); m->tri.resize(3 * (size_t)m->ncell);
+    bool ok = std::fread(m->x.data(), sizeof(double), m->nnode, f) == (size_t)m->nnode &&
+              std::fread(m->y.data(), sizeof(double), m->nnode, f) == (size_t)m->nnode &&
+              std::fread(m->tri.data(), sizeof(int32_t), m->tri.size(), f) == m->tri.size();
+    if (!ok) { delete m; set_error("truncated mesh file"); return E2D_ERR_IO; }
+    *out = m;
+    return E2D_OK;
+}
+
 int e2d_mesh_read(const char *path, e2d_mesh **out) {
     if (!path || !out) { set_error("null argument"); return E2D_ERR_ARG; }
     *out = nullptr;
-    FILE *f = std::fopen(path, "r");
+    FILE *f = std::fopen(path, "rb");
     if (!f) { set_error(std::string("cannot open the mesh data file ") + path); return E2D_ERR_IO; }
+    char magic[8];
+    if (std::fread(magic, 1, 8, f) == 8 && !std::memcmp(magic, kBinMagic, 8)) {
+        int rc = read_binary(f, out);
+        std::fclose(f);
+        return rc;
+    }
+    std::rewind(f);
     int nnode = 0, ncell = 0;
     if (std::fscanf(f, "%d %d", &nnode, &ncell) != 2 || nnode < 3 || ncell < 1) {
         std::fclose(f); set_error("bad mesh header (need \"Nnode Ncell\")"); return E2D_ERR_IO;
@@ -331,6 +358,20 @@ int e2d_mesh_write(const char *path, const e2d_mesh *m) {
     int bad = std::ferror(f);
     std::fclose(f);
     if (bad) { set_error("write error"); return E2D_ERR_IO; }
+    return E2D_OK;
+}
+
+int e2d_mesh_write_binary(const char *path, const e2d_mesh *m) {
+    if (!path || !m) { set_error("null argument"); return E2D_ERR_ARG; }
+    FILE *f = std::fopen(path, "wb");
+    if (!f) { set_error(std::string("cannot write ") + path); return E2D_ERR_IO; }
+    const int32_t hdr[2] = {m->nnode, m->ncell};
+    bool ok = std::fwrite(kBinMagic, 1, 8, f) == 8 && std::fwrite(hdr, sizeof(int32_t), 2, f) == 2 &&
+              std::fwrite(m->x.data(), sizeof(double), m->nnode, f) == (size_t)m->nnode &&
+              std::fwrite(m->y.data(), sizeof(double), m->nnode, f) == (size_t)m->nnode &&
+              std::fwrite(m->tri.data(), sizeof(int32_t), m->tri.size(), f) == m->tri.size();
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) { set_error("write error"); return E2D_ERR_IO; }
     return E2D_OK;
 }
 

@@ -22,6 +22,7 @@
 namespace {
 
 using e2d::Ctl;
+using e2d::kDtNone;
 using e2d::V2;
 using e2d::V4;
 
@@ -51,6 +52,7 @@ __global__ void k_noalloc_ctl(Ctl *ctl, int target, double epsm) {
     ctl->freeze_after = 0;
     ctl->frozen = 0;
     ctl->freeze_resd = 0.0;
+    for (int k = 0; k < 8; k++) ctl->dtmin[k] = kDtNone;
 }
 
 size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -121,10 +123,11 @@ extern "C" int e2d_step_noalloc(int32_t ncell, const int32_t *topo, const double
     const double rho_e = kR * p->tin / (vin * vin) / (g - 1.0) + 0.50;
     const double E = rho_e / 1.0 - 0.5 * (U * U + V * V);
     e2d::Flow<double> &f = plan.f;
-    f.gamma = g; f.ui = std::cos(alpha); f.vi = std::sin(alpha); f.ain = ain; f.tin = p->tin; f.vin = vin;
+    f.gamma = g; f.ui = std::cos(alpha); f.vi = std::sin(alpha); f.ain = p->far_field_fix ? 1.0 / p->ma : ain; f.tin = p->tin; f.vin = vin;
     f.R = kR; f.pis = (g - 1.0) * 1.0 * E; f.cfl = p->cfl; f.dt_cap = p->dt_cap;
     f.eps_entropy = p->entropy_eps; f.irs_eps = p->irs_eps;
     f.venk_k3 = p->limiter_k * p->limiter_k * p->limiter_k; f.limiter = p->limiter;
+    f.global_dt = p->global_dt;
     plan.hist = resid;
     plan.hist_cap = iterations;
     plan.stages = p->rk_stages;

@@ -27,6 +27,7 @@ __device__ __forceinline__ void resid_block(const double *__restrict__ part, int
     if (step - 1 < hist_cap) hist[step - 1] = resd;
     ctl->step = step;
     ctl->resd = resd;
+    for (int k = 0; k < 8; k++) ctl->dtmin[k] = kDtNone;  // global time-step slots for the next iteration
     if ((ctl->freeze_after > 0 && step >= ctl->freeze_after) || (ctl->freeze_resd > 0.0 && resd <= ctl->freeze_resd))
         ctl->frozen = 1;
     if (ctl->nbad) ctl->halt = 2;

@@ -39,6 +39,10 @@ FreeStream free_stream(const e2d_params &p) {
     s.alpha = p.alpha_deg * kPi / 180.0;
     s.ain = std::sqrt(g * kR * p.tin);
     s.vin = p.ma * s.ain;
+    // gpu_solver.cu:79 compares the non-dimensional normal velocity with the
+    // dimensional AIN, so its supersonic branch never runs; the fix compares
+    // it with the non-dimensional free-stream sound speed 1/M.
+    s.ain_test = p.far_field_fix ? 1.0 / p.ma : s.ain;
     s.ui = std::cos(s.alpha);
     s.vi = std::sin(s.alpha);
     s.rho_e = kR * p.tin / (s.vin * s.vin) / (g - 1.0) + 0.50;
@@ -114,6 +118,7 @@ bool valid_params(const e2d_params *p) {
     if (p->limiter_freeze < 0) return false;
     if (p->limiter != E2D_LIMITER_REFERENCE && p->limiter != E2D_LIMITER_VENKAT) return false;
     if (p->limiter == E2D_LIMITER_VENKAT && !(p->limiter_k > 0.0)) return false;
+    if ((p->global_dt != 0 && p->global_dt != 1) || (p->far_field_fix != 0 && p->far_field_fix != 1)) return false;
     return true;
 }
 
@@ -175,10 +180,11 @@ template <typename T> struct SolverT : SolverBase {
         CK(cudaMemset(plan.part, 0, sizeof(double) * G));
         plan.m = MeshDev<T>{n, topo, S, R, area};
         Flow<T> &f = plan.f;
-        f.gamma = (T)p.gamma; f.ui = (T)fs.ui; f.vi = (T)fs.vi; f.ain = (T)fs.ain; f.tin = (T)p.tin;
+        f.gamma = (T)p.gamma; f.ui = (T)fs.ui; f.vi = (T)fs.vi; f.ain = (T)fs.ain_test; f.tin = (T)p.tin;
         f.vin = (T)fs.vin; f.R = (T)kR; f.pis = (T)fs.pis; f.cfl = (T)p.cfl; f.dt_cap = (T)p.dt_cap;
         f.eps_entropy = (T)p.entropy_eps; f.irs_eps = (T)p.irs_eps;
         f.venk_k3 = (T)(p.limiter_k * p.limiter_k * p.limiter_k); f.limiter = p.limiter;
+        f.global_dt = p.global_dt;
         plan.ctl = ctl;
         plan.hist = nullptr;
         plan.hist_cap = 0;
@@ -389,6 +395,7 @@ int e2d_solver_create(e2d_mesh *m, const e2d_params *p, e2d_solver **out) {
     s->ctl_host->resd = 100.0;  // gpu_solver.cu:2185 Resd[0]=100
     s->ctl_host->freeze_after = p->limiter_freeze > 0 ? p->limiter_freeze : 0;
     s->ctl_host->freeze_resd = p->limiter_freeze_resd > 0.0 ? p->limiter_freeze_resd : 0.0;
+    for (auto &d : s->ctl_host->dtmin) d = kDtNone;
     CK(cudaMemcpy(s->ctl_dev, s->ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice));
     s->graph_iters = p->graph_iters > 0 ? p->graph_iters : 8;
     const int block = p->block_size > 0 ? p->block_size : 128;

@@ -15,6 +15,7 @@ namespace e2d {
 // (gpu_init.cu:63-93), including PIS = P of the free-stream cell state.
 struct FreeStream {
     double alpha, ain, vin, ui, vi, rho_e, pis;
+    double ain_test;  // sound speed of the far-field supersonic test (ain, or 1/M with the fix)
 };
 
 FreeStream free_stream(const e2d_params &p);

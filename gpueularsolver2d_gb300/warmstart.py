@@ -55,13 +55,18 @@ def freestream(mach: float, alpha_deg: float, ncell: int) -> np.ndarray:
 
 @dataclass
 class SolverSettings:
-    """Solver settings shared by every run of the pipeline.  The default is the
-    smooth (Venkatakrishnan-type) limiter option: unlike the reference limiter
-    it lets the residual fall to 1e-6, and unlike a frozen limiter its
-    converged state does not depend on the starting state, so warm and
-    free-stream runs converge to the same solution."""
+    """Solver settings shared by every run of the pipeline.
+
+    The reference limiter chatters: its residual stalls near 1e-3, and freezing
+    it early leaves a converged state that depends on where the run started.
+    The default is therefore the smooth (Venkatakrishnan-type) limiter option,
+    frozen once Resd reaches 1e-3 (the smooth limiter alone still stalls near
+    5e-4).  On the 256 x 64 O-grid at M 0.6, alpha 1 in FP64 this reaches a
+    1e-6 drop in about 65k iterations, and runs started from the free stream
+    and from a nearby solution end within 3e-5 in CL and 1e-6 in CD."""
     cfl: float = 3.0
     freeze: int = 0
+    freeze_resd: float = 1e-3
     precision: int = e2d.E2D_FP32
     limiter: int = 1
     limiter_k: float = 5.0
@@ -69,7 +74,8 @@ class SolverSettings:
     def params(self, mach, alpha, maxstep=100000):
         return e2d.default_params(ma=mach, alpha_deg=alpha, cfl=self.cfl, precision=self.precision,
                                   ordering=e2d.E2D_ORDER_MORTON, limiter_freeze=self.freeze, maxstep=maxstep,
-                                  limiter=self.limiter, limiter_k=self.limiter_k)
+                                  limiter=self.limiter, limiter_k=self.limiter_k,
+                                  limiter_freeze_resd=self.freeze_resd)
 
 
 def generate(mesh, conds, settings: SolverSettings, iters: int, chunk: int = 128, log=print):
@@ -181,7 +187,7 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=20000)
     ap.add_argument("--batch", type=int, default=65536)
     ap.add_argument("--target", type=float, default=1e-6)
-    ap.add_argument("--maxit", type=int, default=60000)
+    ap.add_argument("--maxit", type=int, default=120000)
     ap.add_argument("--mach", type=float, nargs=2, default=(0.5, 0.7))
     ap.add_argument("--alpha", type=float, nargs=2, default=(-1.0, 3.0))
     ap.add_argument("--json", default=None)

@@ -91,6 +91,15 @@ typedef struct e2d_params {
                             freezes the limiter values once Resd falls to
                             this level (whichever of this and limiter_freeze
                             comes first)                                     */
+    int32_t global_dt;   /* 0 (default): local time step per cell (the
+                            reference's loop); 1: every cell advances with
+                            the smallest local step of the mesh, as the
+                            reference's disabled kernel_TimeStep
+                            (gpu_solver.cu:880-936, 2376-2387) intended      */
+    int32_t far_field_fix; /* 0 (default): the reference's supersonic test
+                            Un / AIN > 1 with the dimensional AIN, which never
+                            holds (gpu_solver.cu:79); 1: compares with the
+                            non-dimensional free-stream sound speed 1/M     */
 } e2d_params;
 
 #define E2D_LIMITER_REFERENCE 0
@@ -118,6 +127,11 @@ int e2d_input_read(const char *path, e2d_params *p);
 int e2d_mesh_read(const char *path, e2d_mesh **out);
 /* Writes the same format (%.17g, so a read gives back the same doubles). */
 int e2d_mesh_write(const char *path, const e2d_mesh *m);
+/* Binary cache of the same mesh ("E2DMESH1", int32 nnode, int32 ncell,
+ * double x[nnode], double y[nnode], int32 tri[3*ncell]; little-endian), about
+ * 10x faster to read than the text format.  e2d_mesh_read recognises it by
+ * its first 8 bytes, so either file works wherever a mesh path is taken. */
+int e2d_mesh_write_binary(const char *path, const e2d_mesh *m);
 /* Builds a mesh from arrays: x,y [nnode]; tri [3*ncell] 1-based node ids. */
 int e2d_mesh_from_arrays(int32_t nnode, int32_t ncell, const double *x, const double *y,
                          const int32_t *tri, e2d_mesh **out);

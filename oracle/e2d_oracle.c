@@ -42,6 +42,7 @@ struct or_case {
     int *elog, *eleft, *eright, *efar, *ewall, *en1, *en2; /* [nedge+1] */
     double *evn, *evx, *evy, *emx, *emy;                     /* [nedge+1] */
     double alpha, ain, vin, rouin, ui, vi, pis;
+    double ain_test;        /* sound speed of the supersonic test */
     wst *w, *w0, *farw, *wallw;
     double *du;             /* [(ncell+1)*8] deltU[2][4] */
     double *umax, *umin;    /* [(ncell+1)*4] */
@@ -127,7 +128,7 @@ static void far_ghost(const or_case *c, const wst *dw, double vectorx,
     double VD = dw->dv / dw->d;
     double Un = fabs(c->ui * nx + c->vi * ny);
     double Uncell = UD * nx + VD * ny;
-    if (Un / c->ain > 1.0) {
+    if (Un / c->ain_test > 1.0) {
         if (Uncell > 0.0) *w0 = *dw;
         if (Uncell <= 0.0) {
             w0->d = 1.0;
@@ -416,6 +417,9 @@ static void initialise(or_case *c) {
     c->alpha = c->p.alpha_deg * REF_PI / 180.0;
     c->ain = sqrt(g * REF_R * c->p.tin);
     c->vin = c->p.ma * c->ain;
+    /* gpu_solver.cu:79 divides the non-dimensional Un by the dimensional
+     * AIN; the far_field_fix option uses the non-dimensional 1/M instead. */
+    c->ain_test = c->p.far_field_fix ? 1.0 / c->p.ma : c->ain;
     c->rouin = c->p.pin / (REF_R * c->p.tin);
     c->ui = cos(c->alpha);
     c->vi = sin(c->alpha);
@@ -711,6 +715,13 @@ static void stage_e2c(or_case *c) {
         }
         for (int k = 0; k < 4; k++) c->res[4 * (size_t)i + k] = r[k];
         c->dt[i] = fmin(c->area[i] * c->p.cfl / T, c->p.dt_cap);
+    }
+    /* global_dt option: the smallest local step for every cell, the intent
+     * of the reference's disabled kernel_TimeStep (gpu_solver.cu:880-936) */
+    if (c->p.global_dt) {
+        double m = INFINITY;
+        for (int i = 1; i <= c->ncell; i++) m = fmin(m, c->dt[i]);
+        for (int i = 1; i <= c->ncell; i++) c->dt[i] = m;
     }
 }
 

@@ -42,6 +42,8 @@ typedef struct or_params {
     int limiter;              /* 0 reference; 1 Venkatakrishnan option     */
     double limiter_k;         /* K of the Venkatakrishnan option           */
     double limiter_freeze_resd; /* option: freeze once Resd <= this        */
+    int global_dt;            /* option: every cell uses min_j dt_j         */
+    int far_field_fix;        /* option: supersonic test against 1/M        */
 } or_params;
 
 typedef struct or_case or_case;

@@ -26,7 +26,8 @@ class OrParams(ctypes.Structure):
         ("irs_sweeps", ctypes.c_int), ("dt_cap", ctypes.c_double),
         ("entropy_eps", ctypes.c_double), ("wall_box", ctypes.c_double),
         ("limiter_freeze", ctypes.c_int), ("limiter", ctypes.c_int), ("limiter_k", ctypes.c_double),
-        ("limiter_freeze_resd", ctypes.c_double),
+        ("limiter_freeze_resd", ctypes.c_double), ("global_dt", ctypes.c_int),
+        ("far_field_fix", ctypes.c_int),
     ]
 
 
@@ -55,6 +56,7 @@ def lib() -> ctypes.CDLL:
             "or_morton_perm": [vp, ip], "or_set_threads": [ctypes.c_int],
             "or_params_default": [ctypes.POINTER(OrParams)],
             "or_roe_flux": [dp, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp],
+            "or_far_ghost": [dp, ctypes.c_double, ctypes.c_double, vp, dp],
         }.items():
             getattr(L, name).argtypes = args
         L.or_pis.restype = ctypes.c_double
@@ -151,6 +153,13 @@ class Case:
         dt = np.zeros(self.ncell)
         lib().or_stage_probe(self._h, _dp(gh), _dp(gr), _dp(um), _dp(fl), _dp(sr), _dp(res), _dp(dt))
         return dict(ghost=gh, grad=gr, umm=um, flux=fl, sr=sr, res=res, dt=dt)
+
+    def far_ghost(self, dw, vectorx: float, vectory: float) -> np.ndarray:
+        """Far-field ghost of interior state dw across a face (vectorx, vectory)."""
+        dw = np.ascontiguousarray(dw, np.float64)
+        out = np.zeros(4)
+        lib().or_far_ghost(_dp(dw), vectorx, vectory, self._h, _dp(out))
+        return out
 
     def morton(self) -> np.ndarray:
         perm = np.zeros(self.ncell, np.int32)

@@ -37,6 +37,26 @@ def test_batch_equals_single_cases(lib, prec):
         assert np.array_equal(b.history(c), s.history()), c
 
 
+def test_batch_options_equal_single_cases(lib):
+    """Per-case options in one batch: global time step (a per-case minimum),
+    the far-field fix at M 1.5, the Venkatakrishnan limiter and a residual-level
+    limiter freeze, each equal to its own single-case run."""
+    meshes = [e2d.Mesh.ogrid(ni, nj, seed=s) for ni, nj, s in SIZES[:4]]
+    params = [e2d.default_params(ma=0.5, alpha_deg=1.0, cfl=1.5, global_dt=1),
+              e2d.default_params(ma=1.5, alpha_deg=0.0, cfl=1.0, far_field_fix=1),
+              e2d.default_params(ma=0.6, alpha_deg=2.0, cfl=2.0, limiter=1, limiter_k=3.0),
+              e2d.default_params(ma=0.6, alpha_deg=1.0, cfl=1.5, limiter_freeze_resd=0.5, global_dt=1)]
+    for p in params:
+        p.ordering = e2d.E2D_ORDER_MORTON
+    b = e2d.Batch(meshes, params)
+    b.step(21)
+    for c, (m, p) in enumerate(zip(meshes, params)):
+        s = e2d.Solver(m, p)
+        s.step(21)
+        assert np.array_equal(b.state(c), s.state()), c
+        assert np.array_equal(b.history(c), s.history()), c
+
+
 def test_batch_launch_shapes_agree(lib):
     meshes, params = make_cases(e2d.E2D_FP64)
     ref = e2d.Batch(meshes, params)

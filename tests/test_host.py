@@ -121,6 +121,22 @@ def test_errors(lib):
     assert ei.value.code == -1
 
 
+def test_binary_mesh_cache_roundtrip(lib, tmp_path):
+    m = e2d.Mesh.ogrid(40, 10, seed=5)
+    p = str(tmp_path / "m.bin")
+    m.write(p, binary=True)
+    assert os.path.getsize(p) == 16 + 16 * 40 * 11 + 12 * 800
+    m2 = e2d.Mesh.read(p)
+    for a, b in zip(m.nodes(), m2.nodes()):
+        assert np.array_equal(a, b)
+    with open(p, "rb") as f:
+        head = f.read(os.path.getsize(p) - 4)
+    with open(p, "wb") as f:
+        f.write(head)
+    with pytest.raises(_lib.E2DError, match="truncated"):
+        e2d.Mesh.read(p)
+
+
 def test_truncated_mesh_file(lib):
     with tempfile.TemporaryDirectory() as d:
         p = os.path.join(d, "m.dat")

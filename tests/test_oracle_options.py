@@ -1,0 +1,64 @@
+"""Scheme options of the oracle that have no reference counterpart (CPU).
+
+global_dt: every cell advances with the smallest local step of the mesh (the
+intent of the reference's disabled kernel_TimeStep, gpu_solver.cu:880-936).
+far_field_fix: the supersonic test of the far-field boundary
+(gpu_solver.cu:79) compares the non-dimensional normal velocity with the
+non-dimensional free-stream sound speed 1/M instead of the dimensional AIN.
+The GPU kernels are checked against these oracle paths bit for bit in
+test_gpu_parity.py."""
+import numpy as np
+
+import gpueularsolver2d_gb300 as e2d
+
+
+def _case(oracle, mesh, **kw):
+    x, y, tri = mesh.nodes()
+    return oracle.Case(x, y, tri, oracle.params(**kw))
+
+
+def test_global_dt_is_min_of_local(lib, oracle):
+    mesh = e2d.Mesh.ogrid(32, 8, seed=3)
+    loc = _case(oracle, mesh, ma=0.6, alpha_deg=1.0, cfl=1.5)
+    glo = _case(oracle, mesh, ma=0.6, alpha_deg=1.0, cfl=1.5, global_dt=1)
+    loc.run(3)
+    glo.set_state(loc.state())
+    a, b = loc.stage_probe(), glo.stage_probe()
+    assert np.all(b["dt"] == a["dt"].min())
+    assert a["dt"].max() > 10 * a["dt"].min()  # the option does change the step
+    np.testing.assert_array_equal(a["res"], b["res"])
+
+
+def test_global_dt_runs_and_converges_slower(lib, oracle):
+    mesh = e2d.Mesh.ogrid(32, 8, seed=3)
+    loc = _case(oracle, mesh, ma=0.5, alpha_deg=1.0, cfl=1.5)
+    glo = _case(oracle, mesh, ma=0.5, alpha_deg=1.0, cfl=1.5, global_dt=1)
+    rl, rg = loc.run(60), glo.run(60)
+    assert np.all(np.isfinite(rg)) and rl[-1] < rg[-1]
+
+
+def test_far_field_fix_supersonic_branch(lib, oracle):
+    mesh = e2d.Mesh.ogrid(32, 8, seed=3)
+    ma = 1.5
+    fix = _case(oracle, mesh, ma=ma, alpha_deg=0.0, far_field_fix=1)
+    ref = _case(oracle, mesh, ma=ma, alpha_deg=0.0)
+    g, T, R = 1.4, 288.15, 287.06
+    ain = np.sqrt(g * R * T)
+    rho_e = R * T / (ma * ain) ** 2 / (g - 1) + 0.5
+    dw = np.array([1.02, 0.98, 0.01, rho_e * 1.01])
+    # outflow face, normal +x (nx = vectory / |v|): ghost = interior state
+    np.testing.assert_array_equal(fix.far_ghost(dw, 0.0, 0.3), dw)
+    # inflow face, normal -x: ghost = free stream
+    np.testing.assert_array_equal(fix.far_ghost(dw, 0.0, -0.3), [1.0, 1.0, 0.0, rho_e])
+    # the reference test never takes the supersonic branch
+    assert not np.array_equal(ref.far_ghost(dw, 0.0, 0.3), dw)
+    # a face whose normal velocity is subsonic keeps the characteristic branch
+    np.testing.assert_array_equal(fix.far_ghost(dw, 0.3, 0.0), ref.far_ghost(dw, 0.3, 0.0))
+
+
+def test_far_field_fix_inactive_when_subsonic(lib, oracle):
+    mesh = e2d.Mesh.ogrid(32, 8, seed=3)
+    a = _case(oracle, mesh, ma=0.6, alpha_deg=2.0, cfl=1.5)
+    b = _case(oracle, mesh, ma=0.6, alpha_deg=2.0, cfl=1.5, far_field_fix=1)
+    np.testing.assert_array_equal(a.run(10), b.run(10))
+    np.testing.assert_array_equal(a.state(), b.state())
