@@ -83,6 +83,7 @@ SIGNATURES = {
     "e2d_write_field_plt": (_I, [_P, _P, ctypes.c_char_p]),
     "e2d_write_wall_cp_plt": (_I, [_P, _P, ctypes.c_char_p]),
     "e2d_get_params": (_I, [_P, ctypes.POINTER(Params)]),
+    "e2d_set_precision": (_I, [_P, _I]),
     "e2d_last_device_ms": (_I, [_P, _PD]),
     "e2d_launches_per_iteration": (_I, [_P, _PI]),
     "e2d_profile_passes": (_I, [_P, _I, _PD, _PI]),

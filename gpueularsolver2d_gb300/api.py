@@ -136,6 +136,23 @@ class Solver:
         check(load().e2d_solve(self._h, max_steps, epsl, _dp(hist), ctypes.byref(n)))
         return hist[: n.value].copy()
 
+    def set_precision(self, precision: int) -> None:
+        """Switch the stencil precision in place (state, step count, residual
+        normalisation and history carry over)."""
+        check(load().e2d_set_precision(self._h, precision))
+
+    def solve_mixed(self, max_steps: int, epsl: float, switch: float = 1e-4) -> np.ndarray:
+        """FP32 iterations until Resd <= switch, then FP64 until Resd <= epsl:
+        most of the work at FP32 speed, the end below the FP32 rounding floor.
+        Returns the residuals of both phases."""
+        self.set_precision(E2D_FP32)
+        h1 = self.solve(max_steps, max(switch, epsl))
+        rest = max_steps - len(h1)
+        if rest <= 0 or (len(h1) and h1[-1] <= epsl):
+            return h1
+        self.set_precision(E2D_FP64)
+        return np.concatenate([h1, self.solve(rest, epsl)])
+
     def progress(self):
         st = ctypes.c_int32()
         r = ctypes.c_double()

@@ -38,7 +38,11 @@ UNITS = {
     "resid.o": ("resid.cu", ["nvcc", *NVCC_COMMON]),
     "kernels_f64.o": ("kernels_f64.cu", ["nvcc", *NVCC_COMMON, "--fmad=false"]),
     "noalloc.o": ("noalloc.cu", ["nvcc", *NVCC_COMMON, "--fmad=false"]),
-    "kernels_f32.o": ("kernels_f32.cu", ["nvcc", *NVCC_COMMON, "--fmad=true",
+    # FP32 stencil: no multiply-add contraction either, so every inlined copy
+    # of a device function (single-case and batched kernels, both cells of a
+    # face) rounds the same way and gives the same bits
+    "kernels_f32.o": ("kernels_f32.cu", ["nvcc", *NVCC_COMMON,
+                                          f"--fmad={os.environ.get('E2D_FP32_FMAD', 'false')}",
                                           "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
 }
 HEADERS = ["internal.h", "dev_types.h", "kernels.cuh", "solver_internal.h", "mlp_kernels.cuh"]
@@ -70,7 +74,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
                                                        __file__]
     # rebuild everything when the extra nvcc flags differ from the last build
     stamp = os.path.join(OBJDIR, "nvcc_extra.txt")
-    extra = os.environ.get("E2D_NVCC_EXTRA", "")
+    extra = os.environ.get("E2D_NVCC_EXTRA", "") + "|fp32_fmad=" + os.environ.get("E2D_FP32_FMAD", "false")
     if not os.path.exists(stamp) or open(stamp).read() != extra:
         force = True
         with open(stamp, "w") as f:

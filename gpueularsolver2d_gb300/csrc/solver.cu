@@ -244,6 +244,7 @@ struct e2d_solver {
     bool own_stream = false;
     cudaGraphExec_t gexec = nullptr;
     int graph_iters = 8;
+    int block = 128;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_ms = 0.0;
     std::vector<double> hist;  // host copy of Resd[1..step]
@@ -311,6 +312,21 @@ int build_graph(e2d_solver *s) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) { s->gexec = nullptr; set_error(std::string("graph instantiate: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
     return E2D_OK;
+}
+
+// A stencil of the requested precision over the solver's mesh layout, bound
+// to the solver's stream and control block (its state is not set).
+int make_impl(e2d_solver *s, const e2d_params &p, std::unique_ptr<SolverBase> &out) {
+    if (p.precision == E2D_FP64) {
+        auto *t = new SolverT<double>(&s->L);
+        t->stream = &s->stream;
+        out.reset(t);
+        return t->init(p, s->fs, s->ctl_dev, s->block);
+    }
+    auto *t = new SolverT<float>(&s->L);
+    t->stream = &s->stream;
+    out.reset(t);
+    return t->init(p, s->fs, s->ctl_dev, s->block);
 }
 
 // Copies the residuals of iterations completed since the last call into the
@@ -398,18 +414,8 @@ int e2d_solver_create(e2d_mesh *m, const e2d_params *p, e2d_solver **out) {
     for (auto &d : s->ctl_host->dtmin) d = kDtNone;
     CK(cudaMemcpy(s->ctl_dev, s->ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice));
     s->graph_iters = p->graph_iters > 0 ? p->graph_iters : 8;
-    const int block = p->block_size > 0 ? p->block_size : 128;
-    if (p->precision == E2D_FP64) {
-        auto *t = new SolverT<double>(&s->L);
-        t->stream = &s->stream;
-        s->impl.reset(t);
-        if ((rc = t->init(*p, s->fs, s->ctl_dev, block))) return rc;
-    } else {
-        auto *t = new SolverT<float>(&s->L);
-        t->stream = &s->stream;
-        s->impl.reset(t);
-        if ((rc = t->init(*p, s->fs, s->ctl_dev, block))) return rc;
-    }
+    s->block = p->block_size > 0 ? p->block_size : 128;
+    if ((rc = make_impl(s.get(), *p, s->impl))) return rc;
     // free-stream state (gpu_init.cu:79-86)
     std::vector<double> w0(4 * (size_t)s->L.n);
     for (int i = 0; i < s->L.n; i++) {
@@ -528,6 +534,29 @@ int e2d_write_residual_plt(e2d_solver *s, const char *path) {
     for (int i = 1; i <= step; i++)
         if (i % 100 == 0) std::fprintf(fp, "%d %20.10lf\n", i, s->hist[i - 1]);
     std::fclose(fp);
+    return E2D_OK;
+}
+
+int e2d_set_precision(e2d_solver *s, int32_t precision) {
+    if (!s) { set_error("null argument"); return E2D_ERR_ARG; }
+    if (precision != E2D_FP64 && precision != E2D_FP32) { set_error("precision must be E2D_FP64 or E2D_FP32"); return E2D_ERR_ARG; }
+    if (precision == s->prm.precision) return E2D_OK;
+    int rc = pull_ctl(s);
+    if (rc) return rc;
+    if (s->ctl_host->frozen) {
+        set_error("the limiter values are frozen in the current precision and cannot be carried over");
+        return E2D_ERR_ARG;
+    }
+    std::vector<double> w(4 * (size_t)s->L.n);
+    if ((rc = s->impl->download_state(w.data()))) return rc;
+    e2d_params p = s->prm;
+    p.precision = precision;
+    std::unique_ptr<SolverBase> next;
+    if ((rc = make_impl(s, p, next))) return rc;
+    if ((rc = next->upload_state(w.data()))) return rc;
+    s->impl = std::move(next);
+    s->prm.precision = precision;
+    if (s->gexec) { cudaGraphExecDestroy(s->gexec); s->gexec = nullptr; }
     return E2D_OK;
 }
 

@@ -57,19 +57,22 @@ def freestream(mach: float, alpha_deg: float, ncell: int) -> np.ndarray:
 class SolverSettings:
     """Solver settings shared by every run of the pipeline.
 
-    The reference limiter chatters: its residual stalls near 1e-3, and freezing
-    it early leaves a converged state that depends on where the run started.
-    The default is therefore the smooth (Venkatakrishnan-type) limiter option,
-    frozen once Resd reaches 1e-3 (the smooth limiter alone still stalls near
-    5e-4).  On the 256 x 64 O-grid at M 0.6, alpha 1 in FP64 this reaches a
-    1e-6 drop in about 65k iterations, and runs started from the free stream
-    and from a nearby solution end within 3e-5 in CL and 1e-6 in CD."""
+    The reference limiter chatters: its residual stalls near 1e-3, and a
+    limiter frozen part way leaves a converged state that depends on where the
+    run started, so warm and free-stream runs would not end at the same CL.
+    The default is the smooth (Venkatakrishnan-type) limiter option with a
+    large K: with K = 5 it still stalls near 5e-4, with K = 20 it stalls at
+    M 0.7, alpha 3; with K = 200 both M 0.6, alpha 1 and M 0.7, alpha 3 on the
+    256 x 64 O-grid fall to 1e-4 without any freezing, so the converged state
+    is unique.  ``switch_resd`` > 0 runs FP32 down to that level and FP64
+    below it (FP32 states stall near 2e-5 on that mesh)."""
     cfl: float = 3.0
     freeze: int = 0
-    freeze_resd: float = 1e-3
+    freeze_resd: float = 0.0
     precision: int = e2d.E2D_FP32
     limiter: int = 1
-    limiter_k: float = 5.0
+    limiter_k: float = 200.0
+    switch_resd: float = 0.0
 
     def params(self, mach, alpha, maxstep=100000):
         return e2d.default_params(ma=mach, alpha_deg=alpha, cfl=self.cfl, precision=self.precision,
@@ -147,7 +150,10 @@ def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=N
         s.set_residual_norm(epsm)
     t0 = time.perf_counter()
     try:
-        h = s.solve(maxit, target)
+        if settings.switch_resd > 0.0:
+            h = s.solve_mixed(maxit, target, settings.switch_resd)
+        else:
+            h = s.solve(maxit, target)
         ok = bool(len(h) and h[-1] <= target)
     except E2DError:
         h, ok = s.history(), False
@@ -190,6 +196,8 @@ def main(argv=None):
     ap.add_argument("--maxit", type=int, default=120000)
     ap.add_argument("--mach", type=float, nargs=2, default=(0.5, 0.7))
     ap.add_argument("--alpha", type=float, nargs=2, default=(-1.0, 3.0))
+    ap.add_argument("--eval", choices=["fp64", "mixed"], default="mixed",
+                    help="timed runs in FP64, or FP32 down to 1e-4 and FP64 below")
     ap.add_argument("--json", default=None)
     args = ap.parse_args(argv)
     log = lambda s: print(s, file=sys.stderr, flush=True)  # noqa: E731
@@ -207,7 +215,7 @@ def main(argv=None):
         p = predict(net, ds, mesh, m, a)
         errs.append(float(np.sqrt(np.mean((p - w) ** 2, axis=0)).max() / np.abs(w).max()))
     log(f"held-out prediction RMS error (max over components, rel. to max |W|): median {np.median(errs):.2e}")
-    ev = SolverSettings(precision=e2d.E2D_FP64)
+    ev = SolverSettings(precision=e2d.E2D_FP64, switch_resd=1e-4 if args.eval == "mixed" else 0.0)
     rows = evaluate(net, ds, mesh, held_c[:args.neval], ev, args.target, args.maxit, log=log)
     conv = [r for r in rows if r["warm"]["converged"] and r["free"]["converged"]]
     summary = {
@@ -215,7 +223,7 @@ def main(argv=None):
         "alpha": list(args.alpha), "gen_iters": args.gen_iters, "train_steps": args.steps, "batch": args.batch,
         "train_seconds": t_train, "final_loss": float(loss[-100:].mean()),
         "heldout_pred_err_median": float(np.median(errs)), "target_drop": args.target,
-        "eval_precision": "fp64", "evaluated": len(rows), "both_converged": len(conv),
+        "eval_precision": args.eval, "evaluated": len(rows), "both_converged": len(conv),
         "speedup_wall_median": float(np.median([r["speedup_wall"] for r in conv])) if conv else None,
         "speedup_iter_median": float(np.median([r["speedup_iter"] for r in conv])) if conv else None,
         "max_dcl": float(max(r["dcl"] for r in conv)) if conv else None,

@@ -202,6 +202,12 @@ int e2d_write_field_plt(e2d_solver *s, e2d_mesh *m, const char *path);
 int e2d_write_wall_cp_plt(e2d_solver *s, e2d_mesh *m, const char *path);
 /* Parameters the solver was created with. */
 int e2d_get_params(e2d_solver *s, e2d_params *p);
+/* Switches the stencil between E2D_FP32 and E2D_FP64 in place: the state is
+ * carried over (rounded to FP32 when going down), and the iteration count,
+ * residual normalisation and history continue.  The usual use is a fast FP32
+ * solve to about 1e-4 followed by FP64 below the FP32 state's rounding floor.
+ * Refused while limiter values are frozen (they live in the old precision). */
+int e2d_set_precision(e2d_solver *s, int32_t precision);
 /* Device time of the kernels of the last e2d_step/e2d_solve call, ms,
  * measured with CUDA events on the solver's stream. */
 int e2d_last_device_ms(e2d_solver *s, double *ms);

@@ -54,14 +54,13 @@ def test_fp64_bit_exact_128x32_morton(lib, oracle):
 
 
 def test_fp32_error_vs_fp64(lib):
-    """FP32 stencil against the FP64 run of the same code.
+    """FP32 stencil against the FP64 run of the same code, early in the run.
 
-    One iteration stays at FP32 rounding.  Through the start-up transient the
-    limiter and the smoothing clamp switch on tiny differences and amplify
-    any change of rounding (the reference's own FMA-contracted FP64 kernels
-    drift from the oracle the same way, at the FP64 level), so longer runs
-    are held to the median error, the maximum error and the residual
-    history, with the tolerances written here."""
+    One iteration stays at FP32 rounding, ten within 1e-4.  Later in the
+    start-up transient the limiter and the smoothing clamp switch on tiny
+    differences and amplify any change of rounding (the reference's own
+    FMA-contracted FP64 kernels drift from the oracle the same way, at the
+    FP64 level), so the comparison that matters is the converged one below."""
     mesh = e2d.Mesh.ogrid(128, 32, seed=1)
     kw = dict(ma=0.5, alpha_deg=1.25, cfl=2.0)
     s64 = e2d.Solver(mesh, e2d.default_params(**kw))
@@ -69,21 +68,66 @@ def test_fp32_error_vs_fp64(lib):
 
     def err():
         w64, w32 = s64.state(), s32.state()
-        d = np.abs(w32 - w64) / np.abs(w64).max(axis=0)
-        return d.max(), np.median(d)
+        return (np.abs(w32 - w64) / np.abs(w64).max(axis=0)).max()
 
     s64.step(1)
     s32.step(1)
-    assert err()[0] < 5e-6
+    assert err() < 5e-6
     s64.step(9)
     s32.step(9)
-    assert err()[0] < 1e-4
-    s64.step(290)
-    s32.step(290)
-    mx, med = err()
-    assert mx < 2e-2 and med < 1e-3, (mx, med)
-    h64, h32 = s64.history(), s32.history()
-    assert np.max(np.abs(h32 - h64) / h64) < 2e-2
+    assert err() < 1e-4
+
+
+def test_fp32_converged_solution_vs_fp64(lib):
+    """Converged FP32 and FP64 solutions of the same case (smooth limiter,
+    K = 20, so that both converge to one steady state): the FP32 state stalls
+    near its rounding floor (~1e-5 drop), FP64 goes on to 1e-6.  Tolerances:
+    state 1e-4 max / 1e-5 median relative to each component's largest
+    magnitude, CL and CD within 1e-5."""
+    mesh = e2d.Mesh.ogrid(128, 32, seed=1)
+    kw = dict(ma=0.5, alpha_deg=1.25, cfl=3.0, limiter=1, limiter_k=20.0, ordering=e2d.E2D_ORDER_MORTON,
+              maxstep=40000)
+    s64 = e2d.Solver(mesh, e2d.default_params(**kw))
+    h64 = s64.solve(40000, 1e-6)
+    assert h64[-1] <= 1e-6
+    s32 = e2d.Solver(mesh, e2d.default_params(precision=e2d.E2D_FP32, **kw))
+    h32 = s32.solve(20000, 1e-6)
+    assert h32[-1] < 1e-4
+    w64, w32 = s64.state(), s32.state()
+    d = np.abs(w32 - w64) / np.abs(w64).max(axis=0)
+    assert d.max() < 1e-4 and np.median(d) < 1e-5, (d.max(), np.median(d))
+    (cl64, cd64), (cl32, cd32) = s64.forces(), s32.forces()
+    assert abs(cl32 - cl64) < 1e-5 and abs(cd32 - cd64) < 1e-5, (cl32 - cl64, cd32 - cd64)
+
+
+def test_set_precision_continues_the_run(lib):
+    """Switching FP32 -> FP64 part way equals saving the FP32 state and
+    residual norm and continuing in a fresh FP64 solver, bit for bit; the
+    history runs on across the switch."""
+    mesh = e2d.Mesh.ogrid(48, 12, seed=7)
+    kw = dict(ma=0.6, alpha_deg=1.0, cfl=1.5, ordering=e2d.E2D_ORDER_MORTON)
+    a = e2d.Solver(mesh, e2d.default_params(precision=e2d.E2D_FP32, **kw))
+    a.step(40)
+    w, epsm, h32 = a.state(), a.residual_norm(), a.history()
+    a.set_precision(e2d.E2D_FP64)
+    assert np.array_equal(a.state(), w)
+    a.step(25)
+    c = e2d.Solver(mesh, e2d.default_params(**kw))
+    c.set_state(w)
+    c.set_residual_norm(epsm)
+    c.step(25)
+    assert np.array_equal(a.state(), c.state())
+    h = a.history()
+    assert len(h) == 65 and np.array_equal(h[:40], h32) and np.array_equal(h[40:], c.history())
+    a.set_precision(e2d.E2D_FP32)  # and back down: the state rounds to FP32
+    assert np.allclose(a.state(), c.state(), rtol=1e-6, atol=0)
+    a.step(1)
+    with pytest.raises(Exception):
+        a.set_precision(7)
+    frozen = e2d.Solver(mesh, e2d.default_params(limiter_freeze=1, precision=e2d.E2D_FP32, **kw))
+    frozen.step(2)
+    with pytest.raises(Exception, match="frozen"):
+        frozen.set_precision(e2d.E2D_FP64)
 
 
 def test_solve_stops_like_reference_loop(lib, oracle):
