@@ -141,9 +141,17 @@ def replica_rate(world: int, ncell: int, stages: int, steps: int, t_max: float) 
     return world * ncell * stages * steps / t_max
 
 
-def make_params(e2d, wl, precision, block=0):
+ORDERINGS = {"morton": ("E2D_ORDER_MORTON", "Morton"), "rcm": ("E2D_ORDER_RCM", "RCM"),
+             "file": ("E2D_ORDER_FILE", "file order")}
+
+
+def make_params(e2d, wl, precision, block=0, ordering="morton"):
     return e2d.default_params(ma=wl["ma"], alpha_deg=wl["alpha"], cfl=wl["cfl"], precision=precision,
-                              ordering=e2d.E2D_ORDER_MORTON, maxstep=1000000, block_size=block)
+                              ordering=getattr(e2d, ORDERINGS[ordering][0]), maxstep=1000000, block_size=block)
+
+
+def workload_desc(wl, ordering="morton") -> str:
+    return wl["desc"].replace("Morton", ORDERINGS[ordering][1])
 
 
 def cpu_port_rate(wl, steps_wanted: float, threads: int | None = None, mesh=None):
@@ -196,7 +204,7 @@ def run_reference(args, rank: int, world: int):
         "n_gpus": world, "steps": k, "warmup": args.warmup, "ms_per_step": dt / k * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded NACA0012 O-grid)",
-        "config": {"workload": wl["desc"], "cells": case.ncell, "stages": p.rk_stages,
+        "config": {"workload": workload_desc(wl, args.ordering), "cells": case.ncell, "stages": p.rk_stages,
                    "parallelism": f"replicas{world}"},
         "cpu_baseline": {"value": rate, "unit": "cell-stage/s", "cores": th, "kind": "port",
                          "sample": f"{k} of the {args.steps} requested iterations (capped at ~60 s of host "
@@ -220,7 +228,7 @@ def run_gpu(args, rank: int, world: int):
     wl = WORKLOADS[args.workload]
     prec = e2d.E2D_FP64 if args.fp64 else e2d.E2D_FP32
     mesh = e2d.Mesh.ogrid(wl["ni"], wl["nj"], seed=1)
-    params = make_params(e2d, wl, prec, args.block)
+    params = make_params(e2d, wl, prec, args.block, args.ordering)
     solver = e2d.Solver(mesh, params)
     ncell, stages = solver.ncell, params.rk_stages
     launches = solver.launches_per_iteration()
@@ -292,8 +300,8 @@ def run_gpu(args, rank: int, world: int):
     fp_err = None
     if rank == 0 and prec == e2d.E2D_FP32:
         n_err = 20
-        a32 = e2d.Solver(mesh, make_params(e2d, wl, e2d.E2D_FP32))
-        a64 = e2d.Solver(mesh, make_params(e2d, wl, e2d.E2D_FP64))
+        a32 = e2d.Solver(mesh, make_params(e2d, wl, e2d.E2D_FP32, ordering=args.ordering))
+        a64 = e2d.Solver(mesh, make_params(e2d, wl, e2d.E2D_FP64, ordering=args.ordering))
         a32.step(n_err)
         a64.step(n_err)
         w32, w64 = a32.state(), a64.state()
@@ -319,7 +327,7 @@ def run_gpu(args, rank: int, world: int):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if prec == e2d.E2D_FP64 else "f32",
             "data": "synthetic (seeded NACA0012 O-grid)",
-            "config": {"workload": wl["desc"], "cells": ncell, "stages": stages,
+            "config": {"workload": workload_desc(wl, args.ordering), "cells": ncell, "stages": stages,
                        "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (working set > 1 GB), no flush"},
             "wall_ms_per_step": wall / args.steps * 1e3,
@@ -405,6 +413,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch64"], default="large")
     ap.add_argument("--fp64", action="store_true")
     ap.add_argument("--block", type=int, default=0, help="threads per CTA (0: library default)")
+    ap.add_argument("--ordering", choices=sorted(ORDERINGS), default="morton", help="cell order in device memory")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -160,11 +160,46 @@ static inline uint64_t spread21(uint64_t v) {
     return v;
 }
 
+// Reverse Cuthill-McKee order of the cell adjacency graph (interior faces).
+// Deterministic: each component starts at its lowest-degree cell (lowest
+// index among equals), neighbours join the queue by (degree, index), and the
+// whole Cuthill-McKee sequence is reversed at the end.
+static void rcm_order(const MeshTopo &t, int N, std::vector<int> &perm) {
+    std::vector<int> deg(N, 0), order;
+    order.reserve(N);
+    for (int c = 0; c < N; c++)
+        for (int k = 0; k < 3; k++) deg[c] += t.nb[3 * (size_t)c + k] >= 0;
+    std::vector<char> seen(N, 0);
+    std::vector<int> byd(N);
+    for (int i = 0; i < N; i++) byd[i] = i;
+    std::stable_sort(byd.begin(), byd.end(), [&](int a, int b) { return deg[a] < deg[b]; });
+    size_t next_start = 0;
+    while (order.size() < (size_t)N) {
+        while (seen[byd[next_start]]) next_start++;
+        const int s0 = byd[next_start];
+        seen[s0] = 1;
+        size_t head = order.size();
+        order.push_back(s0);
+        while (head < order.size()) {
+            const int c = order[head++];
+            int nb[3], cnt = 0;
+            for (int k = 0; k < 3; k++) {
+                const int q = t.nb[3 * (size_t)c + k];
+                if (q >= 0 && !seen[q]) { nb[cnt++] = q; seen[q] = 1; }
+            }
+            std::sort(nb, nb + cnt, [&](int a, int b) { return deg[a] != deg[b] ? deg[a] < deg[b] : a < b; });
+            for (int k = 0; k < cnt; k++) order.push_back(nb[k]);
+        }
+    }
+    for (int i = 0; i < N; i++) perm[i] = order[N - 1 - i];
+}
+
 void cell_order(const e2d_mesh *m, int ordering, std::vector<int> &perm) {
     const MeshTopo &t = m->topo;
     const int N = m->ncell;
     perm.resize(N);
     for (int i = 0; i < N; i++) perm[i] = i;
+    if (ordering == E2D_ORDER_RCM) { rcm_order(t, N, perm); return; }
     if (ordering != E2D_ORDER_MORTON) return;
     double x0 = t.cx[0], x1 = t.cx[0], y0 = t.cy[0], y1 = t.cy[0];
     for (int i = 1; i < N; i++) {
@@ -445,7 +480,10 @@ int e2d_mesh_nodes(const e2d_mesh *m, double *x, double *y, int32_t *tri) {
 
 int e2d_mesh_order(e2d_mesh *m, int32_t ordering, int32_t *perm) {
     if (!m || !perm) { set_error("null argument"); return E2D_ERR_ARG; }
-    if (ordering != E2D_ORDER_FILE && ordering != E2D_ORDER_MORTON) { set_error("unknown ordering"); return E2D_ERR_ARG; }
+    if (ordering != E2D_ORDER_FILE && ordering != E2D_ORDER_MORTON && ordering != E2D_ORDER_RCM) {
+        set_error("unknown ordering");
+        return E2D_ERR_ARG;
+    }
     double wb = m->topo.wall_box >= 0 ? m->topo.wall_box : 2.0;
     int rc = build_topology(m, wb);
     if (rc) return rc;

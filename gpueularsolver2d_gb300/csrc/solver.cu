@@ -112,7 +112,7 @@ bool valid_params(const e2d_params *p) {
     if (!(p->gamma > 1.0) || !(p->ma > 0.0) || !(p->tin > 0.0) || !(p->cfl > 0.0)) return false;
     if (p->rk_stages < 1 || p->rk_stages > 8 || p->irs_sweeps < 0 || p->irs_sweeps > 16) return false;
     if (p->precision != E2D_FP64 && p->precision != E2D_FP32) return false;
-    if (p->ordering != E2D_ORDER_FILE && p->ordering != E2D_ORDER_MORTON) return false;
+    if (p->ordering != E2D_ORDER_FILE && p->ordering != E2D_ORDER_MORTON && p->ordering != E2D_ORDER_RCM) return false;
     if (p->block_size != 0 && (p->block_size < 32 || p->block_size > 256 || p->block_size % 32)) return false;
     if (p->graph_iters < 0 || p->graph_iters > 256) return false;
     if (p->limiter_freeze < 0) return false;

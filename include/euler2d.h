@@ -44,6 +44,7 @@ extern "C" {
 
 #define E2D_ORDER_FILE 0     /* cells in file order                    */
 #define E2D_ORDER_MORTON 1   /* cells sorted by centroid Morton code   */
+#define E2D_ORDER_RCM 2      /* reverse Cuthill-McKee of cell adjacency */
 
 typedef struct e2d_mesh e2d_mesh;
 typedef struct e2d_solver e2d_solver;
@@ -70,7 +71,7 @@ typedef struct e2d_params {
     double entropy_eps;  /* Harten fix width; reference 0.05 (gpu_solver.cu:603) */
     double wall_box;     /* boundary face is wall if |mid x|,|mid y| < wall_box;
                             reference 2.0 (gpu_init.cu:190)                 */
-    int32_t ordering;    /* E2D_ORDER_FILE (default) or E2D_ORDER_MORTON    */
+    int32_t ordering;    /* E2D_ORDER_FILE (default), _MORTON or _RCM        */
     int32_t block_size;  /* threads per CTA, 0 = tuned default              */
     int32_t graph_iters; /* iterations captured per CUDA graph, 0 = default */
     int32_t verbose;     /* e2d_solve prints "step,resid" lines like the

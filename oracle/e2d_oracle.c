@@ -905,3 +905,47 @@ void or_morton_perm(const or_case *c, int *perm) {
     for (int k = 0; k < c->ncell; k++) perm[k] = a[k].id;
     free(a);
 }
+
+/* ------------------------------------------------------------------ */
+/* Reverse Cuthill-McKee order (no counterpart in the reference)       */
+/* ------------------------------------------------------------------ */
+
+/* Breadth-first over interior neighbours (neicell > 0).  A component starts
+ * at its unvisited cell of smallest degree (CLog), smallest id among equals;
+ * the unvisited neighbours of each dequeued cell join the queue by (degree,
+ * id); the resulting sequence is reversed.  perm[k] = 1-based file id. */
+static const int *rcm_deg;
+
+static int rcm_cmp(const void *a, const void *b) {
+    int x = *(const int *)a, y = *(const int *)b;
+    if (rcm_deg[x] != rcm_deg[y]) return rcm_deg[x] < rcm_deg[y] ? -1 : 1;
+    return x < y ? -1 : (x > y);
+}
+
+void or_rcm_perm(const or_case *c, int *perm) {
+    const int N = c->ncell;
+    int *order = xcalloc(N, sizeof(int));
+    char *seen = xcalloc(N + 1, 1);
+    int *cand = xcalloc(N, sizeof(int));
+    rcm_deg = c->clog;
+    for (int i = 0; i < N; i++) cand[i] = i + 1;
+    qsort(cand, N, sizeof(int), rcm_cmp); /* start candidates by (degree, id) */
+    int n = 0, next = 0;
+    while (n < N) {
+        while (seen[cand[next]]) next++;
+        int head = n;
+        order[n++] = cand[next];
+        seen[cand[next]] = 1;
+        while (head < n) {
+            int i = order[head++], nb[3], k = 0;
+            for (int f = 0; f < 3; f++) {
+                int q = c->neicell[3 * i + f];
+                if (q > 0 && !seen[q]) { nb[k++] = q; seen[q] = 1; }
+            }
+            qsort(nb, k, sizeof(int), rcm_cmp);
+            for (int f = 0; f < k; f++) order[n++] = nb[f];
+        }
+    }
+    for (int k = 0; k < N; k++) perm[k] = order[N - 1 - k];
+    free(order); free(seen); free(cand);
+}

@@ -103,6 +103,11 @@ void or_stage_probe(or_case *c, double *ghost, double *grad, double *umm,
  * sits at position k.  Ties keep file order. */
 void or_morton_perm(const or_case *c, int *perm);
 
+/* Reverse Cuthill-McKee order of the interior-face adjacency: breadth-first
+ * from the smallest-degree cell (smallest id among equals), neighbours queued
+ * by (degree, id), sequence reversed.  perm[k] = 1-based file id. */
+void or_rcm_perm(const or_case *c, int *perm);
+
 /* Point kernels, for function-level known-answer checks. */
 void or_roe_flux(const double lw[4], const double rw[4], double nx, double ny,
                  double gamma, double entropy_eps, double flux[4]);

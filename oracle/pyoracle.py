@@ -53,7 +53,7 @@ def lib() -> ctypes.CDLL:
             "or_destroy": [vp], "or_counts": [vp, ip], "or_topology": [vp, ip, dp, ip, dp],
             "or_get_state": [vp, dp], "or_set_state": [vp, dp], "or_get_pta": [vp, dp],
             "or_run": [vp, ctypes.c_int, dp], "or_stage_probe": [vp, dp, dp, dp, dp, dp, dp, dp],
-            "or_morton_perm": [vp, ip], "or_set_threads": [ctypes.c_int],
+            "or_morton_perm": [vp, ip], "or_rcm_perm": [vp, ip], "or_set_threads": [ctypes.c_int],
             "or_params_default": [ctypes.POINTER(OrParams)],
             "or_roe_flux": [dp, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp],
             "or_far_ghost": [dp, ctypes.c_double, ctypes.c_double, vp, dp],
@@ -153,6 +153,11 @@ class Case:
         dt = np.zeros(self.ncell)
         lib().or_stage_probe(self._h, _dp(gh), _dp(gr), _dp(um), _dp(fl), _dp(sr), _dp(res), _dp(dt))
         return dict(ghost=gh, grad=gr, umm=um, flux=fl, sr=sr, res=res, dt=dt)
+
+    def rcm(self) -> np.ndarray:
+        perm = np.zeros(self.ncell, np.int32)
+        lib().or_rcm_perm(self._h, _ip(perm))
+        return perm
 
     def far_ghost(self, dw, vectorx: float, vectory: float) -> np.ndarray:
         """Far-field ghost of interior state dw across a face (vectorx, vectory)."""

@@ -34,6 +34,7 @@ def run_pair(mesh, oracle, nsteps, **kw):
     dict(ma=0.6, alpha_deg=1.0, cfl=1.5, limiter_freeze_resd=0.5, ordering=e2d.E2D_ORDER_MORTON),
     dict(ma=0.5, alpha_deg=1.0, cfl=1.5, global_dt=1, ordering=e2d.E2D_ORDER_MORTON),
     dict(ma=1.5, alpha_deg=0.0, cfl=1.0, far_field_fix=1, ordering=e2d.E2D_ORDER_MORTON),
+    dict(ma=0.6, alpha_deg=1.0, cfl=1.5, ordering=e2d.E2D_ORDER_RCM),
 ])
 def test_fp64_bit_exact_vs_oracle(lib, oracle, kw):
     mesh = e2d.Mesh.ogrid(48, 12, seed=7)

@@ -36,6 +36,7 @@ def test_setup_matches_oracle(lib, oracle, ni, nj, seed):
     for a, b in zip(mesh.topology(), case.topology()):
         assert np.array_equal(a, b)
     assert np.array_equal(mesh.order(e2d.E2D_ORDER_MORTON) + 1, case.morton())
+    assert np.array_equal(mesh.order(e2d.E2D_ORDER_RCM) + 1, case.rcm())
     assert np.array_equal(mesh.order(e2d.E2D_ORDER_FILE), np.arange(case.ncell))
 
 
@@ -49,6 +50,24 @@ def test_setup_matches_oracle_on_reference_meshes(lib, oracle, name):
     for a, b in zip(mesh.topology(), case.topology()):
         assert np.array_equal(a, b)
     assert np.array_equal(mesh.order(e2d.E2D_ORDER_MORTON) + 1, case.morton())
+    assert np.array_equal(mesh.order(e2d.E2D_ORDER_RCM) + 1, case.rcm())
+
+
+def test_rcm_is_a_banded_permutation(lib):
+    """RCM is a permutation whose neighbour index distance (bandwidth) is far
+    below the cell count on an O-grid."""
+    mesh = e2d.Mesh.ogrid(96, 24, seed=4)
+    perm = mesh.order(e2d.E2D_ORDER_RCM)
+    n = len(perm)
+    assert np.array_equal(np.sort(perm), np.arange(n))
+    pos = np.empty(n, np.int64)
+    pos[perm] = np.arange(n)
+    _, _, ci, _ = mesh.topology()
+    nb = ci[:, 4:7].reshape(-1) - 1
+    i = np.repeat(np.arange(n), 3)
+    ok = nb >= 0
+    band = np.abs(pos[i[ok]] - pos[nb[ok]]).max()
+    assert band < n // 8, band
 
 
 def test_ogrid_sizes_and_tags(lib):
