@@ -82,3 +82,31 @@ def test_reference_kernels_timed_on_this_gpu(lib, oracle):
     print(res)
     # the product path (FP32 stencil) must beat the reference kernels on the same GPU
     assert res["fp32_ms_per_iteration"] < res["reference_ms_per_iteration"]
+
+
+def test_reference_diverges_on_the_transonic_case_too(lib, oracle):
+    """The transonic configuration (512 x 128 O-grid, M 0.80, alpha 1.25,
+    CFL 2, reference 4-stage RK and smoothing) blows up with the reference
+    scheme: the reference's own GPU program reaches a non-finite residual
+    after about 6800 iterations, and this library's FP64 path stops with a
+    divergence error at about the same iteration.  (Runs the reference's
+    O(N^2) mesh set-up on 65k nodes: about a minute.)"""
+    if oracle.ref_harness_path() is None:
+        pytest.skip("reference sources not available")
+    mesh = e2d.Mesh.ogrid(512, 128, seed=1)
+    n = 8000
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "mesh.dat")
+        mesh.write(path)
+        out = oracle.run_reference("gpu", path, f"0.8 1.25 1.4 101325 288.15 2.0 1e-12 {n}")
+    lines = [l for l in out["stdout"].splitlines() if l.count(",") == 1 and l.split(",")[0].isdigit()]
+    res = np.array([float(l.split(",")[1]) for l in lines])
+    bad = np.flatnonzero(~np.isfinite(res))
+    assert len(bad) and 5000 < bad[0] + 1 < n, (len(res), bad[:3])
+    s = e2d.Solver(mesh, e2d.default_params(ma=0.8, alpha_deg=1.25, cfl=2.0, maxstep=n + 10))
+    with pytest.raises(Exception, match="diverged"):
+        s.step(n)
+    assert abs(len(s.history()) - (bad[0] + 1)) < 500
+    # before the blow-up the two histories overlay (the reference's FMA-contracted
+    # kernels drift from the FP64 path only by rounding growth)
+    np.testing.assert_allclose(s.history()[:100], res[:100], rtol=1e-6)

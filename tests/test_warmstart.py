@@ -2,9 +2,13 @@
 solver, MLP training on the GPU, prediction for a held-out condition.  The
 prediction must be closer to the held-out steady state than the free stream,
 and a solve started from it must begin with a smaller residual (normalised by
-the free-stream run's first iteration) and, run to a 1e-6 drop (FP32 down to
+the free-stream run's first iteration) and, run to a 1e-8 drop (FP32 down to
 1e-4, FP64 below), reach the lift and drag of the free-stream run within
-1e-4."""
+1e-4: the smooth-limiter scheme has one steady state whatever the start.
+(At a 1e-6 drop the two runs still differ by about 2e-4 in CL on this coarse
+mesh: the residual is the density change of one iteration, and the slowest
+mode decays by only ~1e-4 per iteration, so it understates the distance to
+the steady state.)"""
 import numpy as np
 import pytest
 
@@ -29,8 +33,8 @@ def test_warm_start_small(lib):
     err_free = np.abs(ws.freestream(m, a, p.shape[0]) - w_true).mean()
     assert err_pred < 0.5 * err_free, (err_pred, err_free)
     ev = ws.SolverSettings(cfl=3.0, precision=e2d.E2D_FP64, switch_resd=1e-4)
-    free = ws.run_to_drop(mesh, m, a, ev, 1e-6, 80000)
-    warm = ws.run_to_drop(mesh, m, a, ev, 1e-6, 80000, w0=p, epsm=free["epsm"])
+    free = ws.run_to_drop(mesh, m, a, ev, 1e-8, 80000)
+    warm = ws.run_to_drop(mesh, m, a, ev, 1e-8, 80000, w0=p, epsm=free["epsm"])
     assert free["converged"] and warm["converged"]
     assert warm["first_resd"] < 0.5
     assert abs(warm["cl"] - free["cl"]) < 1e-4
