@@ -62,6 +62,12 @@ template <typename T> __device__ __forceinline__ T tsqrt(T v) { return sqrt(v); 
 template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return fmin(a, b); }
 template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return fmax(a, b); }
 
+// a * b + c: two roundings in FP64 (the oracle's arithmetic; the FP64 units
+// are built without contraction), one fused multiply-add in FP32.  Explicit,
+// so the FP32 result does not depend on where the compiler contracts.
+template <typename T> __device__ __forceinline__ T madd(T a, T b, T c) { return a * b + c; }
+template <> __device__ __forceinline__ float madd<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
 template <typename T> __device__ __forceinline__ T comp(const V4<T> &v, int k) {
     return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
 }
@@ -159,6 +165,19 @@ __device__ __forceinline__ T spectral_radius(const V4<T> &a, const V4<T> &b, T v
     return tabs(VC) + CS;
 }
 
+// FP32: the same quantity with one reciprocal and fused multiply-adds.
+template <>
+__device__ __forceinline__ float spectral_radius<float>(const V4<float> &a, const V4<float> &b, float vectorx,
+                                                       float vectory, float g) {
+    const float rou = (a.x + b.x) * 0.5f, ir = 1.0f / rou;
+    const float u = (a.y + b.y) * (0.5f * ir), v = (a.z + b.z) * (0.5f * ir);
+    const float EE = fmaf((a.w + b.w) * 0.5f, ir, -0.5f * fmaf(u, u, v * v));
+    const float VC = fmaf(u, vectory, v * vectorx);
+    const float p = rou * EE * (g - 1.0f);
+    const float CS = sqrtf(g * p * ir * fmaf(vectorx, vectorx, vectory * vectory));
+    return fabsf(VC) + CS;
+}
+
 // gpu_solver.cu:552-566 (kernel_Calc_Function)
 template <typename T>
 __device__ __forceinline__ void calc_function(const V4<T> &w, T g, T &A, T &U, T &V, T &H, T &P) {
@@ -225,6 +244,57 @@ __device__ __forceinline__ V4<T> roe(const V4<T> &LW, const V4<T> &RW, T nx, T n
     return F;
 }
 
+// FP32: the same flux, algebraically identical, arranged for the FP32 units
+// (shared reciprocals, explicit fused multiply-adds); the FP32 pass is issue
+// bound, not memory bound.  Rounding differs from the generic form at FP32
+// level only.
+template <>
+__device__ __forceinline__ V4<float> roe<float>(const V4<float> &LW, const V4<float> &RW, float nx, float ny,
+                                               float g, float epsilon) {
+    const float gm1 = g - 1.0f;
+    const float il = 1.0f / LW.x, ir = 1.0f / RW.x;
+    const float U0 = LW.y * il, V0 = LW.z * il, U1 = RW.y * ir, V1 = RW.z * ir;
+    const float P0 = gm1 * fmaf(-0.5f * LW.x, fmaf(U0, U0, V0 * V0), LW.w);
+    const float P1 = gm1 * fmaf(-0.5f * RW.x, fmaf(U1, U1, V1 * V1), RW.w);
+    const float H0 = (LW.w + P0) * il, H1 = (RW.w + P1) * ir;
+    const float M0 = fmaf(U0, nx, V0 * ny), M1 = fmaf(U1, nx, V1 * ny);
+    const float DVC = M1 - M0;
+    const float sl = sqrtf(LW.x), sr = sqrtf(RW.x);
+    const float ROUB = sl * sr, is = 1.0f / (sl + sr);
+    const float UB = fmaf(U0, sl, U1 * sr) * is;
+    const float VB = fmaf(V0, sl, V1 * sr) * is;
+    const float HB = fmaf(H0, sl, H1 * sr) * is;
+    const float QB = fmaf(UB, UB, VB * VB);
+    const float AB = sqrtf(gm1 * fmaf(-0.5f, QB, HB));
+    const float VC = fmaf(UB, nx, VB * ny);
+    const float e2 = epsilon * epsilon, ie = 0.5f / epsilon;
+    const float l0 = VC - AB, l2 = VC + AB;
+    const float AD0 = fabsf(l0) < epsilon ? fmaf(l0, l0, e2) * ie : fabsf(l0);
+    const float AD1 = fabsf(VC) < epsilon ? fmaf(VC, VC, e2) * ie : fabsf(VC);
+    const float AD2 = fabsf(l2) < epsilon ? fmaf(l2, l2, e2) * ie : fabsf(l2);
+    const float dP = P1 - P0, ia2 = 1.0f / (AB * AB), rad = ROUB * AB * DVC, h2 = 0.5f * ia2;
+    const float F00 = AD0 * (dP - rad) * h2;
+    const float F20 = AD2 * (dP + rad) * h2;
+    const float F10 = AD1 * fmaf(-dP, ia2, RW.x - LW.x);
+    const float du = U1 - U0, dv = V1 - V0, aR = AD1 * ROUB;
+    const float F01 = F00 * fmaf(-AB, nx, UB), F21 = F20 * fmaf(AB, nx, UB);
+    const float F02 = F00 * fmaf(-AB, ny, VB), F22 = F20 * fmaf(AB, ny, VB);
+    const float F03 = F00 * fmaf(-AB, VC, HB), F23 = F20 * fmaf(AB, VC, HB);
+    const float F11 = fmaf(F10, UB, aR * fmaf(-DVC, nx, du));
+    const float F12 = fmaf(F10, VB, aR * fmaf(-DVC, ny, dv));
+    const float F13 = fmaf(F10 * 0.5f, QB, aR * fmaf(UB, du, fmaf(VB, dv, -DVC * VC)));
+    const float WL0 = LW.x * M0, WR0 = RW.x * M1;
+    const float WL1 = fmaf(U0, WL0, nx * P0), WR1 = fmaf(U1, WR0, nx * P1);
+    const float WL2 = fmaf(V0, WL0, ny * P0), WR2 = fmaf(V1, WR0, ny * P1);
+    const float WL3 = WL0 * H0, WR3 = WR0 * H1;
+    V4<float> F;
+    F.x = 0.5f * ((WL0 + WR0) - (F00 + F10 + F20));
+    F.y = 0.5f * ((WL1 + WR1) - (F01 + F11 + F21));
+    F.z = 0.5f * ((WL2 + WR2) - (F02 + F12 + F22));
+    F.w = 0.5f * ((WL3 + WR3) - (F03 + F13 + F23));
+    return F;
+}
+
 // ---------------------------------------------------------------------------
 // Pass A: gpu_solver.cu:137-223 (kernel_Boundary), 225-383 (kernel_Gradient),
 // 385-454 (kernel_deltT), 456-549 (kernel_Limiter / kernel_LBJinterpolate),
@@ -268,8 +338,8 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
                 if (c > jmax[q]) jmax[q] = c;
             }
             T u = comp(U, q);
-            g0[q] += T(0.5) * (u + c) * S[k].x;
-            g1[q] += T(0.5) * (u + c) * S[k].y;
+            g0[q] = madd(T(0.5) * (u + c), S[k].x, g0[q]);
+            g1[q] = madd(T(0.5) * (u + c), S[k].y, g1[q]);
         }
         Tsum += spectral_radius(U, nbv[k], S[k].y, S[k].x, f.gamma);
     }
@@ -294,7 +364,7 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
             T fi = T(1.0), d[4], ph[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                T delt2 = gx[q] * r.x + gy[q] * r.y;
+                T delt2 = madd(gx[q], r.x, gy[q] * r.y);
                 T u = comp(U, q);
                 if (reuse) fi = comp(pf, q);
                 else if (f.limiter == 1) {
@@ -310,8 +380,7 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
                     if (delt2 == T(0)) fi = T(1.0);
                 }
                 ph[q] = fi;
-                delt2 *= fi;
-                d[q] = u + delt2;
+                d[q] = madd(delt2, fi, u);
             }
             o.x = d[0]; o.y = d[1]; o.z = d[2]; o.w = d[3];
             if (phi && !frozen) {
@@ -541,10 +610,10 @@ __device__ __forceinline__ void smooth_cell(const MeshDev<T> &m, const T eps, co
     const V4<T> r0 = res[i];
     const T den = T(1.0) + (eps) * T(tp.w);
     V4<T> o;
-    o.x = (d.x * (eps) + r0.x) / den;
-    o.y = (d.y * (eps) + r0.y) / den;
-    o.z = (d.z * (eps) + r0.z) / den;
-    o.w = (d.w * (eps) + r0.w) / den;
+    o.x = madd(d.x, eps, r0.x) / den;
+    o.y = madd(d.y, eps, r0.y) / den;
+    o.z = madd(d.z, eps, r0.z) / den;
+    o.w = madd(d.w, eps, r0.w) / den;
     dst[i] = o;
 }
 
@@ -562,12 +631,18 @@ __global__ void __launch_bounds__(256) k_smooth(MeshDev<T> m, T eps, const V4<T>
 // Pass D: gpu_solver.cu:1675-1720 (kernel_Smooth2, last sweep + clamp) fused
 // with 938-966 (kernel_RKStep); on the last stage also 968-1020 (kernel_drou)
 // as FP64 block partials and a count of unphysical cells.
+//
+// Mixed mode (Wm not null): the stage's increment is computed in T as usual
+// but applied to the FP64 state Wm, and Wout receives that sum rounded to T
+// (the stencil's working copy); the last stage also stores the FP64 sum back
+// into Wm.  Increments far below the FP32 spacing of the state then still
+// accumulate, so the residual can fall below the FP32 state's rounding floor.
 template <typename T>
 __device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &f, const T rk,
                                             const int smooth, const int i, const V4<T> *__restrict__ src,
                                             const V4<T> *__restrict__ res, const T dti,
-                                            const V4<T> *W0, V4<T> *Wout, const bool want, double &d2,
-                                            int &bad) {
+                                            const V4<T> *W0, V4<T> *Wout, V4<double> *Wm, const bool last,
+                                            const bool want, double &d2, int &bad) {
     {
         const int4 tp = m.topo[i];
         V4<T> r = res[i];
@@ -575,8 +650,8 @@ __device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &
             const V4<T> d = nb_sum(tp, src);
             const T eps = f.irs_eps;
             const T den = T(1.0) + (eps) * T(tp.w);
-            T s0 = (d.x * (eps) + r.x) / den, s1 = (d.y * (eps) + r.y) / den;
-            T s2 = (d.z * (eps) + r.z) / den, s3 = (d.w * (eps) + r.w) / den;
+            T s0 = madd(d.x, eps, r.x) / den, s1 = madd(d.y, eps, r.y) / den;
+            T s2 = madd(d.z, eps, r.z) / den, s3 = madd(d.w, eps, r.w) / den;
             if (tabs(r.x) > tabs(s0)) r.x = s0;
             if (tabs(r.y) > tabs(s1)) r.y = s1;
             if (tabs(r.z) > tabs(s2)) r.z = s2;
@@ -585,6 +660,25 @@ __device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &
         T RK = rk;
         RK *= dti;
         const T A = m.area[i];
+        if (Wm) {
+            const V4<double> w0 = Wm[i];
+            V4<double> w;
+            w.x = w0.x - (double)(RK * r.x / A);
+            w.y = w0.y - (double)(RK * r.y / A);
+            w.z = w0.z - (double)(RK * r.z / A);
+            w.w = w0.w - (double)(RK * r.w / A);
+            V4<T> o;
+            o.x = (T)w.x; o.y = (T)w.y; o.z = (T)w.z; o.w = (T)w.w;
+            Wout[i] = o;
+            if (last) Wm[i] = w;
+            if (want) {
+                const double dd = w.x - w0.x;
+                d2 = dd * dd;
+                const double q = 0.5 * (w.y * w.y + w.z * w.z) / w.x;
+                bad = !(w.x > 0.0) || !(w.w - q > 0.0);
+            }
+            return;
+        }
         const V4<T> w0 = W0[i];
         V4<T> w;
         w.x = w0.x - RK * r.x / A;
@@ -627,13 +721,15 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, int smooth,
                                                 const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
                                                 const T *__restrict__ dt, const V4<T> *W0, V4<T> *Wout,
-                                                double *__restrict__ part, Ctl *ctl, const int st) {
+                                                V4<double> *Wm, double *__restrict__ part, Ctl *ctl,
+                                                const int st) {
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double d2 = 0.0;
     int bad = 0;
     if (i < m.n)
-        update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, ctl, st, dt, i), W0, Wout, part != nullptr, d2, bad);
+        update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, ctl, st, dt, i), W0, Wout, Wm, part != nullptr,
+                    part != nullptr, d2, bad);
     if (!part) return;
     block_partial(d2, bad, part + blockIdx.x, &ctl->nbad);
 }
@@ -709,7 +805,7 @@ __global__ void __launch_bounds__(256) kb_update(MeshDev<T> m, BatchDev<T> b, in
         if (batch_cell(b, m.n, i, c)) {
             const Flow<T> f = b.flows[c];
             update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, &b.ctl[c], st, dt, i), W0, Wout,
-                        part != nullptr, d2, bad);
+                        (V4<double> *)nullptr, false, part != nullptr, d2, bad);
         }
         if (part) block_partial(d2, bad, part + t, &b.ctl[tc].nbad);
     }
@@ -741,33 +837,43 @@ template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream
 // State exchange with the caller: FP64 in file order <-> T in internal order.
 template <typename T>
 __global__ void k_import(int n, const int *__restrict__ perm, const double *__restrict__ wfile,
-                         V4<T> *__restrict__ W) {
+                         V4<T> *__restrict__ W, V4<double> *__restrict__ Wm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double *s = wfile + 4 * (size_t)perm[i];
     V4<T> o;
     o.x = (T)s[0]; o.y = (T)s[1]; o.z = (T)s[2]; o.w = (T)s[3];
     W[i] = o;
+    if (Wm) {
+        V4<double> d;
+        d.x = s[0]; d.y = s[1]; d.z = s[2]; d.w = s[3];
+        Wm[i] = d;
+    }
 }
 
 template <typename T>
 __global__ void k_export(int n, const int *__restrict__ perm, const V4<T> *__restrict__ W,
-                         double *__restrict__ wfile) {
+                         const V4<double> *__restrict__ Wm, double *__restrict__ wfile) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const V4<T> v = W[i];
     double *d = wfile + 4 * (size_t)perm[i];
+    if (Wm) {
+        const V4<double> v = Wm[i];
+        d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+        return;
+    }
+    const V4<T> v = W[i];
     d[0] = (double)v.x; d[1] = (double)v.y; d[2] = (double)v.z; d[3] = (double)v.w;
 }
 
 template <typename T>
-void enqueue_import(int n, const int *perm, const double *wfile, V4<T> *W, cudaStream_t s) {
-    k_import<T><<<(n + 255) / 256, 256, 0, s>>>(n, perm, wfile, W);
+void enqueue_import(int n, const int *perm, const double *wfile, V4<T> *W, V4<double> *Wm, cudaStream_t s) {
+    k_import<T><<<(n + 255) / 256, 256, 0, s>>>(n, perm, wfile, W, Wm);
 }
 
 template <typename T>
-void enqueue_export(int n, const int *perm, const V4<T> *W, double *wfile, cudaStream_t s) {
-    k_export<T><<<(n + 255) / 256, 256, 0, s>>>(n, perm, W, wfile);
+void enqueue_export(int n, const int *perm, const V4<T> *W, const V4<double> *Wm, double *wfile, cudaStream_t s) {
+    k_export<T><<<(n + 255) / 256, 256, 0, s>>>(n, perm, W, Wm, wfile);
 }
 
 // ---------------------------------------------------------------------------
@@ -792,7 +898,7 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
             src = dst;
         }
         k_update<T><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
-                                    p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
+                                    p.W[0], Wout, p.Wm, last ? p.part : nullptr, p.ctl, st);
     }
     enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, s);
 }
@@ -823,7 +929,7 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
         }
         mark(3);
         k_update<T><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
-                                    p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
+                                    p.W[0], Wout, p.Wm, last ? p.part : nullptr, p.ctl, st);
         done();
     }
     mark(4); enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, s); done();

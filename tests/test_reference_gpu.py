@@ -107,6 +107,9 @@ def test_reference_diverges_on_the_transonic_case_too(lib, oracle):
     with pytest.raises(Exception, match="diverged"):
         s.step(n)
     assert abs(len(s.history()) - (bad[0] + 1)) < 500
-    # before the blow-up the two histories overlay (the reference's FMA-contracted
-    # kernels drift from the FP64 path only by rounding growth)
-    np.testing.assert_allclose(s.history()[:100], res[:100], rtol=1e-6)
+    # The printed residual values are not compared: the reference's
+    # kernel_drou finishes its block sum with a warp-synchronous reduction on a
+    # non-volatile shared array without __syncwarp (gpu_solver.cu:1008-1016),
+    # which on current GPUs drops terms, so its Resd differs from the full sum
+    # by a few percent from iteration 2 on while its state agrees with this
+    # library's to 1e-10 (test_reference_gpu_program_matches).
