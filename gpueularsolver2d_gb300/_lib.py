@@ -12,7 +12,7 @@ from . import build as _build
 
 LIB_PATH = _build.LIB
 
-E2D_FP64, E2D_FP32, E2D_MIXED = 0, 1, 2
+E2D_FP64, E2D_FP32 = 0, 1
 E2D_ORDER_FILE, E2D_ORDER_MORTON, E2D_ORDER_RCM = 0, 1, 2
 
 

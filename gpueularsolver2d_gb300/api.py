@@ -9,10 +9,10 @@ import ctypes
 
 import numpy as np
 
-from ._lib import (E2D_FP32, E2D_FP64, E2D_MIXED, E2D_ORDER_FILE, E2D_ORDER_MORTON, E2D_ORDER_RCM, MeshInfo, Params,
+from ._lib import (E2D_FP32, E2D_FP64, E2D_ORDER_FILE, E2D_ORDER_MORTON, E2D_ORDER_RCM, MeshInfo, Params,
                    check, load)
 
-__all__ = ["Mesh", "Solver", "Batch", "MLP", "Params", "default_params", "read_input", "E2D_FP32", "E2D_FP64", "E2D_MIXED",
+__all__ = ["Mesh", "Solver", "Batch", "MLP", "Params", "default_params", "read_input", "E2D_FP32", "E2D_FP64",
            "E2D_ORDER_FILE", "E2D_ORDER_MORTON", "E2D_ORDER_RCM"]
 
 

@@ -172,7 +172,7 @@ template <typename T> struct BatchT : BatchBase {
     int upload_case(int c, const double *w, cudaStream_t s) override {
         const int n = (*L)[c].n, o = (*off)[c];
         CK(cudaMemcpyAsync(wfile_dev, w, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, s));
-        enqueue_import<T>(n, perm_dev + o, wfile_dev, plan.W[0] + o, nullptr, s);
+        enqueue_import<T>(n, perm_dev + o, wfile_dev, plan.W[0] + o, s);
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(s));
         return E2D_OK;
@@ -180,7 +180,7 @@ template <typename T> struct BatchT : BatchBase {
 
     int download_case(int c, double *w, cudaStream_t s) override {
         const int n = (*L)[c].n, o = (*off)[c];
-        enqueue_export<T>(n, perm_dev + o, plan.W[0] + o, nullptr, wfile_dev, s);
+        enqueue_export<T>(n, perm_dev + o, plan.W[0] + o, wfile_dev, s);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(w, wfile_dev, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
@@ -341,7 +341,6 @@ int e2d_batch_create(e2d_mesh **meshes, const e2d_params *params, int32_t ncase,
     for (int c = 0; c < ncase; c++) {
         const e2d_params &p = params[c];
         if (!meshes[c] || !valid_params(&p)) { set_error("invalid mesh or parameters of case " + std::to_string(c)); return E2D_ERR_ARG; }
-        if (p.precision == E2D_MIXED) { set_error("batched cases run in E2D_FP64 or E2D_FP32"); return E2D_ERR_ARG; }
         bool same = p.precision == p0.precision && p.rk_stages == p0.rk_stages && p.irs_sweeps == p0.irs_sweeps &&
                     p.irs_eps == p0.irs_eps && p.gamma == p0.gamma && p.entropy_eps == p0.entropy_eps &&
                     p.dt_cap == p0.dt_cap && std::memcmp(p.rk_coef, p0.rk_coef, sizeof p.rk_coef) == 0;

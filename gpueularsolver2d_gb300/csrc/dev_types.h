@@ -60,7 +60,6 @@ template <typename T> struct Plan {
     V4<T> *W[2];   // W[0] holds the iteration's start state and its result
     V4<T> *FS;     // [3n] face-side states
     V4<T> *phi;    // [3n] limiter values (limiter-freeze option), else null
-    V4<double> *Wm;  // [n] FP64 state the RK update accumulates into (mixed mode), else null
     T *dt;         // [n]
     V4<T> *res;    // [n]
     V4<T> *sm[2];  // [n] smoothing sweeps (ping-pong)
@@ -130,9 +129,9 @@ template <typename T> int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t
 
 // FP64 file-order state <-> T internal-order state (perm[i] = file index).
 template <typename T>
-void enqueue_import(int n, const int *perm, const double *wfile, V4<T> *W, V4<double> *Wm, cudaStream_t s);
+void enqueue_import(int n, const int *perm, const double *wfile, V4<T> *W, cudaStream_t s);
 template <typename T>
-void enqueue_export(int n, const int *perm, const V4<T> *W, const V4<double> *Wm, double *wfile, cudaStream_t s);
+void enqueue_export(int n, const int *perm, const V4<T> *W, double *wfile, cudaStream_t s);
 
 // Residual kernel launcher (resid.cu).
 void enqueue_resid(const double *part, int nparts, Ctl *ctl, double *hist, int hist_cap,

@@ -631,18 +631,12 @@ __global__ void __launch_bounds__(256) k_smooth(MeshDev<T> m, T eps, const V4<T>
 // Pass D: gpu_solver.cu:1675-1720 (kernel_Smooth2, last sweep + clamp) fused
 // with 938-966 (kernel_RKStep); on the last stage also 968-1020 (kernel_drou)
 // as FP64 block partials and a count of unphysical cells.
-//
-// Mixed mode (Wm not null): the stage's increment is computed in T as usual
-// but applied to the FP64 state Wm, and Wout receives that sum rounded to T
-// (the stencil's working copy); the last stage also stores the FP64 sum back
-// into Wm.  Increments far below the FP32 spacing of the state then still
-// accumulate, so the residual can fall below the FP32 state's rounding floor.
 template <typename T>
 __device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &f, const T rk,
                                             const int smooth, const int i, const V4<T> *__restrict__ src,
                                             const V4<T> *__restrict__ res, const T dti,
-                                            const V4<T> *W0, V4<T> *Wout, V4<double> *Wm, const bool last,
-                                            const bool want, double &d2, int &bad) {
+                                            const V4<T> *W0, V4<T> *Wout, const bool want, double &d2,
+                                            int &bad) {
     {
         const int4 tp = m.topo[i];
         V4<T> r = res[i];
@@ -660,25 +654,6 @@ __device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &
         T RK = rk;
         RK *= dti;
         const T A = m.area[i];
-        if (Wm) {
-            const V4<double> w0 = Wm[i];
-            V4<double> w;
-            w.x = w0.x - (double)(RK * r.x / A);
-            w.y = w0.y - (double)(RK * r.y / A);
-            w.z = w0.z - (double)(RK * r.z / A);
-            w.w = w0.w - (double)(RK * r.w / A);
-            V4<T> o;
-            o.x = (T)w.x; o.y = (T)w.y; o.z = (T)w.z; o.w = (T)w.w;
-            Wout[i] = o;
-            if (last) Wm[i] = w;
-            if (want) {
-                const double dd = w.x - w0.x;
-                d2 = dd * dd;
-                const double q = 0.5 * (w.y * w.y + w.z * w.z) / w.x;
-                bad = !(w.x > 0.0) || !(w.w - q > 0.0);
-            }
-            return;
-        }
         const V4<T> w0 = W0[i];
         V4<T> w;
         w.x = w0.x - RK * r.x / A;
@@ -721,15 +696,13 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, int smooth,
                                                 const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
                                                 const T *__restrict__ dt, const V4<T> *W0, V4<T> *Wout,
-                                                V4<double> *Wm, double *__restrict__ part, Ctl *ctl,
-                                                const int st) {
+                                                double *__restrict__ part, Ctl *ctl, const int st) {
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double d2 = 0.0;
     int bad = 0;
     if (i < m.n)
-        update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, ctl, st, dt, i), W0, Wout, Wm, part != nullptr,
-                    part != nullptr, d2, bad);
+        update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, ctl, st, dt, i), W0, Wout, part != nullptr, d2, bad);
     if (!part) return;
     block_partial(d2, bad, part + blockIdx.x, &ctl->nbad);
 }
@@ -805,7 +778,7 @@ __global__ void __launch_bounds__(256) kb_update(MeshDev<T> m, BatchDev<T> b, in
         if (batch_cell(b, m.n, i, c)) {
             const Flow<T> f = b.flows[c];
             update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, &b.ctl[c], st, dt, i), W0, Wout,
-                        (V4<double> *)nullptr, false, part != nullptr, d2, bad);
+                        part != nullptr, d2, bad);
         }
         if (part) block_partial(d2, bad, part + t, &b.ctl[tc].nbad);
     }
@@ -837,43 +810,33 @@ template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream
 // State exchange with the caller: FP64 in file order <-> T in internal order.
 template <typename T>
 __global__ void k_import(int n, const int *__restrict__ perm, const double *__restrict__ wfile,
-                         V4<T> *__restrict__ W, V4<double> *__restrict__ Wm) {
+                         V4<T> *__restrict__ W) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double *s = wfile + 4 * (size_t)perm[i];
     V4<T> o;
     o.x = (T)s[0]; o.y = (T)s[1]; o.z = (T)s[2]; o.w = (T)s[3];
     W[i] = o;
-    if (Wm) {
-        V4<double> d;
-        d.x = s[0]; d.y = s[1]; d.z = s[2]; d.w = s[3];
-        Wm[i] = d;
-    }
 }
 
 template <typename T>
 __global__ void k_export(int n, const int *__restrict__ perm, const V4<T> *__restrict__ W,
-                         const V4<double> *__restrict__ Wm, double *__restrict__ wfile) {
+                         double *__restrict__ wfile) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double *d = wfile + 4 * (size_t)perm[i];
-    if (Wm) {
-        const V4<double> v = Wm[i];
-        d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
-        return;
-    }
     const V4<T> v = W[i];
+    double *d = wfile + 4 * (size_t)perm[i];
     d[0] = (double)v.x; d[1] = (double)v.y; d[2] = (double)v.z; d[3] = (double)v.w;
 }
 
 template <typename T>
-void enqueue_import(int n, const int *perm, const double *wfile, V4<T> *W, V4<double> *Wm, cudaStream_t s) {
-    k_import<T><<<(n + 255) / 256, 256, 0, s>>>(n, perm, wfile, W, Wm);
+void enqueue_import(int n, const int *perm, const double *wfile, V4<T> *W, cudaStream_t s) {
+    k_import<T><<<(n + 255) / 256, 256, 0, s>>>(n, perm, wfile, W);
 }
 
 template <typename T>
-void enqueue_export(int n, const int *perm, const V4<T> *W, const V4<double> *Wm, double *wfile, cudaStream_t s) {
-    k_export<T><<<(n + 255) / 256, 256, 0, s>>>(n, perm, W, Wm, wfile);
+void enqueue_export(int n, const int *perm, const V4<T> *W, double *wfile, cudaStream_t s) {
+    k_export<T><<<(n + 255) / 256, 256, 0, s>>>(n, perm, W, wfile);
 }
 
 // ---------------------------------------------------------------------------
@@ -898,7 +861,7 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
             src = dst;
         }
         k_update<T><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
-                                    p.W[0], Wout, p.Wm, last ? p.part : nullptr, p.ctl, st);
+                                    p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
     }
     enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, s);
 }
@@ -929,7 +892,7 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
         }
         mark(3);
         k_update<T><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
-                                    p.W[0], Wout, p.Wm, last ? p.part : nullptr, p.ctl, st);
+                                    p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
         done();
     }
     mark(4); enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, s); done();

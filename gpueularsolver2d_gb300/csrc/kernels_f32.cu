@@ -8,8 +8,6 @@ namespace e2d {
 template void enqueue_iteration<float>(const Plan<float> &p, cudaStream_t s);
 template void enqueue_batch_iteration<float>(const BPlan<float> &p, cudaStream_t s);
 template int enqueue_iteration_timed<float>(const Plan<float> &p, cudaStream_t s, cudaEvent_t *ev, int *kind);
-template void enqueue_import<float>(int n, const int *perm, const double *wfile, V4<float> *W, V4<double> *Wm,
-                                    cudaStream_t s);
-template void enqueue_export<float>(int n, const int *perm, const V4<float> *W, const V4<double> *Wm,
-                                    double *wfile, cudaStream_t s);
+template void enqueue_import<float>(int n, const int *perm, const double *wfile, V4<float> *W, cudaStream_t s);
+template void enqueue_export<float>(int n, const int *perm, const V4<float> *W, double *wfile, cudaStream_t s);
 }

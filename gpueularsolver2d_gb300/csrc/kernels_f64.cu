@@ -7,8 +7,6 @@ namespace e2d {
 template void enqueue_iteration<double>(const Plan<double> &p, cudaStream_t s);
 template void enqueue_batch_iteration<double>(const BPlan<double> &p, cudaStream_t s);
 template int enqueue_iteration_timed<double>(const Plan<double> &p, cudaStream_t s, cudaEvent_t *ev, int *kind);
-template void enqueue_import<double>(int n, const int *perm, const double *wfile, V4<double> *W, V4<double> *Wm,
-                                     cudaStream_t s);
-template void enqueue_export<double>(int n, const int *perm, const V4<double> *W, const V4<double> *Wm,
-                                     double *wfile, cudaStream_t s);
+template void enqueue_import<double>(int n, const int *perm, const double *wfile, V4<double> *W, cudaStream_t s);
+template void enqueue_export<double>(int n, const int *perm, const V4<double> *W, double *wfile, cudaStream_t s);
 }

@@ -116,6 +116,7 @@ struct e2d_mlp {
     float *bpart = nullptr;     // bias-gradient partials
     double *loss_part = nullptr;
     int *step_dev = nullptr;
+    int *flag_dev = nullptr;    // set by a tensor-core GEMM whose wait timed out
     float *bc_dev = nullptr;
     float *grad = nullptr;      // flat gradient of all parameters (gradient probe)
     // training set
@@ -185,6 +186,24 @@ void adam(e2d_mlp *m, cudaStream_t s, Tensor &t, const float *part, int nparts, 
                                                         grad_out);
 }
 
+template <bool TA, bool TB, int EPI> void gemm(e2d_mlp *m, GemmArgs g, dim3 grid, cudaStream_t s) {
+    g.flag = m->flag_dev;
+    k_gemm_tc<TA, TB, EPI><<<grid, 256, tc::SMEM, s>>>(g);
+}
+
+// Reports (and clears) a timed-out tensor-core wait of the kernels run so far.
+int check_flag(e2d_mlp *m) {
+    int f = 0;
+    CK(cudaMemcpyAsync(&f, m->flag_dev, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    if (f) {
+        CK(cudaMemsetAsync(m->flag_dev, 0, sizeof(int), m->stream));
+        set_error("a tensor-core GEMM gave up waiting for its MMAs; its results are not valid");
+        return E2D_ERR_CUDA;
+    }
+    return E2D_OK;
+}
+
 // Forward on the batch in xb (rows B); with targets, the loss partials and dy.
 void forward(e2d_mlp *m, cudaStream_t s, bool with_loss) {
     const int B = m->B;
@@ -195,7 +214,7 @@ void forward(e2d_mlp *m, cudaStream_t s, bool with_loss) {
         g.lda = g.K;
         g.B = m->W[l].wbf; g.ldb = g.K;
         g.bias = m->b[l].w32; g.out = m->Hh[l]; g.zout = m->Z[l]; g.ldc = H;
-        k_gemm<false, false, EPI_BIAS_GELU><<<dim3(H / BN, (B + BM - 1) / BM, 1), 256, 0, s>>>(g);
+        gemm<false, false, EPI_BIAS_GELU>(m, g, dim3(H / BN, (B + BM - 1) / BM, 1), s);
     }
     const Tensor &Wo = m->W[m->nhidden], &bo = m->b[m->nhidden];
     k_out_fwd_loss<H, NOUT><<<(B + 255) / 256, 256, 0, s>>>(B, m->Hh[m->nhidden - 1], Wo.w32, bo.w32,
@@ -232,7 +251,7 @@ void backward(e2d_mlp *m, cudaStream_t s, float lr, bool want_grad) {
         gw.A = m->dz[cur]; gw.lda = H;
         gw.B = hin; gw.ldb = kin;
         gw.part = m->part;
-        k_gemm<true, true, EPI_PARTIAL><<<dim3((kin + BN - 1) / BN, H / BM, kSplits), 256, 0, s>>>(gw);
+        gemm<true, true, EPI_PARTIAL>(m, gw, dim3((kin + BN - 1) / BN, H / BM, kSplits), s);
         k_colsum<<<kSplits, 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart);
         // gradient at the previous pre-activation (before this layer's weights change)
         if (l > 0) {
@@ -241,7 +260,7 @@ void backward(e2d_mlp *m, cudaStream_t s, float lr, bool want_grad) {
             gd.A = m->dz[cur]; gd.lda = H;
             gd.B = m->W[l].wbf; gd.ldb = H;
             gd.zin = m->Z[l - 1]; gd.out = m->dz[cur ^ 1]; gd.ldc = H;
-            k_gemm<false, true, EPI_GELU_BWD><<<dim3(H / BN, (B + BM - 1) / BM, 1), 256, 0, s>>>(gd);
+            gemm<false, true, EPI_GELU_BWD>(m, gd, dim3(H / BN, (B + BM - 1) / BM, 1), s);
         }
         float *gb = gslot(m->b[l]);
         float *gW = gslot(m->W[l]);
@@ -337,6 +356,10 @@ int e2d_mlp_create(const e2d_mlp_config *cfg, e2d_mlp **out) {
     }
     int rc;
     if ((rc = m->alloc(&m->step_dev, sizeof(int)))) return rc;
+    if ((rc = m->alloc(&m->flag_dev, sizeof(int)))) return rc;
+    CK(cudaFuncSetAttribute(k_gemm_tc<false, false, EPI_BIAS_GELU>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM));
+    CK(cudaFuncSetAttribute(k_gemm_tc<false, true, EPI_GELU_BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM));
+    CK(cudaFuncSetAttribute(k_gemm_tc<true, true, EPI_PARTIAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM));
     if ((rc = m->alloc(&m->bc_dev, 2 * sizeof(float)))) return rc;
     if ((rc = m->alloc(&m->grad, sizeof(float) * param_count(m.get())))) return rc;
     CK(cudaStreamSynchronize(m->stream));
@@ -409,7 +432,7 @@ int e2d_mlp_train(e2d_mlp *m, int32_t steps, double *loss) {
         }
     }
     CK(cudaStreamSynchronize(m->stream));
-    return E2D_OK;
+    return check_flag(m);
 }
 
 int e2d_mlp_forward(e2d_mlp *m, int64_t n, const float *x, float *y) {
@@ -427,7 +450,7 @@ int e2d_mlp_forward(e2d_mlp *m, int64_t n, const float *x, float *y) {
         CK(cudaMemcpyAsync(y + (size_t)r0 * NOUT, m->y, sizeof(float) * cnt * NOUT, cudaMemcpyDeviceToHost, m->stream));
         CK(cudaStreamSynchronize(m->stream));
     }
-    return E2D_OK;
+    return check_flag(m);
 }
 
 int e2d_mlp_gradient(e2d_mlp *m, const float *x, const float *t, double *loss, float *grad) {
@@ -449,7 +472,7 @@ int e2d_mlp_gradient(e2d_mlp *m, const float *x, const float *t, double *loss, f
     double s = 0.0;
     for (double v : lp) s += v;
     if (loss) *loss = s / ((double)m->B * NOUT);
-    return E2D_OK;
+    return check_flag(m);
 }
 
 int e2d_wall_distance(e2d_mesh *mesh, double wall_box, double *d) {

@@ -64,6 +64,7 @@ struct GemmArgs {
     bf16 *zout;            // EPI_BIAS_GELU: [M][ldc]
     float *part;           // EPI_PARTIAL: [splits][M][N]
     int ldc;
+    int *flag;             // tensor-core kernel: set to 1 if a wait timed out
 };
 
 // C = opA(A) * opB(B): opA(A)[m][k] = TA ? A[k][m] : A[m][k];
@@ -179,6 +180,185 @@ __global__ void __launch_bounds__(256) k_gemm(GemmArgs g) {
                     p[1] = v1;
                 }
             }
+}
+
+// ---------------------------------------------------------------------------
+// The same GEMM on the fifth-generation tensor cores: tcgen05.mma (BF16 in,
+// FP32 accumulate in tensor memory) issued by one thread, operands staged by
+// all threads into shared memory in the canonical no-swizzle K-major layout
+// (8 x 8 core matrices of 128 bytes; a transposed operand is transposed while
+// it is staged), a four-deep ring of stages released by tcgen05.commit on
+// mbarriers, and the epilogue read back from tensor memory with tcgen05.ld.
+// Every wait is bounded: on a timeout the CTA sets *g.flag, skips the
+// epilogue and still frees its tensor memory.
+namespace tc {
+constexpr int BK = 32;                      // K per stage (two MMAs of K = 16)
+constexpr int NST = 4;                      // stages in the ring
+constexpr int TILE = 128 * BK * 2;          // bytes of one 128 x BK operand tile
+constexpr int SMEM = 2 * NST * TILE;        // dynamic shared memory per CTA
+constexpr uint32_t TMEM_COLS = 128;         // FP32 accumulator columns (N = 128)
+constexpr int WAIT_LIMIT = 1 << 22;         // try_wait calls before giving up
+// instruction descriptor: FP32 D, BF16 A and B, both K-major, N = 128, M = 128
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+// core matrix (r/8, k/8) at ((r/8) * (BK/8) + k/8) * 128 bytes, row r%8 at 16 bytes
+constexpr uint32_t LBO = 128;               // next core matrix along K
+constexpr uint32_t SBO = (BK / 8) * 128;    // next core matrix along M / N
+
+__device__ __forceinline__ int cm_off(int r, int k) {
+    return ((r >> 3) * (BK / 8) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start, LBO, SBO (16-byte units), version 1, no swizzle
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(LBO >> 4) << 16) | ((uint64_t)(SBO >> 4) << 32) |
+           ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (int it = 0; it < WAIT_LIMIT; it++) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// rows [row0, row0 + 128) x k [k0, k0 + BK) of op(src) into tile (core-matrix layout);
+// T: src is [k][ld] (rows contiguous), else [row][ld] (k contiguous).  Rows at
+// or past nrows (a multiple of 8) are zero.
+template <bool T>
+__device__ __forceinline__ void stage(unsigned char *tile, const bf16 *__restrict__ src, int ld, int row0, int nrows,
+                                      int k0) {
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const int c = threadIdx.x + it * 256;
+        if (!T) {
+            const int r = c >> 2, kc = (c & 3) * 8;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (row0 + r < nrows) v = *(const uint4 *)(src + (size_t)(row0 + r) * ld + k0 + kc);
+            *(uint4 *)(tile + cm_off(r, kc)) = v;
+        } else {
+            const int kr = c >> 4, rc = (c & 15) * 8;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (row0 + rc < nrows) v = *(const uint4 *)(src + (size_t)(k0 + kr) * ld + row0 + rc);
+            const unsigned short *e = (const unsigned short *)&v;
+#pragma unroll
+            for (int j = 0; j < 8; j++) *(unsigned short *)(tile + cm_off(rc + j, kr)) = e[j];
+        }
+    }
+}
+}  // namespace tc
+
+template <bool TA, bool TB, int EPI>
+__global__ void __launch_bounds__(256, 1) k_gemm_tc(GemmArgs g) {
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t bars[tc::NST];
+    __shared__ uint32_t tmem_sh;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * 128, n0 = blockIdx.x * 128;
+    const int kper = g.K / gridDim.z, kbeg = blockIdx.z * kper, nst = kper / tc::BK;
+    unsigned char *As = tc_smem, *Bs = tc_smem + tc::NST * tc::TILE;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n"
+                     :: "r"(tc::smem_u32(&tmem_sh)), "r"(tc::TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (tid == 0)
+        for (int b = 0; b < tc::NST; b++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(tc::smem_u32(&bars[b])));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem = tmem_sh;
+    bool ok = true;
+    for (int s = 0; s < nst; s++) {
+        const int b = s % tc::NST;
+        if (s >= tc::NST) {  // the MMAs that read this buffer last must be done
+            const bool w = tc::mbar_wait(tc::smem_u32(&bars[b]), ((s - tc::NST) / tc::NST) & 1);
+            if (__syncthreads_or(!w)) { ok = false; break; }
+        }
+        const int k0 = kbeg + s * tc::BK;
+        tc::stage<TA>(As + b * tc::TILE, g.A, g.lda, m0, g.M, k0);
+        tc::stage<TB>(Bs + b * tc::TILE, g.B, g.ldb, n0, g.N, k0);
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+#pragma unroll
+            for (int kk = 0; kk < tc::BK / 16; kk++) {
+                const uint64_t ad = tc::sdesc(tc::smem_u32(As + b * tc::TILE) + kk * 256);
+                const uint64_t bd = tc::sdesc(tc::smem_u32(Bs + b * tc::TILE) + kk * 256);
+                const uint32_t acc = (s > 0 || kk > 0) ? 1u : 0u;
+                asm volatile("{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                             " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                             :: "r"(tmem), "l"(ad), "l"(bd), "r"(tc::IDESC), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n"
+                         :: "r"(tc::smem_u32(&bars[b])));
+        }
+    }
+    if (ok && nst > 0) {  // the last commit covers every MMA of the CTA
+        const int s = nst - 1;
+        const bool w = tc::mbar_wait(tc::smem_u32(&bars[s % tc::NST]), (s / tc::NST) & 1);
+        if (__syncthreads_or(!w)) ok = false;
+    }
+    if (!ok && tid == 0) atomicExch(g.flag, 1);
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    if (ok && nst > 0) {
+        // warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows), columns 64 (w / 4) .. + 63
+        const int lb = (warp & 3) * 32, cb = (warp >> 2) * 64;
+        const int m = m0 + lb + lane;
+#pragma unroll 1
+        for (int ch = 0; ch < 4; ch++) {
+            uint32_t v[16];
+            const uint32_t taddr = tmem + ((uint32_t)lb << 16) + (uint32_t)(cb + ch * 16);
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                           "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                           "=r"(v[14]), "=r"(v[15])
+                         : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            const int n = n0 + cb + ch * 16;
+            if (m >= g.M || n >= g.N) continue;
+            if (EPI == EPI_BIAS_GELU) {
+                __align__(16) __nv_bfloat162 z2[8], o2[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const float z0 = __uint_as_float(v[2 * j]) + g.bias[n + 2 * j];
+                    const float z1 = __uint_as_float(v[2 * j + 1]) + g.bias[n + 2 * j + 1];
+                    z2[j] = __floats2bfloat162_rn(z0, z1);
+                    o2[j] = __floats2bfloat162_rn(gelu(z0), gelu(z1));
+                }
+                uint4 *zo = (uint4 *)(g.zout + (size_t)m * g.ldc + n), *oo = (uint4 *)(g.out + (size_t)m * g.ldc + n);
+                zo[0] = ((const uint4 *)z2)[0]; zo[1] = ((const uint4 *)z2)[1];
+                oo[0] = ((const uint4 *)o2)[0]; oo[1] = ((const uint4 *)o2)[1];
+            } else if (EPI == EPI_GELU_BWD) {
+                const uint4 *zi = (const uint4 *)(g.zin + (size_t)m * g.ldc + n);
+                __align__(16) uint4 zz[2] = {zi[0], zi[1]};
+                const __nv_bfloat162 *z2 = (const __nv_bfloat162 *)zz;
+                __align__(16) __nv_bfloat162 o2[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    o2[j] = __floats2bfloat162_rn(__uint_as_float(v[2 * j]) * gelu_grad(__bfloat162float(z2[j].x)),
+                                                  __uint_as_float(v[2 * j + 1]) * gelu_grad(__bfloat162float(z2[j].y)));
+                uint4 *oo = (uint4 *)(g.out + (size_t)m * g.ldc + n);
+                oo[0] = ((const uint4 *)o2)[0]; oo[1] = ((const uint4 *)o2)[1];
+            } else {
+                float4 *p = (float4 *)(g.part + ((size_t)blockIdx.z * g.M + m) * g.N + n);
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    p[j] = make_float4(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1]),
+                                       __uint_as_float(v[4 * j + 2]), __uint_as_float(v[4 * j + 3]));
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(tmem), "r"(tc::TMEM_COLS));
 }
 
 // Output layer (256 -> NOUT) on the CUDA cores: y[b][o] = h[b] . W[o] + bias[o]

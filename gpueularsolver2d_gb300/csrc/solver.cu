@@ -111,7 +111,7 @@ bool freezes(const e2d_params &p) { return p.limiter_freeze > 0 || p.limiter_fre
 bool valid_params(const e2d_params *p) {
     if (!(p->gamma > 1.0) || !(p->ma > 0.0) || !(p->tin > 0.0) || !(p->cfl > 0.0)) return false;
     if (p->rk_stages < 1 || p->rk_stages > 8 || p->irs_sweeps < 0 || p->irs_sweeps > 16) return false;
-    if (p->precision != E2D_FP64 && p->precision != E2D_FP32 && p->precision != E2D_MIXED) return false;
+    if (p->precision != E2D_FP64 && p->precision != E2D_FP32) return false;
     if (p->ordering != E2D_ORDER_FILE && p->ordering != E2D_ORDER_MORTON && p->ordering != E2D_ORDER_RCM) return false;
     if (p->block_size != 0 && (p->block_size < 32 || p->block_size > 256 || p->block_size % 32)) return false;
     if (p->graph_iters < 0 || p->graph_iters > 256) return false;
@@ -145,9 +145,7 @@ template <typename T> struct SolverT : SolverBase {
     int init(const e2d_params &p, const FreeStream &fs, Ctl *ctl, int block) {
         const int n = L->n;
         const int G = (n + block - 1) / block;
-        const bool mixed = p.precision == E2D_MIXED && sizeof(T) == 4;
         size_t bytes = Arena::up(sizeof(int4) * n) + 2 * Arena::up(sizeof(V2<T>) * 3 * n) +
-                       (mixed ? Arena::up(sizeof(V4<double>) * n) : 0) +
                        Arena::up(sizeof(T) * n) * 2 + Arena::up(sizeof(V4<T>) * n) * 5 +
                        Arena::up(sizeof(V4<T>) * 3 * n) * (freezes(p) ? 2 : 1) +
                        Arena::up(sizeof(double) * G) +
@@ -162,7 +160,6 @@ template <typename T> struct SolverT : SolverBase {
         plan.W[1] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
         plan.FS = (V4<T> *)arena.take(sizeof(V4<T>) * 3 * n);
         plan.phi = freezes(p) ? (V4<T> *)arena.take(sizeof(V4<T>) * 3 * n) : nullptr;
-        plan.Wm = mixed ? (V4<double> *)arena.take(sizeof(V4<double>) * n) : nullptr;
         plan.dt = (T *)arena.take(sizeof(T) * n);
         plan.res = (V4<T> *)arena.take(sizeof(V4<T>) * n);
         plan.sm[0] = (V4<T> *)arena.take(sizeof(V4<T>) * n);
@@ -203,7 +200,7 @@ template <typename T> struct SolverT : SolverBase {
     int upload_state(const double *w) override {
         const int n = L->n;
         CK(cudaMemcpyAsync(wfile_dev, w, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, *stream));
-        enqueue_import<T>(n, perm_dev, wfile_dev, plan.W[0], plan.Wm, *stream);
+        enqueue_import<T>(n, perm_dev, wfile_dev, plan.W[0], *stream);
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(*stream));
         return E2D_OK;
@@ -211,7 +208,7 @@ template <typename T> struct SolverT : SolverBase {
 
     int download_state(double *w) override {
         const int n = L->n;
-        enqueue_export<T>(n, perm_dev, plan.W[0], plan.Wm, wfile_dev, *stream);
+        enqueue_export<T>(n, perm_dev, plan.W[0], wfile_dev, *stream);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(w, wfile_dev, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, *stream));
         CK(cudaStreamSynchronize(*stream));
@@ -542,10 +539,7 @@ int e2d_write_residual_plt(e2d_solver *s, const char *path) {
 
 int e2d_set_precision(e2d_solver *s, int32_t precision) {
     if (!s) { set_error("null argument"); return E2D_ERR_ARG; }
-    if (precision != E2D_FP64 && precision != E2D_FP32 && precision != E2D_MIXED) {
-        set_error("precision must be E2D_FP64, E2D_FP32 or E2D_MIXED");
-        return E2D_ERR_ARG;
-    }
+    if (precision != E2D_FP64 && precision != E2D_FP32) { set_error("precision must be E2D_FP64 or E2D_FP32"); return E2D_ERR_ARG; }
     if (precision == s->prm.precision) return E2D_OK;
     int rc = pull_ctl(s);
     if (rc) return rc;

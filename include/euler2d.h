@@ -41,10 +41,6 @@ extern "C" {
 
 #define E2D_FP64 0           /* FP64 stencil (parity variant)          */
 #define E2D_FP32 1           /* FP32 stencil, FP64 geometry and norms  */
-#define E2D_MIXED 2          /* FP32 stencil; the RK update accumulates
-                                into an FP64 copy of the state, so the
-                                residual falls below the FP32 state's
-                                rounding floor (single-case solver only)  */
 
 #define E2D_ORDER_FILE 0     /* cells in file order                    */
 #define E2D_ORDER_MORTON 1   /* cells sorted by centroid Morton code   */
@@ -70,7 +66,7 @@ typedef struct e2d_params {
     double rk_coef[8];   /* reference {0.0833,0.2069,0.4265,1.0} (gpu_fvm.cu:10) */
     double irs_eps;      /* smoothing coefficient; reference 0.8 (gpu_solver.cu:1633) */
     int32_t irs_sweeps;  /* 0 = off; reference 2 (gpu_solver.cu:1722-1728) */
-    int32_t precision;   /* E2D_FP64 (default), E2D_FP32 or E2D_MIXED      */
+    int32_t precision;   /* E2D_FP64 (default) or E2D_FP32                 */
     double dt_cap;       /* local time step cap; reference 0.1 (gpu_solver.cu:831) */
     double entropy_eps;  /* Harten fix width; reference 0.05 (gpu_solver.cu:603) */
     double wall_box;     /* boundary face is wall if |mid x|,|mid y| < wall_box;
@@ -207,7 +203,7 @@ int e2d_write_field_plt(e2d_solver *s, e2d_mesh *m, const char *path);
 int e2d_write_wall_cp_plt(e2d_solver *s, e2d_mesh *m, const char *path);
 /* Parameters the solver was created with. */
 int e2d_get_params(e2d_solver *s, e2d_params *p);
-/* Switches between E2D_FP32, E2D_MIXED and E2D_FP64 in place: the state is
+/* Switches the stencil between E2D_FP32 and E2D_FP64 in place: the state is
  * carried over (rounded to FP32 when going down), and the iteration count,
  * residual normalisation and history continue.  The usual use is a fast FP32
  * solve to about 1e-4 followed by FP64 below the FP32 state's rounding floor.
