@@ -23,6 +23,7 @@
 #pragma once
 
 #include "dev_types.h"
+#include "pdl.cuh"
 
 namespace e2d {
 
@@ -419,6 +420,7 @@ template <typename T>
 __global__ void E2D_LB_FACES k_faces(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ W,
                                      V4<T> *__restrict__ FS, T *__restrict__ dt,
                                      Ctl *__restrict__ ctl, V4<T> *__restrict__ phi, const int st) {
+    wait_prior_grid();
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (!f.global_dt) {
@@ -569,6 +571,7 @@ __device__ __forceinline__ void flux_tile(const MeshDev<T> &m, const Flow<T> &f,
 template <typename T>
 __global__ void E2D_LB_FLUX k_flux_tile(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ FS,
                                         V4<T> *__restrict__ res, const Ctl *__restrict__ ctl) {
+    wait_prior_grid();
     if (ctl->halt) return;
     const int base = blockIdx.x * blockDim.x;
     flux_tile(m, f, base, min((int)blockDim.x, m.n - base), FS, res);
@@ -577,6 +580,7 @@ __global__ void E2D_LB_FLUX k_flux_tile(MeshDev<T> m, Flow<T> f, const V4<T> *__
 template <typename T>
 __global__ void E2D_LB_FLUX k_flux(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ FS,
                                    V4<T> *__restrict__ res, const Ctl *__restrict__ ctl) {
+    wait_prior_grid();
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.n) return;
@@ -621,6 +625,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_smooth(MeshDev<T> m, T eps, const V4<T> *__restrict__ src,
                                                 const V4<T> *__restrict__ res, V4<T> *__restrict__ dst,
                                                 const Ctl *__restrict__ ctl) {
+    wait_prior_grid();
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.n) return;
@@ -697,6 +702,7 @@ __global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, i
                                                 const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
                                                 const T *__restrict__ dt, const V4<T> *W0, V4<T> *Wout,
                                                 double *__restrict__ part, Ctl *ctl, const int st) {
+    wait_prior_grid();
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double d2 = 0.0;
@@ -723,6 +729,7 @@ template <typename T>
 __global__ void E2D_LB_FACES kb_faces(MeshDev<T> m, BatchDev<T> b, int ntiles, const V4<T> *__restrict__ W,
                                       V4<T> *__restrict__ FS, T *__restrict__ dt, V4<T> *__restrict__ phi,
                                       const int st) {
+    wait_prior_grid();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int i = t * blockDim.x + threadIdx.x;
         const int tc = b.chunk_case[(t * blockDim.x) / kChunk];  // the tile's case
@@ -739,6 +746,7 @@ __global__ void E2D_LB_FACES kb_faces(MeshDev<T> m, BatchDev<T> b, int ntiles, c
 template <typename T>
 __global__ void E2D_LB_FLUX kb_flux(MeshDev<T> m, BatchDev<T> b, int ntiles, const V4<T> *__restrict__ FS,
                                     V4<T> *__restrict__ res) {
+    wait_prior_grid();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int base = t * blockDim.x;
         const int tc = b.chunk_case[base / kChunk];  // every cell of a tile is in one case
@@ -757,6 +765,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) kb_smooth(MeshDev<T> m, BatchDev<T> b, int ntiles, T eps,
                                                  const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
                                                  V4<T> *__restrict__ dst) {
+    wait_prior_grid();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int i = t * blockDim.x + threadIdx.x;
         int c;
@@ -769,6 +778,7 @@ __global__ void __launch_bounds__(256) kb_update(MeshDev<T> m, BatchDev<T> b, in
                                                  const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
                                                  const T *__restrict__ dt, const V4<T> *W0, V4<T> *Wout,
                                                  double *__restrict__ part, const int st) {
+    wait_prior_grid();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int tc = b.chunk_case[(t * blockDim.x) / kChunk];  // the tile's case
         if (b.ctl[tc].halt) continue;                             // uniform over the block
@@ -792,16 +802,16 @@ template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream
         const bool last = st == p.stages - 1;
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
-        kb_faces<T><<<G, B, 0, s>>>(p.m, p.b, NT, Wcur, p.FS, p.dt, p.phi, st);
-        kb_flux<T><<<G, B, 0, s>>>(p.m, p.b, NT, p.FS, p.res);
+        launch_chained(kb_faces<T>, G, B, s, p.m, p.b, NT, Wcur, p.FS, p.dt, p.phi, st);
+        launch_chained(kb_flux<T>, G, B, s, p.m, p.b, NT, p.FS, p.res);
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
             V4<T> *dst = p.sm[sw & 1];
-            kb_smooth<T><<<G, B, 0, s>>>(p.m, p.b, NT, p.f.irs_eps, src, p.res, dst);
+            launch_chained(kb_smooth<T>, G, B, s, p.m, p.b, NT, p.f.irs_eps, src, p.res, dst);
             src = dst;
         }
-        kb_update<T><<<G, B, 0, s>>>(p.m, p.b, NT, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt, p.W[0],
-                                     Wout, last ? p.part : nullptr, st);
+        launch_chained(kb_update<T>, G, B, s, p.m, p.b, NT, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
+                       p.W[0], Wout, last ? p.part : nullptr, st);
     }
     enqueue_batch_resid(p.part, p.case_tiles, p.ncase, p.b.ctl, p.hist, p.hist_cap, s);
 }
@@ -851,17 +861,17 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
         const bool last = st == p.stages - 1;
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
-        k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
-        if (FluxTiled<T>::value) k_flux_tile<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
-        else k_flux<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
+        launch_chained(k_faces<T>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
+        if (FluxTiled<T>::value) launch_chained(k_flux_tile<T>, G, B, s, p.m, p.f, p.FS, p.res, p.ctl);
+        else launch_chained(k_flux<T>, G, B, s, p.m, p.f, p.FS, p.res, p.ctl);
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
             V4<T> *dst = p.sm[sw & 1];
-            k_smooth<T><<<G, B, 0, s>>>(p.m, p.f.irs_eps, src, p.res, dst, p.ctl);
+            launch_chained(k_smooth<T>, G, B, s, p.m, p.f.irs_eps, src, p.res, dst, p.ctl);
             src = dst;
         }
-        k_update<T><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
-                                    p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
+        launch_chained(k_update<T>, G, B, s, p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
+                       p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
     }
     enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, s);
 }

@@ -1,5 +1,6 @@
 // resid.cu -- residual of one iteration (gpu_solver.cu:2404-2433).
 #include "dev_types.h"
+#include "pdl.cuh"
 
 namespace e2d {
 
@@ -37,6 +38,7 @@ __device__ __forceinline__ void resid_block(const double *__restrict__ part, int
 
 __global__ void __launch_bounds__(256) k_resid(const double *__restrict__ part, int nparts, Ctl *ctl,
                                                double *hist, int hist_cap) {
+    wait_prior_grid();
     if (ctl->halt) return;
     resid_block(part, nparts, ctl, hist, hist_cap);
 }
@@ -46,6 +48,7 @@ __global__ void __launch_bounds__(256) k_resid(const double *__restrict__ part, 
 // its partials is the one a single-case run of the same block size uses).
 __global__ void __launch_bounds__(256) kb_resid(const double *__restrict__ part, const int2 *case_tiles,
                                                 Ctl *ctl, double *hist, int hist_cap) {
+    wait_prior_grid();
     const int c = blockIdx.x;
     if (ctl[c].halt) return;
     const int2 ct = case_tiles[c];
@@ -54,12 +57,12 @@ __global__ void __launch_bounds__(256) kb_resid(const double *__restrict__ part,
 
 void enqueue_resid(const double *part, int nparts, Ctl *ctl, double *hist, int hist_cap,
                    cudaStream_t s) {
-    k_resid<<<1, 256, 0, s>>>(part, nparts, ctl, hist, hist_cap);
+    launch_chained(k_resid, 1, 256, s, part, nparts, ctl, hist, hist_cap);
 }
 
 void enqueue_batch_resid(const double *part, const int2 *case_tiles, int ncase, Ctl *ctl, double *hist,
                          int hist_cap, cudaStream_t s) {
-    kb_resid<<<ncase, 256, 0, s>>>(part, case_tiles, ctl, hist, hist_cap);
+    launch_chained(kb_resid, ncase, 256, s, part, case_tiles, ctl, hist, hist_cap);
 }
 
 }  // namespace e2d

@@ -242,7 +242,8 @@ struct e2d_solver {
     int hist_cap = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    cudaGraphExec_t gexec = nullptr;
+    cudaGraphExec_t gexec = nullptr;   // graph_iters iterations
+    cudaGraphExec_t gexec1 = nullptr;  // one iteration (remainders, short runs)
     int graph_iters = 8;
     int block = 128;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -251,6 +252,7 @@ struct e2d_solver {
 
     ~e2d_solver() {
         if (gexec) cudaGraphExecDestroy(gexec);
+        if (gexec1) cudaGraphExecDestroy(gexec1);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (own_stream && stream) cudaStreamDestroy(stream);
@@ -273,6 +275,11 @@ int pull_ctl(e2d_solver *s) {
     return E2D_OK;
 }
 
+void drop_graphs(e2d_solver *s) {
+    if (s->gexec) { cudaGraphExecDestroy(s->gexec); s->gexec = nullptr; }
+    if (s->gexec1) { cudaGraphExecDestroy(s->gexec1); s->gexec1 = nullptr; }
+}
+
 // The history buffer lives behind a pointer captured in the graph, so it is
 // sized once per growth and the graph is rebuilt when it moves.
 int ensure_hist(e2d_solver *s, int need) {
@@ -287,7 +294,7 @@ int ensure_hist(e2d_solver *s, int need) {
     }
     s->hist_dev = nh;
     s->hist_cap = cap;
-    if (s->gexec) { cudaGraphExecDestroy(s->gexec); s->gexec = nullptr; }
+    drop_graphs(s);
     return E2D_OK;
 }
 
@@ -297,21 +304,29 @@ template <typename T> void set_hist(SolverBase *b, double *h, int cap) {
     t->plan.hist_cap = cap;
 }
 
-int build_graph(e2d_solver *s) {
-    if (s->gexec) return E2D_OK;
-    if (s->prm.precision == E2D_FP64) set_hist<double>(s->impl.get(), s->hist_dev, s->hist_cap);
-    else set_hist<float>(s->impl.get(), s->hist_dev, s->hist_cap);
+// One CUDA graph of `iters` iterations on the solver's stream.
+int capture(e2d_solver *s, int iters, cudaGraphExec_t *out) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     int rc = E2D_OK;
-    for (int it = 0; it < s->graph_iters && rc == E2D_OK; it++) rc = s->impl->enqueue(s->stream);
+    for (int it = 0; it < iters && rc == E2D_OK; it++) rc = s->impl->enqueue(s->stream);
     cudaError_t e = cudaStreamEndCapture(s->stream, &g);
     if (rc) { if (g) cudaGraphDestroy(g); return rc; }
     if (e != cudaSuccess) { set_error(std::string("graph capture: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
-    e = cudaGraphInstantiate(&s->gexec, g, 0);
+    e = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
-    if (e != cudaSuccess) { s->gexec = nullptr; set_error(std::string("graph instantiate: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
+    if (e != cudaSuccess) { *out = nullptr; set_error(std::string("graph instantiate: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
     return E2D_OK;
+}
+
+int build_graph(e2d_solver *s) {
+    if (s->gexec && s->gexec1) return E2D_OK;
+    if (s->prm.precision == E2D_FP64) set_hist<double>(s->impl.get(), s->hist_dev, s->hist_cap);
+    else set_hist<float>(s->impl.get(), s->hist_dev, s->hist_cap);
+    drop_graphs(s);
+    int rc = capture(s, s->graph_iters, &s->gexec);
+    if (rc == E2D_OK) rc = capture(s, 1, &s->gexec1);
+    return rc;
 }
 
 // A stencil of the requested precision over the solver's mesh layout, bound
@@ -359,16 +374,19 @@ int run(e2d_solver *s, int n, bool check, double epsl, int poll_every) {
     c.check_epsl = check ? 1 : 0;
     c.epsl = epsl;
     if ((rc = push_ctl(s))) return rc;
-    const int launches = (n + s->graph_iters - 1) / s->graph_iters;
+    // whole graphs of graph_iters iterations, then single-iteration graphs for
+    // the remainder (no launches of iterations that would only find the halt flag)
+    const int full = n / s->graph_iters, rem = n % s->graph_iters;
     CK(cudaEventRecord(s->ev0, s->stream));
-    for (int k = 0; k < launches; k++) {
+    for (int k = 0; k < full; k++) {
         CK(cudaGraphLaunch(s->gexec, s->stream));
-        if (check && poll_every > 0 && (k + 1) % poll_every == 0 && k + 1 < launches) {
+        if (check && poll_every > 0 && (k + 1) % poll_every == 0 && (k + 1 < full || rem)) {
             if ((rc = pull_ctl(s))) return rc;
             if ((rc = sync_hist(s))) return rc;
             if (c.halt) break;
         }
     }
+    for (int k = 0; k < rem && !c.halt; k++) CK(cudaGraphLaunch(s->gexec1, s->stream));
     CK(cudaEventRecord(s->ev1, s->stream));
     if ((rc = pull_ctl(s))) return rc;
     float ms = 0.f;
@@ -556,7 +574,7 @@ int e2d_set_precision(e2d_solver *s, int32_t precision) {
     if ((rc = next->upload_state(w.data()))) return rc;
     s->impl = std::move(next);
     s->prm.precision = precision;
-    if (s->gexec) { cudaGraphExecDestroy(s->gexec); s->gexec = nullptr; }
+    drop_graphs(s);
     return E2D_OK;
 }
 
