@@ -1,8 +1,7 @@
 // mlp_kernels.cuh -- kernels of the coordinate MLP used for the learned warm
-// start: BF16 GEMMs on the tensor cores with FP32 accumulation
-// (mma.sync.m16n8k16, operands staged in shared memory and fed by ldmatrix),
-// fused bias / GELU epilogues, the small output layer, the MSE loss, and Adam.
-// No reference counterpart.
+// start: BF16 GEMMs on the fifth-generation tensor cores with FP32
+// accumulation in tensor memory, fused bias / GELU epilogues, the small
+// output layer, the MSE loss, and Adam.  No reference counterpart.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -14,9 +13,7 @@ namespace mlp {
 
 typedef __nv_bfloat16 bf16;
 
-constexpr int BM = 128, BN = 128, BK = 32;  // CTA tile
-constexpr int PADK = BK + 8;                 // row pitch (bf16) of [rows][BK] tiles
-constexpr int PADM = BM + 8;                 // row pitch (bf16) of [BK][rows] tiles
+constexpr int BM = 128, BN = 128;  // CTA tile of every GEMM
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 
@@ -25,175 +22,44 @@ __device__ __forceinline__ float gelu_grad(float x) {
     return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
 }
 
-__device__ __forceinline__ void ldsm_x4(uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3, const void *p) {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(a));
-}
-
-__device__ __forceinline__ void ldsm_x4_t(uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3, const void *p) {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(a));
-}
-
-__device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
 // Epilogue modes of the GEMM.
 enum Epi : int {
-    EPI_BIAS_GELU = 0,  // z = acc + bias[n]; out = gelu(z) (bf16), zout = z (bf16)
-    EPI_GELU_BWD = 1,   // out = acc * gelu'(zin[m,n])  (bf16): gradient at the previous pre-activation
+    EPI_BIAS_GELU = 0,  // z = acc + bias[n]; out = gelu(z), zout = z (bf16); outT = out transposed
+    EPI_GELU_BWD = 1,   // out = acc * gelu'(zin[m,n]) (bf16), outT = out transposed
     EPI_PARTIAL = 2,    // part[split][m][n] = acc (fp32): split-K partial of a weight gradient
 };
 
+// C[M][N] = A[M][K] * B[N][K]^T: both operands K-major (row-major with the
+// reduction index contiguous), which is why the forward pass also writes
+// transposed copies of the activations for the weight gradients.
 struct GemmArgs {
-    int M, N, K;           // C is M x N, reduction over K (per split: K / gridDim.z)
-    const bf16 *A;         // TA=false: [M][lda] ; TA=true: [K][lda]
+    int M, N, K;           // reduction over K (per split: K / gridDim.z, a multiple of 32)
+    const bf16 *A;         // [M][lda]
     int lda;
-    const bf16 *B;         // TB=false: [N][ldb] ; TB=true: [K][ldb]
+    const bf16 *B;         // [N][ldb]
     int ldb;
     const float *bias;     // EPI_BIAS_GELU
     const bf16 *zin;       // EPI_GELU_BWD: [M][ldc]
     bf16 *out;             // EPI_BIAS_GELU / EPI_GELU_BWD: [M][ldc]
     bf16 *zout;            // EPI_BIAS_GELU: [M][ldc]
+    bf16 *outT;            // optional [N][ldt]: out transposed
     float *part;           // EPI_PARTIAL: [splits][M][N]
-    int ldc;
-    int *flag;             // tensor-core kernel: set to 1 if a wait timed out
+    int ldc, ldt;
+    int *flag;             // set to 1 if a wait timed out
 };
 
-// C = opA(A) * opB(B): opA(A)[m][k] = TA ? A[k][m] : A[m][k];
-//                     opB(B)[k][n] = TB ? B[k][n] : B[n][k].
-// 256 threads = 8 warps as 2 (M) x 4 (N); each warp computes 64 x 32.  M and N
-// may be ragged (zero-filled tiles, guarded stores); K per split must be a
-// multiple of BK.
-template <bool TA, bool TB, int EPI>
-__global__ void __launch_bounds__(256) k_gemm(GemmArgs g) {
-    __shared__ __align__(16) bf16 As[TA ? BK * PADM : BM * PADK];
-    __shared__ __align__(16) bf16 Bs[TB ? BK * PADM : BN * PADK];
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-    const int kper = g.K / gridDim.z, kbeg = blockIdx.z * kper, kend = kbeg + kper;
-    const int wm = (warp >> 2) * 64, wn = (warp & 3) * 32;
-    float acc[4][4][4];
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-#pragma unroll
-            for (int q = 0; q < 4; q++) acc[i][j][q] = 0.f;
-    for (int k0 = kbeg; k0 < kend; k0 += BK) {
-        // global -> shared, 16-byte chunks; out-of-range rows / columns are zero
-#pragma unroll
-        for (int it = 0; it < 2; it++) {
-            const int c = tid + it * 256;  // 512 chunks of 8 bf16 per operand tile
-            uint4 va = make_uint4(0, 0, 0, 0), vb = make_uint4(0, 0, 0, 0);
-            if (!TA) {  // A[m][k]: 128 rows x 4 chunks
-                const int r = c >> 2, kc = (c & 3) * 8;
-                if (m0 + r < g.M) va = *(const uint4 *)(g.A + (size_t)(m0 + r) * g.lda + k0 + kc);
-                *(uint4 *)(As + r * PADK + kc) = va;
-            } else {    // A[k][m]: 32 rows x 16 chunks
-                const int r = c >> 4, mc = (c & 15) * 8;
-                if (m0 + mc < g.M) va = *(const uint4 *)(g.A + (size_t)(k0 + r) * g.lda + m0 + mc);
-                *(uint4 *)(As + r * PADM + mc) = va;
-            }
-            if (!TB) {  // B[n][k]
-                const int r = c >> 2, kc = (c & 3) * 8;
-                if (n0 + r < g.N) vb = *(const uint4 *)(g.B + (size_t)(n0 + r) * g.ldb + k0 + kc);
-                *(uint4 *)(Bs + r * PADK + kc) = vb;
-            } else {    // B[k][n]
-                const int r = c >> 4, nc = (c & 15) * 8;
-                if (n0 + nc < g.N) vb = *(const uint4 *)(g.B + (size_t)(k0 + r) * g.ldb + n0 + nc);
-                *(uint4 *)(Bs + r * PADM + nc) = vb;
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < BK; kk += 16) {
-            uint32_t af[4][4], bfr[4][2];
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                const int mb = wm + i * 16;
-                if (!TA) {
-                    const bf16 *p = As + (mb + (lane & 15)) * PADK + kk + (lane >> 4) * 8;
-                    ldsm_x4(af[i][0], af[i][1], af[i][2], af[i][3], p);
-                } else {
-                    // matrices: (m0-7,k0-7) (m8-15,k0-7) (m0-7,k8-15) (m8-15,k8-15), stored [k][m]
-                    const int krow = kk + (lane & 7) + ((lane >> 4) << 3);
-                    const int mcol = mb + ((lane >> 3) & 1) * 8;
-                    ldsm_x4_t(af[i][0], af[i][1], af[i][2], af[i][3], As + krow * PADM + mcol);
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < 4; j += 2) {
-                const int nb = wn + j * 8;
-                uint32_t r0, r1, r2, r3;
-                if (!TB) {
-                    // matrices: (n0-7,k0-7) (n0-7,k8-15) (n8-15,k0-7) (n8-15,k8-15), stored [n][k]
-                    const int nrow = nb + (lane & 7) + ((lane >> 4) << 3);
-                    const int kcol = kk + ((lane >> 3) & 1) * 8;
-                    ldsm_x4(r0, r1, r2, r3, Bs + nrow * PADK + kcol);
-                } else {
-                    // same four matrices, stored [k][n]
-                    const int krow = kk + (lane & 7) + ((lane >> 3) & 1) * 8;
-                    const int ncol = nb + (lane >> 4) * 8;
-                    ldsm_x4_t(r0, r1, r2, r3, Bs + krow * PADM + ncol);
-                }
-                bfr[j][0] = r0; bfr[j][1] = r1; bfr[j + 1][0] = r2; bfr[j + 1][1] = r3;
-            }
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++) mma_bf16(acc[i][j], af[i], bfr[j][0], bfr[j][1]);
-        }
-        __syncthreads();
-    }
-    // epilogue: c0,c1 at (row g, cols 2t,2t+1), c2,c3 at row g+8
-    const int gr = lane >> 2, tc = (lane & 3) * 2;
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int m = m0 + wm + i * 16 + gr + h * 8;
-                const int n = n0 + wn + j * 8 + tc;
-                if (m >= g.M || n >= g.N) continue;
-                const float v0 = acc[i][j][2 * h], v1 = acc[i][j][2 * h + 1];
-                if (EPI == EPI_BIAS_GELU) {
-                    const float z0 = v0 + g.bias[n], z1 = v1 + g.bias[n + 1];
-                    *(__nv_bfloat162 *)(g.zout + (size_t)m * g.ldc + n) = __floats2bfloat162_rn(z0, z1);
-                    *(__nv_bfloat162 *)(g.out + (size_t)m * g.ldc + n) = __floats2bfloat162_rn(gelu(z0), gelu(z1));
-                } else if (EPI == EPI_GELU_BWD) {
-                    const __nv_bfloat162 z = *(const __nv_bfloat162 *)(g.zin + (size_t)m * g.ldc + n);
-                    const float d0 = v0 * gelu_grad(__bfloat162float(z.x));
-                    const float d1 = v1 * gelu_grad(__bfloat162float(z.y));
-                    *(__nv_bfloat162 *)(g.out + (size_t)m * g.ldc + n) = __floats2bfloat162_rn(d0, d1);
-                } else {
-                    float *p = g.part + ((size_t)blockIdx.z * g.M + m) * g.N + n;
-                    p[0] = v0;
-                    p[1] = v1;
-                }
-            }
-}
-
 // ---------------------------------------------------------------------------
-// The same GEMM on the fifth-generation tensor cores: tcgen05.mma (BF16 in,
-// FP32 accumulate in tensor memory) issued by one thread, operands staged by
-// all threads into shared memory in the canonical no-swizzle K-major layout
-// (8 x 8 core matrices of 128 bytes; a transposed operand is transposed while
-// it is staged), a four-deep ring of stages released by tcgen05.commit on
-// mbarriers, and the epilogue read back from tensor memory with tcgen05.ld.
-// Every wait is bounded: on a timeout the CTA sets *g.flag, skips the
-// epilogue and still frees its tensor memory.
+// GEMM on tcgen05: one thread issues tcgen05.mma (kind::f16, M = N = 128,
+// K = 16) into a 128-column FP32 accumulator in tensor memory; operands are
+// copied global -> shared with cp.async straight into the canonical
+// no-swizzle K-major layout (8 x 8 core matrices of 128 bytes), three stages
+// ahead of the MMAs through a four-buffer ring; tcgen05.commit on a per-buffer
+// mbarrier releases a buffer for refill; the epilogue reads the accumulator
+// back with tcgen05.ld.  Every wait is bounded: on a timeout the CTA sets
+// *g.flag, skips the epilogue and still frees its tensor memory.
 namespace tc {
 constexpr int BK = 32;                      // K per stage (two MMAs of K = 16)
-constexpr int NST = 4;                      // stages in the ring
+constexpr int NST = 4;                      // buffers in the ring
 constexpr int TILE = 128 * BK * 2;          // bytes of one 128 x BK operand tile
 constexpr int SMEM = 2 * NST * TILE;        // dynamic shared memory per CTA
 constexpr uint32_t TMEM_COLS = 128;         // FP32 accumulator columns (N = 128)
@@ -204,9 +70,7 @@ constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 
 constexpr uint32_t LBO = 128;               // next core matrix along K
 constexpr uint32_t SBO = (BK / 8) * 128;    // next core matrix along M / N
 
-__device__ __forceinline__ int cm_off(int r, int k) {
-    return ((r >> 3) * (BK / 8) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
-}
+__device__ __forceinline__ int cm_off(int r, int k) { return ((r >> 3) * (BK / 8) + (k >> 3)) * 128 + (r & 7) * 16; }
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -227,39 +91,31 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-// rows [row0, row0 + 128) x k [k0, k0 + BK) of op(src) into tile (core-matrix layout);
-// T: src is [k][ld] (rows contiguous), else [row][ld] (k contiguous).  Rows at
-// or past nrows (a multiple of 8) are zero.
-template <bool T>
+// rows [row0, row0 + 128) x k [k0, k0 + BK) of src[row][ld] into tile with
+// cp.async; rows at or past nrows are zero-filled (no bytes read).
 __device__ __forceinline__ void stage(unsigned char *tile, const bf16 *__restrict__ src, int ld, int row0, int nrows,
                                       int k0) {
 #pragma unroll
     for (int it = 0; it < 2; it++) {
         const int c = threadIdx.x + it * 256;
-        if (!T) {
-            const int r = c >> 2, kc = (c & 3) * 8;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (row0 + r < nrows) v = *(const uint4 *)(src + (size_t)(row0 + r) * ld + k0 + kc);
-            *(uint4 *)(tile + cm_off(r, kc)) = v;
-        } else {
-            const int kr = c >> 4, rc = (c & 15) * 8;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (row0 + rc < nrows) v = *(const uint4 *)(src + (size_t)(k0 + kr) * ld + row0 + rc);
-            const unsigned short *e = (const unsigned short *)&v;
-#pragma unroll
-            for (int j = 0; j < 8; j++) *(unsigned short *)(tile + cm_off(rc + j, kr)) = e[j];
-        }
+        const int r = c >> 2, kc = (c & 3) * 8;
+        const bool in = row0 + r < nrows;
+        const bf16 *g = in ? src + (size_t)(row0 + r) * ld + k0 + kc : src;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n"
+                     :: "r"(smem_u32(tile + cm_off(r, kc))), "l"(g), "r"(in ? 16 : 0) : "memory");
     }
 }
+
+__device__ __forceinline__ void commit_group() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 }  // namespace tc
 
-template <bool TA, bool TB, int EPI>
+template <int EPI>
 __global__ void __launch_bounds__(256, 1) k_gemm_tc(GemmArgs g) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __shared__ __align__(8) uint64_t bars[tc::NST];
     __shared__ uint32_t tmem_sh;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int m0 = blockIdx.y * 128, n0 = blockIdx.x * 128;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
     const int kper = g.K / gridDim.z, kbeg = blockIdx.z * kper, nst = kper / tc::BK;
     unsigned char *As = tc_smem, *Bs = tc_smem + tc::NST * tc::TILE;
     if (warp == 0) {
@@ -274,16 +130,18 @@ __global__ void __launch_bounds__(256, 1) k_gemm_tc(GemmArgs g) {
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n");
     const uint32_t tmem = tmem_sh;
+    // prologue: stages 0 .. NST-2 in flight
+    for (int s = 0; s < tc::NST - 1; s++) {
+        if (s < nst) {
+            tc::stage(As + s * tc::TILE, g.A, g.lda, m0, g.M, kbeg + s * tc::BK);
+            tc::stage(Bs + s * tc::TILE, g.B, g.ldb, n0, g.N, kbeg + s * tc::BK);
+        }
+        tc::commit_group();
+    }
     bool ok = true;
     for (int s = 0; s < nst; s++) {
         const int b = s % tc::NST;
-        if (s >= tc::NST) {  // the MMAs that read this buffer last must be done
-            const bool w = tc::mbar_wait(tc::smem_u32(&bars[b]), ((s - tc::NST) / tc::NST) & 1);
-            if (__syncthreads_or(!w)) { ok = false; break; }
-        }
-        const int k0 = kbeg + s * tc::BK;
-        tc::stage<TA>(As + b * tc::TILE, g.A, g.lda, m0, g.M, k0);
-        tc::stage<TB>(Bs + b * tc::TILE, g.B, g.ldb, n0, g.N, k0);
+        asm volatile("cp.async.wait_group %0;\n" :: "n"(tc::NST - 2) : "memory");  // stage s has landed
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         __syncthreads();
         if (tid == 0) {
@@ -300,7 +158,19 @@ __global__ void __launch_bounds__(256, 1) k_gemm_tc(GemmArgs g) {
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n"
                          :: "r"(tc::smem_u32(&bars[b])));
         }
+        // refill the buffer of stage s - 1 with stage s + NST - 1 once its MMAs are done
+        const int sn = s + tc::NST - 1;
+        if (sn < nst) {
+            if (s >= 1) {
+                const bool w = tc::mbar_wait(tc::smem_u32(&bars[(s - 1) % tc::NST]), ((s - 1) / tc::NST) & 1);
+                if (__syncthreads_or(!w)) { ok = false; break; }
+            }
+            tc::stage(As + (sn % tc::NST) * tc::TILE, g.A, g.lda, m0, g.M, kbeg + sn * tc::BK);
+            tc::stage(Bs + (sn % tc::NST) * tc::TILE, g.B, g.ldb, n0, g.N, kbeg + sn * tc::BK);
+        }
+        tc::commit_group();
     }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     if (ok && nst > 0) {  // the last commit covers every MMA of the CTA
         const int s = nst - 1;
         const bool w = tc::mbar_wait(tc::smem_u32(&bars[s % tc::NST]), (s / tc::NST) & 1);
@@ -324,8 +194,17 @@ __global__ void __launch_bounds__(256, 1) k_gemm_tc(GemmArgs g) {
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
             const int n = n0 + cb + ch * 16;
             if (m >= g.M || n >= g.N) continue;
+            if (EPI == EPI_PARTIAL) {
+                float4 *p = (float4 *)(g.part + ((size_t)blockIdx.z * g.M + m) * g.N + n);
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    p[j] = make_float4(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1]),
+                                       __uint_as_float(v[4 * j + 2]), __uint_as_float(v[4 * j + 3]));
+                continue;
+            }
+            __align__(16) __nv_bfloat162 o2[8];
             if (EPI == EPI_BIAS_GELU) {
-                __align__(16) __nv_bfloat162 z2[8], o2[8];
+                __align__(16) __nv_bfloat162 z2[8];
 #pragma unroll
                 for (int j = 0; j < 8; j++) {
                     const float z0 = __uint_as_float(v[2 * j]) + g.bias[n + 2 * j];
@@ -333,32 +212,47 @@ __global__ void __launch_bounds__(256, 1) k_gemm_tc(GemmArgs g) {
                     z2[j] = __floats2bfloat162_rn(z0, z1);
                     o2[j] = __floats2bfloat162_rn(gelu(z0), gelu(z1));
                 }
-                uint4 *zo = (uint4 *)(g.zout + (size_t)m * g.ldc + n), *oo = (uint4 *)(g.out + (size_t)m * g.ldc + n);
+                uint4 *zo = (uint4 *)(g.zout + (size_t)m * g.ldc + n);
                 zo[0] = ((const uint4 *)z2)[0]; zo[1] = ((const uint4 *)z2)[1];
-                oo[0] = ((const uint4 *)o2)[0]; oo[1] = ((const uint4 *)o2)[1];
-            } else if (EPI == EPI_GELU_BWD) {
+            } else {
                 const uint4 *zi = (const uint4 *)(g.zin + (size_t)m * g.ldc + n);
                 __align__(16) uint4 zz[2] = {zi[0], zi[1]};
                 const __nv_bfloat162 *z2 = (const __nv_bfloat162 *)zz;
-                __align__(16) __nv_bfloat162 o2[8];
 #pragma unroll
                 for (int j = 0; j < 8; j++)
                     o2[j] = __floats2bfloat162_rn(__uint_as_float(v[2 * j]) * gelu_grad(__bfloat162float(z2[j].x)),
                                                   __uint_as_float(v[2 * j + 1]) * gelu_grad(__bfloat162float(z2[j].y)));
-                uint4 *oo = (uint4 *)(g.out + (size_t)m * g.ldc + n);
-                oo[0] = ((const uint4 *)o2)[0]; oo[1] = ((const uint4 *)o2)[1];
-            } else {
-                float4 *p = (float4 *)(g.part + ((size_t)blockIdx.z * g.M + m) * g.N + n);
+            }
+            uint4 *oo = (uint4 *)(g.out + (size_t)m * g.ldc + n);
+            oo[0] = ((const uint4 *)o2)[0]; oo[1] = ((const uint4 *)o2)[1];
+            if (g.outT) {  // lanes hold consecutive m: each column is written as 64 contiguous bytes per warp
 #pragma unroll
-                for (int j = 0; j < 4; j++)
-                    p[j] = make_float4(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1]),
-                                       __uint_as_float(v[4 * j + 2]), __uint_as_float(v[4 * j + 3]));
+                for (int j = 0; j < 8; j++) {
+                    g.outT[(size_t)(n + 2 * j) * g.ldt + m] = o2[j].x;
+                    g.outT[(size_t)(n + 2 * j + 1) * g.ldt + m] = o2[j].y;
+                }
             }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(tmem), "r"(tc::TMEM_COLS));
+}
+
+// [rows][cols] -> [cols][rows] (bf16), 32 x 32 tiles through shared memory.
+__global__ void __launch_bounds__(256) k_transpose(int rows, int cols, const bf16 *__restrict__ a,
+                                                   bf16 *__restrict__ t) {
+    __shared__ bf16 tile[32][33];
+    const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+    for (int k = threadIdx.x; k < 1024; k += 256) {
+        const int r = k >> 5, c = k & 31;
+        if (r0 + r < rows && c0 + c < cols) tile[r][c] = a[(size_t)(r0 + r) * cols + c0 + c];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 1024; k += 256) {
+        const int c = k >> 5, r = k & 31;
+        if (r0 + r < rows && c0 + c < cols) t[(size_t)(c0 + c) * rows + r0 + r] = tile[r][c];
+    }
 }
 
 // Output layer (256 -> NOUT) on the CUDA cores: y[b][o] = h[b] . W[o] + bias[o]
@@ -413,7 +307,8 @@ __global__ void __launch_bounds__(256) k_out_fwd_loss(int B, const bf16 *__restr
 // Output layer backward: dz[b][k] = (sum_o dy[b][o] W[o][k]) * gelu'(z[b][k]) (bf16).
 template <int H, int NOUT>
 __global__ void __launch_bounds__(256) k_out_bwd_data(int B, const float *__restrict__ dy, const float *__restrict__ W,
-                                                      const bf16 *__restrict__ z, bf16 *__restrict__ dz) {
+                                                      const bf16 *__restrict__ z, bf16 *__restrict__ dz,
+                                                      bf16 *__restrict__ dzT) {
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;  // one (b, pair of k)
     if (idx >= (size_t)B * (H / 2)) return;
     const int b = (int)(idx / (H / 2)), k = (int)(idx % (H / 2)) * 2;
@@ -425,8 +320,11 @@ __global__ void __launch_bounds__(256) k_out_bwd_data(int B, const float *__rest
         s1 += d * W[o * H + k + 1];
     }
     const __nv_bfloat162 zz = *(const __nv_bfloat162 *)(z + (size_t)b * H + k);
-    *(__nv_bfloat162 *)(dz + (size_t)b * H + k) =
+    const __nv_bfloat162 d =
         __floats2bfloat162_rn(s0 * gelu_grad(__bfloat162float(zz.x)), s1 * gelu_grad(__bfloat162float(zz.y)));
+    *(__nv_bfloat162 *)(dz + (size_t)b * H + k) = d;
+    dzT[(size_t)k * B + b] = d.x;
+    dzT[(size_t)(k + 1) * B + b] = d.y;
 }
 
 // Split partials of the output layer's weight gradient: part[blk][o][k] =
@@ -463,28 +361,6 @@ __global__ void __launch_bounds__(256) k_colsum(int B, int N, int rows_per_block
         for (int b = b0; b < b1; b++) s += __bfloat162float(d[(size_t)b * N + n]);
         part[(size_t)blockIdx.x * N + n] = s;
     }
-}
-
-// Adam on `count` parameters whose gradient is the sum of `nparts` partials
-// (stride `pstride`), summed in a fixed order.  w32 master weights; wbf (may
-// be null) receives the bf16 copy used by the GEMMs.
-__global__ void __launch_bounds__(256) k_adam(int count, const float *__restrict__ part, int nparts, size_t pstride,
-                                              float *__restrict__ w32, bf16 *__restrict__ wbf, float *__restrict__ m,
-                                              float *__restrict__ v, float lr, float beta1, float beta2, float eps,
-                                              float bc1, float bc2, float *__restrict__ grad_out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
-    float g = 0.f;
-    for (int p = 0; p < nparts; p++) g += part[(size_t)p * pstride + i];
-    if (grad_out) grad_out[i] = g;
-    if (lr == 0.f) return;  // gradient only
-    const float mi = beta1 * m[i] + (1.f - beta1) * g;
-    const float vi = beta2 * v[i] + (1.f - beta2) * g * g;
-    m[i] = mi;
-    v[i] = vi;
-    const float w = w32[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
-    w32[i] = w;
-    if (wbf) wbf[i] = __float2bfloat16_rn(w);
 }
 
 // Random mini-batch gather: rows idx(step, j) of the training set, with the
