@@ -125,6 +125,14 @@ def measured_peak_hbm() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
+def measured_peak_bf16() -> tuple[float, str]:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
 def max_over_ranks(t: float, dist, device: str) -> float:
     """The slowest rank's time (the job's time); t itself without a process group."""
     if dist is None:
@@ -388,6 +396,42 @@ def run_batch64(args):
     print(json.dumps(line), flush=True)
 
 
+def run_mlp(args):
+    """Training steps of the warm-start MLP (22 -> 5 x 256 GELU -> 4, batch
+    65536 on the BF16 tensor cores, FP32 accumulate): gather, forward, loss,
+    backward and Adam of one step are one CUDA graph.  FLOPs per step: 3 x the
+    forward GEMM FLOPs (forward, data gradient, weight gradient)."""
+    import numpy as np
+    import torch
+    import gpueularsolver2d_gb300 as e2d
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    net = e2d.MLP(nhidden=5, batch=65536, seed=3)
+    rng = np.random.default_rng(0)
+    n = 32768 * 64
+    x = np.zeros((n, 32), np.float32)
+    x[:, :22] = rng.uniform(-1, 1, (n, 22))
+    t = rng.normal(size=(n, 4)).astype(np.float32)
+    net.set_data(x, t)
+    net.train(args.warmup, record_loss=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    net.train(args.steps, record_loss=False)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / args.steps
+    flops = 3 * 2 * 65536 * (32 * 256 + 4 * 256 * 256 + 256 * 4)
+    peak, kind = measured_peak_bf16()
+    tf = flops / dt / 1e12
+    line = {"metric": "MLP training steps/s (warm-start network, batch 65536)", "value": 1.0 / dt, "unit": "steps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+            "data": "synthetic (uniform features, normal targets)",
+            "config": {"workload": "MLP 32 -> 5 x 256 GELU -> 4, batch 65536, Adam"},
+            "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
+                         "peak_source": f"{kind} bf16_tflops (MEASURED_PEAKS.json)", "traffic": None},
+            "gpu_launches": None}
+    print(json.dumps(line), flush=True)
+
+
 def args_sweeps_count(params) -> int:
     return max(0, params.irs_sweeps - 1)
 
@@ -410,7 +454,7 @@ def main():
     ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch64"], default="large")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch64", "mlp"], default="large")
     ap.add_argument("--fp64", action="store_true")
     ap.add_argument("--block", type=int, default=0, help="threads per CTA (0: library default)")
     ap.add_argument("--ordering", choices=sorted(ORDERINGS), default="morton", help="cell order in device memory")
@@ -420,7 +464,12 @@ def main():
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    if args.workload == "batch64":
+    if args.workload == "mlp":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned warm start"}))
+        elif rank == 0:
+            run_mlp(args)
+    elif args.workload == "batch64":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference solves one case per run; "
                               "the batched sweep has no reference arm"}))
