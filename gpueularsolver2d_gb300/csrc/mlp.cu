@@ -250,9 +250,9 @@ void backward(e2d_mlp *m, cudaStream_t s, float lr, bool want_grad) {
     };
     // output layer: weight / bias partials, then the gradient at the last pre-activation
     Tensor &Wo = m->W[L], &bo = m->b[L];
-    k_out_bwd_weight<H, NOUT><<<kSplits, 256, 0, s>>>(B, rows, m->dy, m->Hh[L - 1], m->bpart);
-    k_out_bwd_data<H, NOUT><<<(B * (H / 2) + 255) / 256, 256, 0, s>>>(B, m->dy, Wo.w32, m->Z[L - 1], m->dz[0],
-                                                                       m->dzT[0]);
+    k_out_bwd_weight<H, NOUT><<<dim3(H / 32, kSplits), 256, 0, s>>>(B, rows, m->dy, m->Hh[L - 1], m->bpart);
+    k_out_bwd_data<H, NOUT><<<(B * (H / 2) + 255) / 256, 256, 0, s>>>(B, m->dy, Wo.w32, m->Z[L - 1], m->dz[0]);
+    transpose(m->dz[0], m->dzT[0], B, H, s);
     const size_t ostride = NOUT * H + NOUT;
     float *gbo = gslot(bo);
     float *gWo = gslot(Wo);
@@ -271,7 +271,7 @@ void backward(e2d_mlp *m, cudaStream_t s, float lr, bool want_grad) {
         gw.B = hinT; gw.ldb = B;
         gw.part = m->part;
         gemm<EPI_PARTIAL>(m, gw, dim3((kin + BN - 1) / BN, H / BM, kSplits), s);
-        k_colsum<<<kSplits, 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart);
+        k_colsum<<<dim3(H / 32, kSplits), 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart);
         // gradient at the previous pre-activation (before this layer's weights change)
         if (l > 0) {
             GemmArgs gd{};

@@ -52,14 +52,14 @@ struct GemmArgs {
 // GEMM on tcgen05: one thread issues tcgen05.mma (kind::f16, M = N = 128,
 // K = 16) into a 128-column FP32 accumulator in tensor memory; operands are
 // copied global -> shared with cp.async straight into the canonical
-// no-swizzle K-major layout (8 x 8 core matrices of 128 bytes), three stages
-// ahead of the MMAs through a four-buffer ring; tcgen05.commit on a per-buffer
+// no-swizzle K-major layout (8 x 8 core matrices of 128 bytes), two stages
+// ahead of the MMAs through a three-buffer ring; tcgen05.commit on a per-buffer
 // mbarrier releases a buffer for refill; the epilogue reads the accumulator
 // back with tcgen05.ld.  Every wait is bounded: on a timeout the CTA sets
 // *g.flag, skips the epilogue and still frees its tensor memory.
 namespace tc {
 constexpr int BK = 32;                      // K per stage (two MMAs of K = 16)
-constexpr int NST = 4;                      // buffers in the ring
+constexpr int NST = 3;                      // buffers in the ring
 constexpr int TILE = 128 * BK * 2;          // bytes of one 128 x BK operand tile
 constexpr int SMEM = 2 * NST * TILE;        // dynamic shared memory per CTA
 constexpr uint32_t TMEM_COLS = 128;         // FP32 accumulator columns (N = 128)
@@ -109,8 +109,12 @@ __device__ __forceinline__ void stage(unsigned char *tile, const bf16 *__restric
 __device__ __forceinline__ void commit_group() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 }  // namespace tc
 
+// resident CTAs per SM the register budget is sized for (the GELU-backward
+// epilogue needs more registers than the others)
+template <int EPI> struct GemmOcc { static constexpr int value = EPI == EPI_GELU_BWD ? 2 : 3; };
+
 template <int EPI>
-__global__ void __launch_bounds__(256, 1) k_gemm_tc(GemmArgs g) {
+__global__ void __launch_bounds__(256, GemmOcc<EPI>::value) k_gemm_tc(GemmArgs g) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __shared__ __align__(8) uint64_t bars[tc::NST];
     __shared__ uint32_t tmem_sh;
@@ -307,8 +311,7 @@ __global__ void __launch_bounds__(256) k_out_fwd_loss(int B, const bf16 *__restr
 // Output layer backward: dz[b][k] = (sum_o dy[b][o] W[o][k]) * gelu'(z[b][k]) (bf16).
 template <int H, int NOUT>
 __global__ void __launch_bounds__(256) k_out_bwd_data(int B, const float *__restrict__ dy, const float *__restrict__ W,
-                                                      const bf16 *__restrict__ z, bf16 *__restrict__ dz,
-                                                      bf16 *__restrict__ dzT) {
+                                                      const bf16 *__restrict__ z, bf16 *__restrict__ dz) {
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;  // one (b, pair of k)
     if (idx >= (size_t)B * (H / 2)) return;
     const int b = (int)(idx / (H / 2)), k = (int)(idx % (H / 2)) * 2;
@@ -323,43 +326,67 @@ __global__ void __launch_bounds__(256) k_out_bwd_data(int B, const float *__rest
     const __nv_bfloat162 d =
         __floats2bfloat162_rn(s0 * gelu_grad(__bfloat162float(zz.x)), s1 * gelu_grad(__bfloat162float(zz.y)));
     *(__nv_bfloat162 *)(dz + (size_t)b * H + k) = d;
-    dzT[(size_t)k * B + b] = d.x;
-    dzT[(size_t)(k + 1) * B + b] = d.y;
 }
 
-// Split partials of the output layer's weight gradient: part[blk][o][k] =
-// sum over the block's rows of dy[b][o] h[b][k]; part[blk][NOUT*H + o] = sum dy.
+// Split partials of the output layer's weight gradient: part[split][o][k] =
+// sum over the split's rows of dy[b][o] h[b][k]; part[split][NOUT*H + o] =
+// sum dy.  Grid (H / 32, splits): lane = column k, the block's 8 warps take
+// every 8th row, then the warps are added in a fixed order (deterministic).
 template <int H, int NOUT>
-__global__ void __launch_bounds__(256) k_out_bwd_weight(int B, int rows_per_block, const float *__restrict__ dy,
+__global__ void __launch_bounds__(256) k_out_bwd_weight(int B, int rows_per_split, const float *__restrict__ dy,
                                                         const bf16 *__restrict__ h, float *__restrict__ part) {
-    const int b0 = blockIdx.x * rows_per_block, b1 = min(B, b0 + rows_per_block);
-    for (int k = threadIdx.x; k < H; k += blockDim.x) {
-        float s[NOUT];
+    __shared__ float red[8][NOUT][32];
+    __shared__ float dred[8][NOUT];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int k = blockIdx.x * 32 + lane;
+    const int b0 = blockIdx.y * rows_per_split, b1 = min(B, b0 + rows_per_split);
+    float s[NOUT], ds[NOUT];
 #pragma unroll
-        for (int o = 0; o < NOUT; o++) s[o] = 0.f;
-        for (int b = b0; b < b1; b++) {
-            const float x = __bfloat162float(h[(size_t)b * H + k]);
+    for (int o = 0; o < NOUT; o++) s[o] = ds[o] = 0.f;
+    for (int b = b0 + warp; b < b1; b += 8) {
+        const float x = __bfloat162float(h[(size_t)b * H + k]);
 #pragma unroll
-            for (int o = 0; o < NOUT; o++) s[o] += dy[(size_t)b * NOUT + o] * x;
+        for (int o = 0; o < NOUT; o++) {
+            const float d = dy[(size_t)b * NOUT + o];
+            s[o] += d * x;
+            ds[o] += d;
         }
-#pragma unroll
-        for (int o = 0; o < NOUT; o++) part[(size_t)blockIdx.x * (NOUT * H + NOUT) + o * H + k] = s[o];
     }
-    if (threadIdx.x < NOUT) {
-        float s = 0.f;
-        for (int b = b0; b < b1; b++) s += dy[(size_t)b * NOUT + threadIdx.x];
-        part[(size_t)blockIdx.x * (NOUT * H + NOUT) + NOUT * H + threadIdx.x] = s;
+#pragma unroll
+    for (int o = 0; o < NOUT; o++) red[warp][o][lane] = s[o];
+    if (lane == 0)
+#pragma unroll
+        for (int o = 0; o < NOUT; o++) dred[warp][o] = ds[o];
+    __syncthreads();
+    float *p = part + (size_t)blockIdx.y * (NOUT * H + NOUT);
+    if (warp < NOUT) {
+        float t = 0.f;
+        for (int w = 0; w < 8; w++) t += red[w][warp][lane];
+        p[warp * H + k] = t;
+    }
+    if (blockIdx.x == 0 && threadIdx.x < NOUT) {
+        float t = 0.f;
+        for (int w = 0; w < 8; w++) t += dred[w][threadIdx.x];
+        p[NOUT * H + threadIdx.x] = t;
     }
 }
 
-// Column sums of a bf16 [B][N] gradient over row blocks: part[blk][n].
-__global__ void __launch_bounds__(256) k_colsum(int B, int N, int rows_per_block, const bf16 *__restrict__ d,
+// Column sums of a bf16 [B][N] gradient over row splits: part[split][n].
+// Grid (N / 32, splits), same shape as k_out_bwd_weight.
+__global__ void __launch_bounds__(256) k_colsum(int B, int N, int rows_per_split, const bf16 *__restrict__ d,
                                                 float *__restrict__ part) {
-    const int b0 = blockIdx.x * rows_per_block, b1 = min(B, b0 + rows_per_block);
-    for (int n = threadIdx.x; n < N; n += blockDim.x) {
-        float s = 0.f;
-        for (int b = b0; b < b1; b++) s += __bfloat162float(d[(size_t)b * N + n]);
-        part[(size_t)blockIdx.x * N + n] = s;
+    __shared__ float red[8][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = blockIdx.x * 32 + lane;
+    const int b0 = blockIdx.y * rows_per_split, b1 = min(B, b0 + rows_per_split);
+    float s = 0.f;
+    for (int b = b0 + warp; b < b1; b += 8) s += __bfloat162float(d[(size_t)b * N + n]);
+    red[warp][lane] = s;
+    __syncthreads();
+    if (warp == 0) {
+        float t = 0.f;
+        for (int w = 0; w < 8; w++) t += red[w][lane];
+        part[(size_t)blockIdx.y * N + n] = t;
     }
 }
 
