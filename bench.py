@@ -326,8 +326,11 @@ def run_gpu(args, rank: int, world: int):
         del solver
         torch.cuda.synchronize()
         rate, k, dt, th = cpu_port_rate(wl, 2, mesh=mesh)
+        rate1, k1, dt1, _ = cpu_port_rate(wl, 1, threads=1, mesh=mesh)
         cpu = {"value": rate, "unit": "cell-stage/s", "cores": th, "kind": "port",
-               "sample": f"{k} iterations of the full {ncell}-cell workload on {th} threads ({dt:.1f} s)"}
+               "sample": f"{k} iterations of the full {ncell}-cell workload on {th} threads ({dt:.1f} s)",
+               "single_thread_value": rate1,
+               "single_thread_sample": f"{k1} iteration on 1 thread ({dt1:.1f} s)"}
     if rank == 0:
         line = {
             "metric": "cell-stage updates/s", "value": value, "unit": "cell-stage/s", "n_gpus": world,
