@@ -373,8 +373,9 @@ def run_batch64(args):
                                  ordering=e2d.E2D_ORDER_MORTON, maxstep=args.steps + args.warmup + 64)
               for m, a in zip(mach, alpha)]
     cells = sum(2 * int(a) * int(b) for a, b in zip(ni, nj))
-    b = e2d.Batch(meshes, params)
-    block, grid, ms_tune = b.autotune(None, iters=16)
+    b = e2d.Batch.tuned(meshes, params, None, iters=16)
+    block, grid = b.launch()
+    order_name = {e2d.E2D_ORDER_MORTON: "Morton", e2d.E2D_ORDER_RCM: "RCM", e2d.E2D_ORDER_FILE: "file"}[b.ordering]
     b.step(args.warmup)
     b.step(args.steps)
     t_batch = b.last_device_ms() / 1e3
@@ -393,7 +394,8 @@ def run_batch64(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded NACA0012 O-grids)",
             "config": {"workload": "64 cases, O-grids {64..512}x{16..128} (seed 2), M U[0.3,0.85], a U[-2,4]",
-                       "cells": cells, "stages": stages, "autotuned_block": block, "autotuned_grid": grid},
+                       "cells": cells, "stages": stages, "autotuned_block": block, "autotuned_grid": grid,
+                       "autotuned_ordering": order_name},
             "sequential_value": seq, "speedup_vs_sequential": agg / seq,
             "gpu_launches": b.launches_per_iteration() * args.steps}
     print(json.dumps(line), flush=True)

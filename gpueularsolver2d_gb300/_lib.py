@@ -102,6 +102,8 @@ SIGNATURES = {
     "e2d_batch_set_launch": (_I, [_P, _I, _I]),
     "e2d_batch_get_launch": (_I, [_P, _PI, _PI]),
     "e2d_batch_autotune": (_I, [_P, ctypes.c_char_p, _I, _PI, _PI, _PD]),
+    "e2d_batch_create_tuned": (_I, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Params), _I, ctypes.c_char_p, _I,
+                                    _PP, _PI]),
     "e2d_batch_last_device_ms": (_I, [_P, _PD]),
     "e2d_batch_launches_per_iteration": (_I, [_P, _PI]),
 }

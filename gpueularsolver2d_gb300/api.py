@@ -241,6 +241,25 @@ class Batch:
         self._h = h
         self.ncells = [m.info(p.wall_box).ncell for m, p in zip(self.meshes, self.params)]
 
+    @classmethod
+    def tuned(cls, meshes, params, cache_path: str | None = None, iters: int = 16):
+        """Batch with the cell order and launch shape picked by the autotuner
+        (e2d_batch_create_tuned); .ordering holds the order chosen."""
+        self = cls.__new__(cls)
+        self.meshes = list(meshes)
+        self.params = list(params)
+        n = len(self.meshes)
+        handles = (ctypes.c_void_p * n)(*[m._h.value for m in self.meshes])
+        parr = (Params * n)(*self.params)
+        h = ctypes.c_void_p()
+        order = ctypes.c_int32()
+        check(load().e2d_batch_create_tuned(handles, parr, n, cache_path.encode() if cache_path else None, iters,
+                                            ctypes.byref(h), ctypes.byref(order)))
+        self._h = h
+        self.ordering = order.value
+        self.ncells = [m.info(p.wall_box).ncell for m, p in zip(self.meshes, self.params)]
+        return self
+
     def step(self, n: int) -> None:
         check(load().e2d_batch_step(self._h, n))
 

@@ -502,6 +502,37 @@ int e2d_batch_get_launch(e2d_batch *b, int32_t *block, int32_t *grid) {
     return E2D_OK;
 }
 
+int e2d_batch_create_tuned(e2d_mesh **meshes, const e2d_params *params, int32_t ncase, const char *cache_path,
+                           int32_t iters, e2d_batch **out, int32_t *ordering) {
+    if (!meshes || !params || !out || ncase < 1 || iters < 1) { set_error("bad argument"); return E2D_ERR_ARG; }
+    *out = nullptr;
+    std::vector<e2d_params> P(params, params + ncase);
+    double best = 1e300;
+    int best_ord = E2D_ORDER_MORTON;
+    for (int ord : {E2D_ORDER_MORTON, E2D_ORDER_RCM, E2D_ORDER_FILE}) {
+        for (auto &p : P) p.ordering = ord;
+        e2d_batch *b = nullptr;
+        int rc = e2d_batch_create(meshes, P.data(), ncase, &b);
+        if (rc) return rc;
+        double ms = 0.0;
+        rc = e2d_batch_autotune(b, cache_path, iters, nullptr, nullptr, &ms);
+        e2d_batch_destroy(b);
+        if (rc) return rc;
+        if (ms < best) { best = ms; best_ord = ord; }
+    }
+    for (auto &p : P) p.ordering = best_ord;
+    int rc = e2d_batch_create(meshes, P.data(), ncase, out);
+    if (rc) return rc;
+    // the winner's launch shape is in the cache when there is one, else tune again
+    if ((rc = e2d_batch_autotune(*out, cache_path, iters, nullptr, nullptr, nullptr))) {
+        e2d_batch_destroy(*out);
+        *out = nullptr;
+        return rc;
+    }
+    if (ordering) *ordering = best_ord;
+    return E2D_OK;
+}
+
 int e2d_batch_last_device_ms(e2d_batch *b, double *ms) {
     if (!b || !ms) { set_error("null argument"); return E2D_ERR_ARG; }
     *ms = b->last_ms;
@@ -525,7 +556,8 @@ int e2d_batch_autotune(e2d_batch *b, const char *cache_path, int32_t iters, int3
     if (!b || iters < 1) { set_error("bad argument"); return E2D_ERR_ARG; }
     std::ostringstream key;
     key << gpu_name() << "|cells=" << b->ntot << "|cases=" << b->ncase << "|prec=" << b->prm[0].precision
-        << "|stages=" << b->prm[0].rk_stages << "|sweeps=" << b->prm[0].irs_sweeps;
+        << "|stages=" << b->prm[0].rk_stages << "|sweeps=" << b->prm[0].irs_sweeps
+        << "|order=" << b->prm[0].ordering;
     std::string text;
     if (cache_path) {
         if (FILE *f = std::fopen(cache_path, "r")) {

@@ -259,6 +259,14 @@ int e2d_batch_get_launch(e2d_batch *b, int32_t *block, int32_t *grid);
  * scheme; a hit is applied without timing, a new result is added. */
 int e2d_batch_autotune(e2d_batch *b, const char *cache_path, int32_t iters, int32_t *block, int32_t *grid,
                        double *ms_per_iter);
+/* e2d_batch_create with the cell order picked by the autotuner too: every
+ * case's params.ordering is replaced by each of E2D_ORDER_MORTON,
+ * E2D_ORDER_RCM and E2D_ORDER_FILE in turn, each candidate batch is
+ * launch-tuned (e2d_batch_autotune, same cache), and the batch of the fastest
+ * order and shape is returned; *ordering (may be NULL) receives the order.
+ * The order changes only the memory layout: results are the same bits. */
+int e2d_batch_create_tuned(e2d_mesh **meshes, const e2d_params *params, int32_t ncase, const char *cache_path,
+                           int32_t iters, e2d_batch **out, int32_t *ordering);
 int e2d_batch_last_device_ms(e2d_batch *b, double *ms);
 int e2d_batch_launches_per_iteration(e2d_batch *b, int32_t *n);
 

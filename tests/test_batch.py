@@ -57,6 +57,24 @@ def test_batch_options_equal_single_cases(lib):
         assert np.array_equal(b.history(c), s.history()), c
 
 
+def test_batch_tuned_order_and_shape(lib, tmp_path):
+    """The autotuner picks a cell order and launch shape; the tuned batch gives
+    the same bits as a plain batch (the order only changes the layout), and
+    the cache holds one entry per order."""
+    meshes, params = make_cases(e2d.E2D_FP32)
+    cache = str(tmp_path / "tune.json")
+    t = e2d.Batch.tuned(meshes, params, cache, iters=8)
+    assert t.ordering in (e2d.E2D_ORDER_MORTON, e2d.E2D_ORDER_RCM, e2d.E2D_ORDER_FILE)
+    assert open(cache).read().count("|order=") == 3
+    ref = e2d.Batch(meshes, params)
+    t.step(9)
+    ref.step(9)
+    for c in range(len(meshes)):
+        assert np.array_equal(t.state(c), ref.state(c)), c
+    t2 = e2d.Batch.tuned(meshes, params, cache, iters=8)  # from the cache
+    assert t2.ordering == t.ordering and t2.launch() == t.launch()
+
+
 def test_batch_launch_shapes_agree(lib):
     meshes, params = make_cases(e2d.E2D_FP64)
     ref = e2d.Batch(meshes, params)
