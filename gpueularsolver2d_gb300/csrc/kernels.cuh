@@ -636,31 +636,6 @@ __global__ void __launch_bounds__(256) k_smooth(MeshDev<T> m, T eps, const V4<T>
 // Pass D: gpu_solver.cu:1675-1720 (kernel_Smooth2, last sweep + clamp) fused
 // with 938-966 (kernel_RKStep); on the last stage also 968-1020 (kernel_drou)
 // as FP64 block partials and a count of unphysical cells.
-// The arithmetic of pass D for one cell: residual r, neighbour sum d of the
-// last sweep's input (used when smooth), time step dti, area A, start state w0.
-template <typename T>
-__device__ __forceinline__ V4<T> rk_update(const Flow<T> &f, const T rk, const int smooth, const int clog, V4<T> r,
-                                           const V4<T> &d, const T dti, const T A, const V4<T> &w0) {
-    if (smooth) {
-        const T eps = f.irs_eps;
-        const T den = T(1.0) + (eps) * T(clog);
-        T s0 = madd(d.x, eps, r.x) / den, s1 = madd(d.y, eps, r.y) / den;
-        T s2 = madd(d.z, eps, r.z) / den, s3 = madd(d.w, eps, r.w) / den;
-        if (tabs(r.x) > tabs(s0)) r.x = s0;
-        if (tabs(r.y) > tabs(s1)) r.y = s1;
-        if (tabs(r.z) > tabs(s2)) r.z = s2;
-        if (tabs(r.w) > tabs(s3)) r.w = s3;
-    }
-    T RK = rk;
-    RK *= dti;
-    V4<T> w;
-    w.x = w0.x - RK * r.x / A;
-    w.y = w0.y - RK * r.y / A;
-    w.z = w0.z - RK * r.z / A;
-    w.w = w0.w - RK * r.w / A;
-    return w;
-}
-
 template <typename T>
 __device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &f, const T rk,
                                             const int smooth, const int i, const V4<T> *__restrict__ src,
@@ -669,13 +644,27 @@ __device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &
                                             int &bad) {
     {
         const int4 tp = m.topo[i];
-        const V4<T> r = res[i];
-        V4<T> d;
-        d.x = T(0.0); d.y = T(0.0); d.z = T(0.0); d.w = T(0.0);
-        if (smooth) d = nb_sum(tp, src);
+        V4<T> r = res[i];
+        if (smooth) {
+            const V4<T> d = nb_sum(tp, src);
+            const T eps = f.irs_eps;
+            const T den = T(1.0) + (eps) * T(tp.w);
+            T s0 = madd(d.x, eps, r.x) / den, s1 = madd(d.y, eps, r.y) / den;
+            T s2 = madd(d.z, eps, r.z) / den, s3 = madd(d.w, eps, r.w) / den;
+            if (tabs(r.x) > tabs(s0)) r.x = s0;
+            if (tabs(r.y) > tabs(s1)) r.y = s1;
+            if (tabs(r.z) > tabs(s2)) r.z = s2;
+            if (tabs(r.w) > tabs(s3)) r.w = s3;
+        }
+        T RK = rk;
+        RK *= dti;
         const T A = m.area[i];
         const V4<T> w0 = W0[i];
-        const V4<T> w = rk_update(f, rk, smooth, tp.w, r, d, dti, A, w0);
+        V4<T> w;
+        w.x = w0.x - RK * r.x / A;
+        w.y = w0.y - RK * r.y / A;
+        w.z = w0.z - RK * r.z / A;
+        w.w = w0.w - RK * r.w / A;
         Wout[i] = w;
         if (want) {
             double dd = (double)w.x - (double)w0.x;
@@ -722,39 +711,6 @@ __global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, i
         update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, ctl, st, dt, i), W0, Wout, part != nullptr, d2, bad);
     if (!part) return;
     block_partial(d2, bad, part + blockIdx.x, &ctl->nbad);
-}
-
-// Pass D of the stages before the last (W0 and Wout are distinct arrays, no
-// residual partials): two cells per thread, cells i and i + blockDim.x of a
-// 2 * blockDim.x tile, so that the loads of both (and their dependent
-// neighbour gathers) are in flight together.  The per-cell arithmetic is
-// update_cell's.  FP32 only: the kernel is memory-latency bound there.
-template <typename T> struct PairUpdate { static constexpr bool value = sizeof(T) == 4; };
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_update_pair(MeshDev<T> m, Flow<T> f, T rk, int smooth,
-                                                     const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
-                                                     const T *__restrict__ dt, const V4<T> *__restrict__ W0,
-                                                     V4<T> *__restrict__ Wout, Ctl *ctl, const int st) {
-    wait_prior_grid();
-    if (ctl->halt) return;
-    const int i0 = blockIdx.x * 2 * blockDim.x + threadIdx.x, i1 = i0 + blockDim.x;
-    const bool a1 = i1 < m.n;
-    if (i0 >= m.n) return;
-    // every independent load of both cells first, then the dependent gathers
-    const int4 tp0 = m.topo[i0];
-    const int4 tp1 = a1 ? m.topo[i1] : make_int4(-1, -1, -1, 0);
-    const V4<T> r0 = res[i0], w00 = W0[i0];
-    const T A0 = m.area[i0], dt0 = stage_dt(f, ctl, st, dt, i0);
-    V4<T> r1 = r0, w01 = w00;
-    T A1 = A0, dt1 = dt0;
-    if (a1) { r1 = res[i1]; w01 = W0[i1]; A1 = m.area[i1]; dt1 = stage_dt(f, ctl, st, dt, i1); }
-    V4<T> d0, d1;
-    d0.x = d0.y = d0.z = d0.w = T(0.0);
-    d1 = d0;
-    if (smooth) { d0 = nb_sum(tp0, src); d1 = nb_sum(tp1, src); }
-    Wout[i0] = rk_update(f, rk, smooth, tp0.w, r0, d0, dt0, A0, w00);
-    if (a1) Wout[i1] = rk_update(f, rk, smooth, tp1.w, r1, d1, dt1, A1, w01);
 }
 
 // ---------------------------------------------------------------------------
@@ -914,12 +870,8 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
             launch_chained(k_smooth<T>, G, B, s, p.m, p.f.irs_eps, src, p.res, dst, p.ctl);
             src = dst;
         }
-        if (!last && PairUpdate<T>::value)
-            launch_chained(k_update_pair<T>, (n + 2 * B - 1) / (2 * B), B, s, p.m, p.f, p.rk[st],
-                           p.sweeps > 0 ? 1 : 0, src, p.res, p.dt, (const V4<T> *)p.W[0], Wout, p.ctl, st);
-        else
-            launch_chained(k_update<T>, G, B, s, p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
-                           p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
+        launch_chained(k_update<T>, G, B, s, p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
+                       p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
     }
     enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, s);
 }
@@ -949,12 +901,8 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
             src = dst;
         }
         mark(3);
-        if (!last && PairUpdate<T>::value)
-            k_update_pair<T><<<(n + 2 * B - 1) / (2 * B), B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src,
-                                                                     p.res, p.dt, p.W[0], Wout, p.ctl, st);
-        else
-            k_update<T><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
-                                        p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
+        k_update<T><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
+                                    p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
         done();
     }
     mark(4); enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, s); done();
