@@ -357,8 +357,9 @@ def run_gpu(args, rank: int, world: int):
 def run_batch64(args):
     """Batched sweep: 64 cases on O-grids of sizes drawn from {64..512}x{16..128}
     (seed 2), Mach U[0.3, 0.85], alpha U[-2, 4] deg, FP32, one launch per pass
-    over all cases with the autotuned launch shape, against the same 64 cases
-    solved one after the other by the single-case solver."""
+    over all cases with the cell order and launch shape picked by the
+    autotuner, against the same 64 cases solved one after the other by the
+    single-case solver."""
     import numpy as np
     import torch
     import gpueularsolver2d_gb300 as e2d
