@@ -44,6 +44,7 @@ struct BatchBase {
     virtual int download_case(int c, double *w_file, cudaStream_t s) = 0;
     virtual int save_state(cudaStream_t s) = 0;
     virtual int restore_state(cudaStream_t s) = 0;
+    virtual const void *topo_ptr() const = 0;
 };
 
 template <typename T> struct BatchT : BatchBase {
@@ -168,6 +169,7 @@ template <typename T> struct BatchT : BatchBase {
     }
 
     int launches() const override { return launches_per_iteration(plan); }
+    const void *topo_ptr() const override { return plan.m.topo; }
 
     int upload_case(int c, const double *w, cudaStream_t s) override {
         const int n = (*L)[c].n, o = (*off)[c];
@@ -243,6 +245,7 @@ int rebuild_graph(e2d_batch *b) {
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc) { if (g) cudaGraphDestroy(g); return rc; }
     if (e != cudaSuccess) { set_error(std::string("graph capture: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
+    keep_in_l2(g, b->impl->topo_ptr(), sizeof(int4) * (size_t)b->ntot);
     e = cudaGraphInstantiate(&b->gexec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) { b->gexec = nullptr; set_error(std::string("graph instantiate: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }

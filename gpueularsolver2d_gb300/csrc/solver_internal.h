@@ -39,6 +39,10 @@ void forces_from_state(const HostLayout &L, const FreeStream &fs, double gamma, 
 // Parameter checks shared by the solver constructors.
 bool valid_params(const e2d_params *p);
 
+// Marks [base, base + bytes) as persisting in L2 for every kernel node of a
+// captured graph (the cell topology, which all four passes read).
+void keep_in_l2(cudaGraph_t g, const void *base, size_t bytes);
+
 // Device arena: one cudaMalloc carved into 256-byte aligned pieces.
 struct Arena {
     char *base = nullptr;
