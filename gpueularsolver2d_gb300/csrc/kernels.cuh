@@ -309,6 +309,25 @@ __device__ __forceinline__ V4<float> roe<float>(const V4<float> &LW, const V4<fl
 // phi; once frozen they are reused instead of re-evaluated, which makes the
 // residual a smooth function of the state so that it can converge below the
 // limiter's chatter floor.
+// Face midpoint minus cell centroid of face k.  FP64 reads the value the host
+// computed with the reference's formulas (midpoint and centroid averages,
+// gpu_init.cu:100-228), which keeps the FP64 parity bit for bit.  FP32
+// derives it from the face vectors already in registers instead of reading 24
+// bytes per cell: with e_j = (-S_j.y, S_j.x) the edge opposite node j,
+// mid_k - centroid = (e_{k+2} - e_{k+1}) / 6 exactly.
+template <typename T>
+__device__ __forceinline__ V2<T> face_offset(const MeshDev<T> &m, const V2<T> *S, int k, int i) {
+    return m.R[k * m.n + i];
+}
+template <>
+__device__ __forceinline__ V2<float> face_offset<float>(const MeshDev<float> &m, const V2<float> *S, int k, int i) {
+    const V2<float> a = S[(k + 1) % 3], b = S[(k + 2) % 3];
+    V2<float> r;
+    r.x = (a.y - b.y) * (1.0f / 6.0f);
+    r.y = (b.x - a.x) * (1.0f / 6.0f);
+    return r;
+}
+
 // Returns the cell's local time step (also stored in dt[i]).
 template <typename T>
 __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, const int i,
@@ -358,7 +377,7 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
     for (int k = 0; k < 3; k++) {
         V4<T> o = U;
         if (code[k] >= 0) {
-            const V2<T> r = m.R[k * n + i];
+            const V2<T> r = face_offset(m, S, k, i);
             const bool reuse = phi && frozen;
             V4<T> pf;
             if (reuse) pf = phi[k * n + i];
