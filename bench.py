@@ -57,10 +57,11 @@ def bytes_per_cell(prec_bytes: int) -> dict:
     T = prec_bytes
     topo = 16
     W, S2x3, R2x3, A, FS, dt, V4 = 4 * T, 6 * T, 6 * T, T, 12 * T, T, 4 * T
+    Af = A
     if T == 4:
-        R2x3 = 0  # the FP32 pass A derives the face offsets from S
+        R2x3, Af = 0, 0  # the FP32 pass A derives face offsets and area from S
     return {
-        "faces": W + topo + S2x3 + R2x3 + A + FS + dt,   # reads W,topo,S,(R),area -> FS, dt
+        "faces": W + topo + S2x3 + R2x3 + Af + FS + dt,  # reads W,topo,S,(R,area) -> FS, dt
         "flux": topo + S2x3 + FS + V4,                   # reads topo,S,FS -> res
         "smooth": topo + V4 + V4 + V4,                   # reads topo,src,res -> dst
         "update": topo + V4 + V4 + dt + A + V4 + V4,     # topo,src,res,dt,area,W0 -> W

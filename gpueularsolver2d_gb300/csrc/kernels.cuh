@@ -328,6 +328,18 @@ __device__ __forceinline__ V2<float> face_offset<float>(const MeshDev<float> &m,
     return r;
 }
 
+// Cell area: FP64 reads the host value (Calc_area, gpu_init.cu:95-98); FP32
+// takes half the cross product of two edge vectors, (S_1.x S_2.y - S_1.y S_2.x) / 2
+// with the edges e_j = (-S_j.y, S_j.x) of a counter-clockwise cell.
+template <typename T>
+__device__ __forceinline__ T cell_area(const MeshDev<T> &m, const V2<T> *S, int i) {
+    return m.area[i];
+}
+template <>
+__device__ __forceinline__ float cell_area<float>(const MeshDev<float> &m, const V2<float> *S, int i) {
+    return 0.5f * fmaf(S[1].x, S[2].y, -(S[1].y * S[2].x));
+}
+
 // Returns the cell's local time step (also stored in dt[i]).
 template <typename T>
 __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, const int i,
@@ -363,7 +375,7 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
         }
         Tsum += spectral_radius(U, nbv[k], S[k].y, S[k].x, f.gamma);
     }
-    const T A = m.area[i];
+    const T A = cell_area(m, S, i);
     const T rA = T(1.0) / A;
     T gx[4], gy[4], umax[4], umin[4];
 #pragma unroll
