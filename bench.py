@@ -29,6 +29,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -78,7 +79,8 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.proc = None
         self.gpu = gpu_index
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu_index}.csv")
+        out = os.environ.get("E2D_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out, f"e2d_clocks_gpu{gpu_index}.csv")
 
     def start(self):
         try:
