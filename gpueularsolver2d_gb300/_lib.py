@@ -150,6 +150,7 @@ SIGNATURES.update({
     "e2d_mlp_get_params": (_I, [_P, _PF]),
     "e2d_mlp_set_params": (_I, [_P, _PF]),
     "e2d_mlp_set_data": (_I, [_P, ctypes.c_int64, _PF, _PF]),
+    "e2d_mlp_set_lr": (_I, [_P, _D]),
     "e2d_mlp_train": (_I, [_P, _I, _PD]),
     "e2d_mlp_forward": (_I, [_P, ctypes.c_int64, _PF, _PF]),
     "e2d_mlp_gradient": (_I, [_P, _PF, _PF, _PD, _PF]),

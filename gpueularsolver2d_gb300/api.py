@@ -382,6 +382,10 @@ class MLP:
         t = np.ascontiguousarray(t, np.float32).reshape(-1, 4)
         check(load().e2d_mlp_set_data(self._h, x.shape[0], _fp(x), _fp(t)))
 
+    def set_lr(self, lr: float) -> None:
+        """Adam step size of the following training steps."""
+        check(load().e2d_mlp_set_lr(self._h, lr))
+
     def train(self, steps: int, record_loss: bool = True) -> np.ndarray:
         loss = np.zeros(steps)
         check(load().e2d_mlp_train(self._h, steps, _dp(loss) if record_loss else None))

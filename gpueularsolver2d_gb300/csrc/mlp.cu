@@ -42,12 +42,12 @@ __global__ void k_step_update(int *step, float beta1, float beta2, float *bc) {
     bc[1] = 1.f - powf(beta2, (float)s);
 }
 
-// wbf / wbfT (may be null): the bf16 copies [rows][cols] and [cols][rows]
-// used by the GEMMs.
-__global__ void __launch_bounds__(256) k_adam_dev(int count, int cols, const float *__restrict__ part, int nparts,
+// wbf (may be null): the bf16 copy used by the GEMMs; lr (device, read at
+// run time so that the host can schedule it) null: gradient only.
+__global__ void __launch_bounds__(256) k_adam_dev(int count, const float *__restrict__ part, int nparts,
                                                   size_t pstride, float *__restrict__ w32, bf16 *__restrict__ wbf,
-                                                  bf16 *__restrict__ wbfT,
-                                                  float *__restrict__ m, float *__restrict__ v, float lr,
+                                                  float *__restrict__ m, float *__restrict__ v,
+                                                  const float *__restrict__ lr_dev,
                                                   float beta1, float beta2, float eps, const float *__restrict__ bc,
                                                   float *__restrict__ grad_out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -55,7 +55,8 @@ __global__ void __launch_bounds__(256) k_adam_dev(int count, int cols, const flo
     float g = 0.f;
     for (int p = 0; p < nparts; p++) g += part[(size_t)p * pstride + i];
     if (grad_out) grad_out[i] = g;
-    if (lr == 0.f) return;
+    if (!lr_dev) return;
+    const float lr = *lr_dev;
     const float mi = beta1 * m[i] + (1.f - beta1) * g;
     const float vi = beta2 * v[i] + (1.f - beta2) * g * g;
     m[i] = mi;
@@ -63,7 +64,6 @@ __global__ void __launch_bounds__(256) k_adam_dev(int count, int cols, const flo
     const float w = w32[i] - lr * (mi / bc[0]) / (sqrtf(vi / bc[1]) + eps);
     w32[i] = w;
     if (wbf) wbf[i] = __float2bfloat16_rn(w);
-    if (wbfT) wbfT[(size_t)(i % cols) * (count / cols) + i / cols] = __float2bfloat16_rn(w);
 }
 
 __global__ void k_to_bf16(int n, const float *__restrict__ a, bf16 *__restrict__ b) {
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) k_wall_distance(int n, const double *__re
 struct Tensor {
     int rows, cols;
     float *w32 = nullptr, *m = nullptr, *v = nullptr;
-    bf16 *wbf = nullptr, *wbfT = nullptr;  // hidden layers: [rows][cols] and [cols][rows]
+    bf16 *wbf = nullptr;  // hidden layers: [rows][cols]
     int count() const { return rows * cols; }
 };
 
@@ -112,17 +112,17 @@ struct e2d_mlp {
     std::vector<Tensor> W, b;  // hidden layers (W: H x in, b: H x 1) then the output layer
     // batch buffers
     int B = 0;
-    bf16 *xb = nullptr, *xbT = nullptr;  // [B][NIN] and [NIN][B]
+    bf16 *xb = nullptr;  // [B][NIN]
     float *tb = nullptr, *y = nullptr, *dy = nullptr;
     std::vector<bf16 *> Z, Hh;  // [nhidden] of [B][H]
-    std::vector<bf16 *> HT;     // [nhidden]: Hh transposed [H][B] for the weight gradients (last: unused)
-    bf16 *dz[2] = {nullptr, nullptr}, *dzT[2] = {nullptr, nullptr};
+    bf16 *dz[2] = {nullptr, nullptr};  // [B][H]
     float *part = nullptr;      // weight-gradient partials (largest tensor x kSplits)
     float *bpart = nullptr;     // bias-gradient partials
     double *loss_part = nullptr;
     int *step_dev = nullptr;
     int *flag_dev = nullptr;    // set by a tensor-core GEMM whose wait timed out
     float *bc_dev = nullptr;
+    float *lr_dev = nullptr;    // Adam step size, read by every step
     float *grad = nullptr;      // flat gradient of all parameters (gradient probe)
     // training set
     bf16 *X = nullptr;
@@ -166,44 +166,34 @@ int ensure_batch(e2d_mlp *m, int B) {
     m->B = B;
     int rc;
     if ((rc = m->alloc(&m->xb, sizeof(bf16) * (size_t)B * NIN))) return rc;
-    if ((rc = m->alloc(&m->xbT, sizeof(bf16) * (size_t)B * NIN))) return rc;
     if ((rc = m->alloc(&m->tb, sizeof(float) * (size_t)B * NOUT))) return rc;
     if ((rc = m->alloc(&m->y, sizeof(float) * (size_t)B * NOUT))) return rc;
     if ((rc = m->alloc(&m->dy, sizeof(float) * (size_t)B * NOUT))) return rc;
     m->Z.resize(m->nhidden);
     m->Hh.resize(m->nhidden);
-    m->HT.assign(m->nhidden, nullptr);
     for (int l = 0; l < m->nhidden; l++) {
         if ((rc = m->alloc(&m->Z[l], sizeof(bf16) * (size_t)B * H))) return rc;
         if ((rc = m->alloc(&m->Hh[l], sizeof(bf16) * (size_t)B * H))) return rc;
-        if (l + 1 < m->nhidden && (rc = m->alloc(&m->HT[l], sizeof(bf16) * (size_t)B * H))) return rc;
     }
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < 2; k++)
         if ((rc = m->alloc(&m->dz[k], sizeof(bf16) * (size_t)B * H))) return rc;
-        if ((rc = m->alloc(&m->dzT[k], sizeof(bf16) * (size_t)B * H))) return rc;
-    }
     if ((rc = m->alloc(&m->part, sizeof(float) * (size_t)kSplits * H * H))) return rc;
     if ((rc = m->alloc(&m->bpart, sizeof(float) * (size_t)kSplits * (NOUT * H + NOUT + H)))) return rc;
     if ((rc = m->alloc(&m->loss_part, sizeof(double) * (B / 256)))) return rc;
     return E2D_OK;
 }
 
-void adam(e2d_mlp *m, cudaStream_t s, Tensor &t, const float *part, int nparts, size_t pstride, float lr,
+void adam(e2d_mlp *m, cudaStream_t s, Tensor &t, const float *part, int nparts, size_t pstride, const float *lr,
           float *grad_out) {
     const auto &c = m->cfg;
-    k_adam_dev<<<(t.count() + 255) / 256, 256, 0, s>>>(t.count(), t.cols, part, nparts, pstride, t.w32, t.wbf,
-                                                        t.wbfT, t.m, t.v,
+    k_adam_dev<<<(t.count() + 255) / 256, 256, 0, s>>>(t.count(), part, nparts, pstride, t.w32, t.wbf, t.m, t.v,
                                                         lr, (float)c.beta1, (float)c.beta2, (float)c.eps, m->bc_dev,
                                                         grad_out);
 }
 
-template <int EPI> void gemm(e2d_mlp *m, GemmArgs g, dim3 grid, cudaStream_t s) {
+template <bool TA, bool TB, int EPI> void gemm(e2d_mlp *m, GemmArgs g, dim3 grid, cudaStream_t s) {
     g.flag = m->flag_dev;
-    k_gemm_tc<EPI><<<grid, 256, tc::SMEM, s>>>(g);
-}
-
-void transpose(const bf16 *a, bf16 *t, int rows, int cols, cudaStream_t s) {
-    k_transpose<<<dim3((cols + 31) / 32, (rows + 31) / 32), 256, 0, s>>>(rows, cols, a, t);
+    k_gemm_tc<TA, TB, EPI><<<grid, 256, tc::SMEM, s>>>(g);
 }
 
 // Reports (and clears) a timed-out tensor-core wait of the kernels run so far.
@@ -229,8 +219,7 @@ void forward(e2d_mlp *m, cudaStream_t s, bool with_loss) {
         g.lda = g.K;
         g.B = m->W[l].wbf; g.ldb = g.K;
         g.bias = m->b[l].w32; g.out = m->Hh[l]; g.zout = m->Z[l]; g.ldc = H;
-        g.outT = m->HT[l]; g.ldt = B;  // null for the last hidden layer
-        gemm<EPI_BIAS_GELU>(m, g, dim3(H / BN, (B + BM - 1) / BM, 1), s);
+        gemm<false, false, EPI_BIAS_GELU>(m, g, dim3(H / BN, (B + BM - 1) / BM, 1), s);
     }
     const Tensor &Wo = m->W[m->nhidden], &bo = m->b[m->nhidden];
     k_out_fwd_loss<H, NOUT><<<(B + 255) / 256, 256, 0, s>>>(B, m->Hh[m->nhidden - 1], Wo.w32, bo.w32,
@@ -238,8 +227,9 @@ void forward(e2d_mlp *m, cudaStream_t s, bool with_loss) {
                                                             with_loss ? m->loss_part : nullptr);
 }
 
-// Backward + Adam (lr = 0: gradient only, written to m->grad in parameter order).
-void backward(e2d_mlp *m, cudaStream_t s, float lr, bool want_grad) {
+// Backward + Adam with the step size at lr (null: gradient only, written to
+// m->grad in parameter order).
+void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
     const int B = m->B, L = m->nhidden;
     const int rows = B / kSplits;
     size_t goff = param_count(m);
@@ -252,7 +242,6 @@ void backward(e2d_mlp *m, cudaStream_t s, float lr, bool want_grad) {
     Tensor &Wo = m->W[L], &bo = m->b[L];
     k_out_bwd_weight<H, NOUT><<<dim3(H / 32, kSplits), 256, 0, s>>>(B, rows, m->dy, m->Hh[L - 1], m->bpart);
     k_out_bwd_data<H, NOUT><<<(B * (H / 2) + 255) / 256, 256, 0, s>>>(B, m->dy, Wo.w32, m->Z[L - 1], m->dz[0]);
-    transpose(m->dz[0], m->dzT[0], B, H, s);
     const size_t ostride = NOUT * H + NOUT;
     float *gbo = gslot(bo);
     float *gWo = gslot(Wo);
@@ -261,26 +250,25 @@ void backward(e2d_mlp *m, cudaStream_t s, float lr, bool want_grad) {
     int cur = 0;
     for (int l = L - 1; l >= 0; l--) {
         const int kin = l == 0 ? NIN : H;
-        const bf16 *hinT = l == 0 ? m->xbT : m->HT[l - 1];
-        // dW_l = dz^T hin (split over the batch; both operands from their
-        // transposed copies, so the reduction index is contiguous), db_l =
-        // column sums of dz
+        // dW_l = dz^T hin (split over the batch; both operands are read
+        // MN-major, the batch index being their slow one), db_l = column sums
+        // of dz
         GemmArgs gw{};
         gw.M = H; gw.N = kin; gw.K = B;
-        gw.A = m->dzT[cur]; gw.lda = B;
-        gw.B = hinT; gw.ldb = B;
+        gw.A = m->dz[cur]; gw.lda = H;
+        gw.B = l == 0 ? m->xb : m->Hh[l - 1]; gw.ldb = kin;
         gw.part = m->part;
-        gemm<EPI_PARTIAL>(m, gw, dim3((kin + BN - 1) / BN, H / BM, kSplits), s);
+        gemm<true, true, EPI_PARTIAL>(m, gw, dim3((kin + BN - 1) / BN, H / BM, kSplits), s);
         k_colsum<<<dim3(H / 32, kSplits), 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart);
-        // gradient at the previous pre-activation (before this layer's weights change)
+        // gradient at the previous pre-activation (before this layer's weights
+        // change): dz W_l, W_l read MN-major ([out][in] = [K][N])
         if (l > 0) {
             GemmArgs gd{};
             gd.M = B; gd.N = H; gd.K = H;
             gd.A = m->dz[cur]; gd.lda = H;
-            gd.B = m->W[l].wbfT; gd.ldb = H;
+            gd.B = m->W[l].wbf; gd.ldb = H;
             gd.zin = m->Z[l - 1]; gd.out = m->dz[cur ^ 1]; gd.ldc = H;
-            gd.outT = m->dzT[cur ^ 1]; gd.ldt = B;
-            gemm<EPI_GELU_BWD>(m, gd, dim3(H / BN, (B + BM - 1) / BM, 1), s);
+            gemm<false, true, EPI_GELU_BWD>(m, gd, dim3(H / BN, (B + BM - 1) / BM, 1), s);
         }
         float *gb = gslot(m->b[l]);
         float *gW = gslot(m->W[l]);
@@ -299,9 +287,8 @@ int build_train_graph(e2d_mlp *m) {
     // the gather reads the step from device memory through its seed argument
     k_gather<<<(m->B + 255) / 256, 256, 0, s>>>(m->B, NIN, NOUT, m->cfg.seed, m->step_dev, m->nsamples, m->X,
                                                   m->T, m->xb, m->tb);
-    transpose(m->xb, m->xbT, m->B, NIN, s);
     forward(m, s, true);
-    backward(m, s, (float)m->cfg.lr, false);
+    backward(m, s, m->lr_dev, false);
     cudaError_t e = cudaStreamEndCapture(s, &g);
     if (e != cudaSuccess) { set_error(std::string("graph capture: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
     e = cudaGraphInstantiate(&m->gexec, g, 0);
@@ -368,24 +355,26 @@ int e2d_mlp_create(const e2d_mlp_config *cfg, e2d_mlp **out) {
             if ((rc = m->alloc(&t->m, sizeof(float) * n))) return rc;
             if ((rc = m->alloc(&t->v, sizeof(float) * n))) return rc;
             if (!last && t == &W && (rc = m->alloc(&t->wbf, sizeof(bf16) * n))) return rc;
-            if (!last && t == &W && (rc = m->alloc(&t->wbfT, sizeof(bf16) * n))) return rc;
         }
         CK(cudaMemcpy(W.w32, hw.data(), sizeof(float) * hw.size(), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(b.w32, hb.data(), sizeof(float) * hb.size(), cudaMemcpyHostToDevice));
-        if (W.wbf) {
-            k_to_bf16<<<(W.count() + 255) / 256, 256, 0, m->stream>>>(W.count(), W.w32, W.wbf);
-            transpose(W.wbf, W.wbfT, W.rows, W.cols, m->stream);
-        }
+        if (W.wbf) k_to_bf16<<<(W.count() + 255) / 256, 256, 0, m->stream>>>(W.count(), W.w32, W.wbf);
         m->W.push_back(W);
         m->b.push_back(b);
     }
     int rc;
     if ((rc = m->alloc(&m->step_dev, sizeof(int)))) return rc;
     if ((rc = m->alloc(&m->flag_dev, sizeof(int)))) return rc;
-    CK(cudaFuncSetAttribute(k_gemm_tc<EPI_BIAS_GELU>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM));
-    CK(cudaFuncSetAttribute(k_gemm_tc<EPI_GELU_BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM));
-    CK(cudaFuncSetAttribute(k_gemm_tc<EPI_PARTIAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM));
+    CK(cudaFuncSetAttribute(k_gemm_tc<false, false, EPI_BIAS_GELU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            tc::SMEM));
+    CK(cudaFuncSetAttribute(k_gemm_tc<false, true, EPI_GELU_BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            tc::SMEM));
+    CK(cudaFuncSetAttribute(k_gemm_tc<true, true, EPI_PARTIAL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            tc::SMEM));
     if ((rc = m->alloc(&m->bc_dev, 2 * sizeof(float)))) return rc;
+    if ((rc = m->alloc(&m->lr_dev, sizeof(float)))) return rc;
+    const float lr0 = (float)cfg->lr;
+    CK(cudaMemcpy(m->lr_dev, &lr0, sizeof(float), cudaMemcpyHostToDevice));
     if ((rc = m->alloc(&m->grad, sizeof(float) * param_count(m.get())))) return rc;
     CK(cudaStreamSynchronize(m->stream));
     *out = m.release();
@@ -417,13 +406,21 @@ int e2d_mlp_set_params(e2d_mlp *m, const float *in) {
     for (size_t l = 0; l < m->W.size(); l++)
         for (Tensor *t : {&m->W[l], &m->b[l]}) {
             CK(cudaMemcpy(t->w32, in + off, sizeof(float) * t->count(), cudaMemcpyHostToDevice));
-            if (t->wbf) {
-                k_to_bf16<<<(t->count() + 255) / 256, 256, 0, m->stream>>>(t->count(), t->w32, t->wbf);
-                transpose(t->wbf, t->wbfT, t->rows, t->cols, m->stream);
-            }
+            if (t->wbf) k_to_bf16<<<(t->count() + 255) / 256, 256, 0, m->stream>>>(t->count(), t->w32, t->wbf);
             off += t->count();
         }
     CK(cudaStreamSynchronize(m->stream));
+    return E2D_OK;
+}
+
+int e2d_mlp_set_lr(e2d_mlp *m, double lr) {
+    if (!m) { set_error("null argument"); return E2D_ERR_ARG; }
+    if (!(lr >= 0.0 && lr < 1e30)) { set_error("lr must be finite and >= 0"); return E2D_ERR_ARG; }
+    const float v = (float)lr;
+    // ordered after the steps already queued on the training stream
+    CK(cudaMemcpyAsync(m->lr_dev, &v, sizeof(float), cudaMemcpyHostToDevice, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    m->cfg.lr = lr;
     return E2D_OK;
 }
 
@@ -489,9 +486,8 @@ int e2d_mlp_gradient(e2d_mlp *m, const float *x, const float *t, double *loss, f
     for (size_t i = 0; i < xb.size(); i++) xb[i] = __float2bfloat16_rn(x[i]);
     CK(cudaMemcpy(m->xb, xb.data(), sizeof(bf16) * xb.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(m->tb, t, sizeof(float) * (size_t)m->B * NOUT, cudaMemcpyHostToDevice));
-    transpose(m->xb, m->xbT, m->B, NIN, m->stream);
     forward(m, m->stream, true);
-    backward(m, m->stream, 0.f, true);
+    backward(m, m->stream, nullptr, true);
     CK(cudaGetLastError());
     const int nlp = m->B / 256;
     std::vector<double> lp(nlp);

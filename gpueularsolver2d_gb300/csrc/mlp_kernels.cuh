@@ -24,27 +24,27 @@ __device__ __forceinline__ float gelu_grad(float x) {
 
 // Epilogue modes of the GEMM.
 enum Epi : int {
-    EPI_BIAS_GELU = 0,  // z = acc + bias[n]; out = gelu(z), zout = z (bf16); outT = out transposed
-    EPI_GELU_BWD = 1,   // out = acc * gelu'(zin[m,n]) (bf16), outT = out transposed
+    EPI_BIAS_GELU = 0,  // z = acc + bias[n]; out = gelu(z), zout = z (bf16)
+    EPI_GELU_BWD = 1,   // out = acc * gelu'(zin[m,n]) (bf16)
     EPI_PARTIAL = 2,    // part[split][m][n] = acc (fp32): split-K partial of a weight gradient
 };
 
-// C[M][N] = A[M][K] * B[N][K]^T: both operands K-major (row-major with the
-// reduction index contiguous), which is why the forward pass also writes
-// transposed copies of the activations for the weight gradients.
+// C = opA(A) * opB(B) with opA(A)[m][k] = TA ? A[k][m] : A[m][k] and
+// opB(B)[k][n] = TB ? B[k][n] : B[n][k]: each operand is read in place, K-major
+// (reduction index contiguous) or MN-major, and staged in the matching
+// tensor-core layout.
 struct GemmArgs {
     int M, N, K;           // reduction over K (per split: K / gridDim.z, a multiple of 32)
-    const bf16 *A;         // [M][lda]
+    const bf16 *A;         // TA ? [K][lda] : [M][lda]
     int lda;
-    const bf16 *B;         // [N][ldb]
+    const bf16 *B;         // TB ? [K][ldb] : [N][ldb]
     int ldb;
     const float *bias;     // EPI_BIAS_GELU
     const bf16 *zin;       // EPI_GELU_BWD: [M][ldc]
     bf16 *out;             // EPI_BIAS_GELU / EPI_GELU_BWD: [M][ldc]
     bf16 *zout;            // EPI_BIAS_GELU: [M][ldc]
-    bf16 *outT;            // optional [N][ldt]: out transposed
     float *part;           // EPI_PARTIAL: [splits][M][N]
-    int ldc, ldt;
+    int ldc;
     int *flag;             // set to 1 if a wait timed out
 };
 
@@ -52,7 +52,8 @@ struct GemmArgs {
 // GEMM on tcgen05: one thread issues tcgen05.mma (kind::f16, M = N = 128,
 // K = 16) into a 128-column FP32 accumulator in tensor memory; operands are
 // copied global -> shared with cp.async straight into the canonical
-// no-swizzle K-major layout (8 x 8 core matrices of 128 bytes), two stages
+// no-swizzle layouts (8 x 8 core matrices of 128 bytes, K-major or MN-major
+// as the operand lies in memory), two stages
 // ahead of the MMAs through a three-buffer ring; tcgen05.commit on a per-buffer
 // mbarrier releases a buffer for refill; the epilogue reads the accumulator
 // back with tcgen05.ld.  Every wait is bounded: on a timeout the CTA sets
@@ -64,20 +65,37 @@ constexpr int TILE = 128 * BK * 2;          // bytes of one 128 x BK operand til
 constexpr int SMEM = 2 * NST * TILE;        // dynamic shared memory per CTA
 constexpr uint32_t TMEM_COLS = 128;         // FP32 accumulator columns (N = 128)
 constexpr int WAIT_LIMIT = 1 << 22;         // try_wait calls before giving up
-// instruction descriptor: FP32 D, BF16 A and B, both K-major, N = 128, M = 128
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
-// core matrix (r/8, k/8) at ((r/8) * (BK/8) + k/8) * 128 bytes, row r%8 at 16 bytes
-constexpr uint32_t LBO = 128;               // next core matrix along K
-constexpr uint32_t SBO = (BK / 8) * 128;    // next core matrix along M / N
+// instruction descriptor: FP32 D, BF16 A and B, N = 128, M = 128; bits 15 / 16
+// set for an MN-major A / B
+template <bool TA, bool TB>
+struct Idesc {
+    static constexpr uint32_t value = (1u << 4) | (1u << 7) | (1u << 10) | ((TA ? 1u : 0u) << 15) |
+                                      ((TB ? 1u : 0u) << 16) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+};
 
-__device__ __forceinline__ int cm_off(int r, int k) { return ((r >> 3) * (BK / 8) + (k >> 3)) * 128 + (r & 7) * 16; }
+// Tile layouts (128 rows of M or N by BK of K, 8 x 8 core matrices of 128 bytes):
+//   K-major : core (r/8, k/8) at ((r/8) * (BK/8) + k/8) * 128, its row r%8 (8 k) at 16 B;
+//             descriptor LBO = 128 (next core along K), SBO = 512 (along M / N),
+//             a K = 16 step moves the start by 256 B
+//   MN-major: core (r/8, k/8) at ((k/8) * 16 + r/8) * 128, its row k%8 (8 r) at 16 B;
+//             descriptor LBO = 2048 (next core along K), SBO = 128 (along M / N),
+//             a K = 16 step moves the start by 4096 B
+template <bool MN> struct Tile;
+template <> struct Tile<false> {
+    static constexpr uint32_t LBO = 128, SBO = (BK / 8) * 128, KSTEP = 256;
+    __device__ static int off(int r, int k) { return ((r >> 3) * (BK / 8) + (k >> 3)) * 128 + (r & 7) * 16; }
+};
+template <> struct Tile<true> {
+    static constexpr uint32_t LBO = 2048, SBO = 128, KSTEP = 4096;
+    __device__ static int off(int r, int k) { return ((k >> 3) * 16 + (r >> 3)) * 128 + (k & 7) * 16; }
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // shared-memory matrix descriptor: start, LBO, SBO (16-byte units), version 1, no swizzle
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
-    return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(LBO >> 4) << 16) | ((uint64_t)(SBO >> 4) << 32) |
-           ((uint64_t)1 << 46);
+template <bool MN> __device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(Tile<MN>::LBO >> 4) << 16) |
+           ((uint64_t)(Tile<MN>::SBO >> 4) << 32) | ((uint64_t)1 << 46);
 }
 
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
@@ -91,18 +109,21 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-// rows [row0, row0 + 128) x k [k0, k0 + BK) of src[row][ld] into tile with
-// cp.async; rows at or past nrows are zero-filled (no bytes read).
+// rows [row0, row0 + 128) x k [k0, k0 + BK) of the operand into tile with
+// cp.async, 16 bytes per copy; MN: src is [k][ld] (rows contiguous), else
+// [row][ld] (k contiguous).  Rows at or past nrows (a multiple of 8) are
+// zero-filled (no bytes read).
+template <bool MN>
 __device__ __forceinline__ void stage(unsigned char *tile, const bf16 *__restrict__ src, int ld, int row0, int nrows,
                                       int k0) {
 #pragma unroll
     for (int it = 0; it < 2; it++) {
         const int c = threadIdx.x + it * 256;
-        const int r = c >> 2, kc = (c & 3) * 8;
+        const int r = MN ? (c & 15) * 8 : c >> 2, k = MN ? c >> 4 : (c & 3) * 8;
         const bool in = row0 + r < nrows;
-        const bf16 *g = in ? src + (size_t)(row0 + r) * ld + k0 + kc : src;
+        const bf16 *g = !in ? src : MN ? src + (size_t)(k0 + k) * ld + row0 + r : src + (size_t)(row0 + r) * ld + k0 + k;
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n"
-                     :: "r"(smem_u32(tile + cm_off(r, kc))), "l"(g), "r"(in ? 16 : 0) : "memory");
+                     :: "r"(smem_u32(tile + Tile<MN>::off(r, k))), "l"(g), "r"(in ? 16 : 0) : "memory");
     }
 }
 
@@ -113,7 +134,7 @@ __device__ __forceinline__ void commit_group() { asm volatile("cp.async.commit_g
 // epilogue needs more registers than the others)
 template <int EPI> struct GemmOcc { static constexpr int value = EPI == EPI_GELU_BWD ? 2 : 3; };
 
-template <int EPI>
+template <bool TA, bool TB, int EPI>
 __global__ void __launch_bounds__(256, GemmOcc<EPI>::value) k_gemm_tc(GemmArgs g) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __shared__ __align__(8) uint64_t bars[tc::NST];
@@ -137,8 +158,8 @@ __global__ void __launch_bounds__(256, GemmOcc<EPI>::value) k_gemm_tc(GemmArgs g
     // prologue: stages 0 .. NST-2 in flight
     for (int s = 0; s < tc::NST - 1; s++) {
         if (s < nst) {
-            tc::stage(As + s * tc::TILE, g.A, g.lda, m0, g.M, kbeg + s * tc::BK);
-            tc::stage(Bs + s * tc::TILE, g.B, g.ldb, n0, g.N, kbeg + s * tc::BK);
+            tc::stage<TA>(As + s * tc::TILE, g.A, g.lda, m0, g.M, kbeg + s * tc::BK);
+            tc::stage<TB>(Bs + s * tc::TILE, g.B, g.ldb, n0, g.N, kbeg + s * tc::BK);
         }
         tc::commit_group();
     }
@@ -152,12 +173,12 @@ __global__ void __launch_bounds__(256, GemmOcc<EPI>::value) k_gemm_tc(GemmArgs g
             asm volatile("tcgen05.fence::after_thread_sync;\n");
 #pragma unroll
             for (int kk = 0; kk < tc::BK / 16; kk++) {
-                const uint64_t ad = tc::sdesc(tc::smem_u32(As + b * tc::TILE) + kk * 256);
-                const uint64_t bd = tc::sdesc(tc::smem_u32(Bs + b * tc::TILE) + kk * 256);
+                const uint64_t ad = tc::sdesc<TA>(tc::smem_u32(As + b * tc::TILE) + kk * tc::Tile<TA>::KSTEP);
+                const uint64_t bd = tc::sdesc<TB>(tc::smem_u32(Bs + b * tc::TILE) + kk * tc::Tile<TB>::KSTEP);
                 const uint32_t acc = (s > 0 || kk > 0) ? 1u : 0u;
                 asm volatile("{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
                              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-                             :: "r"(tmem), "l"(ad), "l"(bd), "r"(tc::IDESC), "r"(acc));
+                             :: "r"(tmem), "l"(ad), "l"(bd), "r"(tc::Idesc<TA, TB>::value), "r"(acc));
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n"
                          :: "r"(tc::smem_u32(&bars[b])));
@@ -169,8 +190,8 @@ __global__ void __launch_bounds__(256, GemmOcc<EPI>::value) k_gemm_tc(GemmArgs g
                 const bool w = tc::mbar_wait(tc::smem_u32(&bars[(s - 1) % tc::NST]), ((s - 1) / tc::NST) & 1);
                 if (__syncthreads_or(!w)) { ok = false; break; }
             }
-            tc::stage(As + (sn % tc::NST) * tc::TILE, g.A, g.lda, m0, g.M, kbeg + sn * tc::BK);
-            tc::stage(Bs + (sn % tc::NST) * tc::TILE, g.B, g.ldb, n0, g.N, kbeg + sn * tc::BK);
+            tc::stage<TA>(As + (sn % tc::NST) * tc::TILE, g.A, g.lda, m0, g.M, kbeg + sn * tc::BK);
+            tc::stage<TB>(Bs + (sn % tc::NST) * tc::TILE, g.B, g.ldb, n0, g.N, kbeg + sn * tc::BK);
         }
         tc::commit_group();
     }
@@ -229,34 +250,11 @@ __global__ void __launch_bounds__(256, GemmOcc<EPI>::value) k_gemm_tc(GemmArgs g
             }
             uint4 *oo = (uint4 *)(g.out + (size_t)m * g.ldc + n);
             oo[0] = ((const uint4 *)o2)[0]; oo[1] = ((const uint4 *)o2)[1];
-            if (g.outT) {  // lanes hold consecutive m: each column is written as 64 contiguous bytes per warp
-#pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    g.outT[(size_t)(n + 2 * j) * g.ldt + m] = o2[j].x;
-                    g.outT[(size_t)(n + 2 * j + 1) * g.ldt + m] = o2[j].y;
-                }
-            }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(tmem), "r"(tc::TMEM_COLS));
-}
-
-// [rows][cols] -> [cols][rows] (bf16), 32 x 32 tiles through shared memory.
-__global__ void __launch_bounds__(256) k_transpose(int rows, int cols, const bf16 *__restrict__ a,
-                                                   bf16 *__restrict__ t) {
-    __shared__ bf16 tile[32][33];
-    const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
-    for (int k = threadIdx.x; k < 1024; k += 256) {
-        const int r = k >> 5, c = k & 31;
-        if (r0 + r < rows && c0 + c < cols) tile[r][c] = a[(size_t)(r0 + r) * cols + c0 + c];
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < 1024; k += 256) {
-        const int c = k >> 5, r = k & 31;
-        if (r0 + r < rows && c0 + c < cols) t[(size_t)(c0 + c) * rows + r0 + r] = tile[r][c];
-    }
 }
 
 // Output layer (256 -> NOUT) on the CUDA cores: y[b][o] = h[b] . W[o] + bias[o]

@@ -67,7 +67,11 @@ class SolverSettings:
     M 0.52-0.54 on this mesh, where the residual grows again after ~5k
     iterations.)  ``switch_resd`` > 0 runs FP32 down to that level and FP64
     below it (FP32 states stall near 2e-5); it must stay above the freeze
-    level, because frozen limiter values do not carry across precisions."""
+    level, because frozen limiter values do not carry across precisions.
+    ``refreeze_resd`` > 0 stops at that level and continues from the state
+    reached in a new solver whose limiter values are frozen after its first
+    iteration, i.e. recomputed from a nearly converged state: a run then
+    depends less on the state it froze its limiter values on first."""
     cfl: float = 3.0
     freeze: int = 0
     freeze_resd: float = 1e-3
@@ -75,6 +79,7 @@ class SolverSettings:
     limiter: int = 1
     limiter_k: float = 10.0
     switch_resd: float = 0.0
+    refreeze_resd: float = 0.0
 
     def params(self, mach, alpha, maxstep=100000):
         return e2d.default_params(ma=mach, alpha_deg=alpha, cfl=self.cfl, precision=self.precision,
@@ -128,11 +133,21 @@ class Dataset:
 
 
 def train(ds: Dataset, steps: int, batch: int = 65536, nhidden: int = 5, lr: float = 1e-3, seed: int = 3,
-          log=print):
+          lr_final: float | None = None, chunk: int = 250, log=print):
+    """Adam steps on random batches.  With lr_final, the step size follows a
+    cosine from lr down to lr_final, set every `chunk` steps."""
     net = e2d.MLP(nhidden=nhidden, batch=batch, seed=seed, lr=lr)
     net.set_data(ds.x, ds.t)
     t0 = time.perf_counter()
-    loss = net.train(steps)
+    if lr_final is None:
+        loss = net.train(steps)
+    else:
+        parts = []
+        for k0 in range(0, steps, chunk):
+            frac = (k0 + 0.5 * min(chunk, steps - k0)) / steps
+            net.set_lr(lr_final + 0.5 * (lr - lr_final) * (1.0 + np.cos(np.pi * frac)))
+            parts.append(net.train(min(chunk, steps - k0)))
+        loss = np.concatenate(parts)
     dt = time.perf_counter() - t0
     log(f"train: {steps} steps of batch {batch} in {dt:.1f} s, loss {loss[:10].mean():.3e} -> {loss[-100:].mean():.3e}")
     return net, loss, dt
@@ -146,23 +161,48 @@ def predict(net, ds: Dataset, mesh, mach, alpha):
 
 def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=None, epsm=None):
     s = e2d.Solver(mesh, settings.params(mach, alpha, maxstep=maxit))
+    cl0, cd0 = float("nan"), float("nan")
     if w0 is not None:
         s.set_state(w0)
+        cl0, cd0 = s.forces()
     if epsm is not None:
         s.set_residual_norm(epsm)
     t0 = time.perf_counter()
+    stop = max(target, settings.refreeze_resd)
     try:
         if settings.switch_resd > 0.0:
-            h = s.solve_mixed(maxit, target, settings.switch_resd)
+            h = s.solve_mixed(maxit, stop, settings.switch_resd)
         else:
-            h = s.solve(maxit, target)
+            h = s.solve(maxit, stop)
         ok = bool(len(h) and h[-1] <= target)
+        if stop > target and len(h) and h[-1] <= stop and len(h) < maxit:
+            # second freeze: a new solver from the state reached, limiter
+            # values frozen after its first iteration
+            w, norm = s.state(), s.residual_norm()
+            s.close()
+            p2 = settings.params(mach, alpha, maxstep=maxit - len(h))
+            p2.limiter_freeze_resd = 1.0
+            s = e2d.Solver(mesh, p2)
+            s.set_state(w)
+            s.set_residual_norm(norm)
+            h2 = s.solve(maxit - len(h), target)
+            h = np.concatenate([h, h2])
+            ok = bool(len(h2) and h2[-1] <= target)
     except E2DError:
         h, ok = s.history(), False
     wall = time.perf_counter() - t0
     cl, cd = s.forces() if ok else (float("nan"), float("nan"))
+    h = np.asarray(h, np.float64)
+
+    def first_below(level):
+        k = np.flatnonzero(h <= level)
+        return int(k[0]) + 1 if len(k) else None
+
     out = {"iterations": int(len(h)), "wall_s": wall, "converged": ok, "cl": cl, "cd": cd,
-           "first_resd": float(h[0]) if len(h) else float("nan"), "epsm": s.residual_norm()}
+           "first_resd": float(h[0]) if len(h) else float("nan"), "epsm": s.residual_norm(),
+           "start_cl": cl0, "start_cd": cd0,
+           "iterations_to": {f"{lv:.0e}": first_below(lv) for lv in (1e-2, 1e-3, 1e-4, 1e-5)},
+           "history_every_1000": [float(v) for v in h[999::1000]]}
     s.close()
     return out
 
@@ -180,7 +220,10 @@ def evaluate(net, ds, mesh, conds, settings: SolverSettings, target: float, maxi
         rows.append(r)
         log(f"eval M{m:.3f} a{a:+.2f}: free {free['iterations']} its {free['wall_s']:.2f} s | warm "
             f"{warm['iterations']} its {warm['wall_s']:.2f} s (first Resd {warm['first_resd']:.2e}) | "
-            f"x{r['speedup_wall']:.2f} wall, dCL {r['dcl']:.1e} dCD {r['dcd']:.1e}")
+            f"x{r['speedup_wall']:.2f} wall, dCL {r['dcl']:.1e} dCD {r['dcd']:.1e} | predicted CL error "
+            f"{abs(warm['start_cl'] - free['cl']):.1e} | its to 1e-3/1e-4/1e-5 free "
+            f"{'/'.join(str(v) for v in list(free['iterations_to'].values())[1:])} warm "
+            f"{'/'.join(str(v) for v in list(warm['iterations_to'].values())[1:])}")
     return rows
 
 
@@ -194,12 +237,18 @@ def main(argv=None):
     ap.add_argument("--gen-iters", type=int, default=20000)
     ap.add_argument("--steps", type=int, default=20000)
     ap.add_argument("--batch", type=int, default=65536)
+    ap.add_argument("--nhidden", type=int, default=5, help="hidden layers of width 256")
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr-final", type=float, default=None,
+                    help="cosine decay of the Adam step size down to this value (default: constant)")
     ap.add_argument("--target", type=float, default=1e-6)
     ap.add_argument("--maxit", type=int, default=120000)
     ap.add_argument("--mach", type=float, nargs=2, default=(0.575, 0.70))
     ap.add_argument("--alpha", type=float, nargs=2, default=(-1.0, 3.0))
     ap.add_argument("--eval", choices=["fp64", "switch"], default="fp64",
                     help="timed runs in FP64, or FP32 down to 2e-3 and FP64 below")
+    ap.add_argument("--refreeze", type=float, default=0.0,
+                    help="freeze the limiter values again, from the state at this level (0: off)")
     ap.add_argument("--json", default=None)
     args = ap.parse_args(argv)
     log = lambda s: print(s, file=sys.stderr, flush=True)  # noqa: E731
@@ -209,7 +258,8 @@ def main(argv=None):
     gen = SolverSettings(precision=e2d.E2D_FP32)
     states, info = generate(mesh, train_c, gen, args.gen_iters, log=log)
     ds = Dataset(mesh, train_c, states)
-    net, loss, t_train = train(ds, args.steps, args.batch, log=log)
+    net, loss, t_train = train(ds, args.steps, args.batch, nhidden=args.nhidden, lr=args.lr,
+                               lr_final=args.lr_final, log=log)
     # prediction error on the held-out conditions against their FP32 solutions
     held_states, _ = generate(mesh, held_c, gen, args.gen_iters, log=log)
     errs = []
@@ -217,15 +267,17 @@ def main(argv=None):
         p = predict(net, ds, mesh, m, a)
         errs.append(float(np.sqrt(np.mean((p - w) ** 2, axis=0)).max() / np.abs(w).max()))
     log(f"held-out prediction RMS error (max over components, rel. to max |W|): median {np.median(errs):.2e}")
-    ev = SolverSettings(precision=e2d.E2D_FP64, switch_resd=2e-3 if args.eval == "switch" else 0.0)
+    ev = SolverSettings(precision=e2d.E2D_FP64, switch_resd=2e-3 if args.eval == "switch" else 0.0,
+                        refreeze_resd=args.refreeze)
     rows = evaluate(net, ds, mesh, held_c[:args.neval], ev, args.target, args.maxit, log=log)
     conv = [r for r in rows if r["warm"]["converged"] and r["free"]["converged"]]
     summary = {
         "mesh": f"{args.ni}x{args.nj}", "ntrain": args.ntrain, "nheld": args.nheld, "mach": list(args.mach),
-        "alpha": list(args.alpha), "gen_iters": args.gen_iters, "train_steps": args.steps, "batch": args.batch,
+        "alpha": list(args.alpha), "gen_iters": args.gen_iters, "train_steps": args.steps, "batch": args.batch, "nhidden": args.nhidden,
+        "lr": args.lr, "lr_final": args.lr_final,
         "train_seconds": t_train, "final_loss": float(loss[-100:].mean()),
         "heldout_pred_err_median": float(np.median(errs)), "target_drop": args.target,
-        "eval_precision": args.eval, "evaluated": len(rows), "both_converged": len(conv),
+        "eval_precision": args.eval, "refreeze": args.refreeze, "evaluated": len(rows), "both_converged": len(conv),
         "speedup_wall_median": float(np.median([r["speedup_wall"] for r in conv])) if conv else None,
         "speedup_iter_median": float(np.median([r["speedup_iter"] for r in conv])) if conv else None,
         "max_dcl": float(max(r["dcl"] for r in conv)) if conv else None,

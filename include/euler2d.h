@@ -298,6 +298,9 @@ int e2d_mlp_get_params(e2d_mlp *m, float *p);
 int e2d_mlp_set_params(e2d_mlp *m, const float *p);
 /* Training set: x [n * E2D_MLP_INPUTS] normalised inputs, t [n * 4] targets. */
 int e2d_mlp_set_data(e2d_mlp *m, int64_t n, const float *x, const float *t);
+/* Adam step size of the following steps (a schedule is a sequence of calls
+ * between e2d_mlp_train calls); lr >= 0. */
+int e2d_mlp_set_lr(e2d_mlp *m, double lr);
 /* steps Adam steps on random batches; loss[k] (may be NULL) = batch MSE. */
 int e2d_mlp_train(e2d_mlp *m, int32_t steps, double *loss);
 /* y [n * 4] = network(x [n * E2D_MLP_INPUTS]). */

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 import gpueularsolver2d_gb300 as e2d
+from gpueularsolver2d_gb300._lib import E2DError
 
 pytestmark = pytest.mark.gpu
 
@@ -57,3 +58,36 @@ def test_training_reduces_loss_and_forward_agrees(lib):
     y = net.forward(x[:5000])
     mse = float(np.mean((y - t[:5000]) ** 2))
     assert mse < 2.0 * loss[-20:].mean() + 1e-4
+
+
+def test_adam_step_size_is_scheduled_on_device(lib):
+    """e2d_mlp_set_lr changes the step size of the steps that follow: lr 0
+    leaves every parameter as it was; Adam's first step moves each parameter
+    by lr * |g| / (|g| + eps), i.e. by lr wherever the gradient is not tiny,
+    and not at all where it is zero (the padding inputs of the first layer)."""
+    B = 2048
+    rng = np.random.default_rng(1)
+    n = 8192
+    x = np.zeros((n, 32), np.float32)
+    x[:, :22] = rng.uniform(-1, 1, size=(n, 22)).astype(np.float32)
+    t = rng.normal(size=(n, 4)).astype(np.float32)
+    net = e2d.MLP(nhidden=2, batch=B, seed=4, lr=1e-3)
+    net.set_data(x, t)
+    p0 = net.params()
+    net.set_lr(0.0)
+    net.train(3, record_loss=False)
+    assert np.array_equal(net.params(), p0)
+    with pytest.raises(E2DError):
+        net.set_lr(-1.0)
+    net2 = e2d.MLP(nhidden=2, batch=B, seed=4, lr=1.0)
+    net2.set_data(x, t)
+    q0 = net2.params()
+    lr = 1e-3
+    net2.set_lr(lr)
+    net2.train(1, record_loss=False)
+    d = np.abs(net2.params().astype(np.float64) - q0)
+    w0 = d[:256 * 32].reshape(256, 32)
+    assert np.all(w0[:, 22:] == 0.0)
+    assert np.all(d <= lr * (1 + 1e-3) + 1e-6)
+    moved = d[d > 0]
+    assert np.median(np.abs(moved - lr)) < 1e-6, np.median(moved)
