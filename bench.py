@@ -410,15 +410,19 @@ def run_batch64(args):
 
 
 def run_mlp(args):
-    """Training steps of the warm-start MLP (22 -> 5 x 256 GELU -> 4, batch
-    65536 on the BF16 tensor cores, FP32 accumulate): gather, forward, loss,
-    backward and Adam of one step are one CUDA graph.  FLOPs per step: 3 x the
-    forward GEMM FLOPs (forward, data gradient, weight gradient)."""
+    """Training steps of the warm-start MLP (22 features padded to 32 -> L x
+    256 GELU -> 4, batch 65536, BF16 tensor-core GEMMs with FP32 accumulate):
+    gather, forward, loss, backward and Adam of one step are one CUDA graph of
+    6 L + 6 kernels.  FLOPs per step: the tensor-core GEMMs, 2 B (32 * 256 +
+    (L - 1) * 256^2) each for the forward pass and the weight gradients and
+    2 B (L - 1) * 256^2 for the data gradients (the first layer needs none);
+    the 256 -> 4 output layer runs on the CUDA cores and is not counted."""
     import numpy as np
     import torch
     import gpueularsolver2d_gb300 as e2d
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    net = e2d.MLP(nhidden=5, batch=65536, seed=3)
+    L, B = args.mlp_layers, 65536
+    net = e2d.MLP(nhidden=L, batch=B, seed=3)
     rng = np.random.default_rng(0)
     n = 32768 * 64
     x = np.zeros((n, 32), np.float32)
@@ -431,17 +435,17 @@ def run_mlp(args):
     net.train(args.steps, record_loss=False)
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t0) / args.steps
-    flops = 3 * 2 * 65536 * (32 * 256 + 4 * 256 * 256 + 256 * 4)
+    flops = 2 * B * (2 * (32 * 256 + (L - 1) * 256 * 256) + (L - 1) * 256 * 256)
     peak, kind = measured_peak_bf16()
     tf = flops / dt / 1e12
     line = {"metric": "MLP training steps/s (warm-start network, batch 65536)", "value": 1.0 / dt, "unit": "steps/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
             "data": "synthetic (uniform features, normal targets)",
-            "config": {"workload": "MLP 32 -> 5 x 256 GELU -> 4, batch 65536, Adam"},
+            "config": {"workload": f"MLP 32 -> {L} x 256 GELU -> 4, batch {B}, Adam"},
             "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
                          "peak_source": f"{kind} bf16_tflops (MEASURED_PEAKS.json)", "traffic": None},
-            "gpu_launches": None}
+            "gpu_launches": (6 * L + 6) * args.steps}
     print(json.dumps(line), flush=True)
 
 
@@ -472,6 +476,7 @@ def main():
     ap.add_argument("--block", type=int, default=0, help="threads per CTA (0: library default)")
     ap.add_argument("--ordering", choices=sorted(ORDERINGS), default="morton", help="cell order in device memory")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mlp-layers", type=int, default=8, help="hidden layers of the MLP workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -10,12 +10,17 @@ Pipeline (no reference counterpart; the plain solver stays the oracle):
    16 random Fourier features of (x, y); e2d_mlp_features) normalised to zero
    mean / unit variance for the first six, and targets W - W_inf(M, a) scaled
    per component.
-3. ``train``: Adam on random batches, all on the GPU (e2d_mlp_train).
+3. ``train``: Adam on random batches, all on the GPU (e2d_mlp_train), the
+   step size decaying on a cosine (e2d_mlp_set_lr between chunks of steps).
 4. ``predict``: W_inf + scale * MLP(features) for a new condition.
 5. ``evaluate``: for held-out conditions, iterations and wall time to the
    target drop from the free stream and from the prediction, with the same
    solver settings and the same residual normalisation (the free-stream run's
-   first-iteration density change), and the converged CL / CD of both.
+   first-iteration density change), and the converged CL / CD of both.  Both
+   runs freeze the limiter values at Resd 1e-3 and again from the state at
+   1e-5 (``refreeze_resd``): a warm run reaches 1e-3 within a few hundred
+   iterations, on a state that still carries the prediction's error, and
+   values frozen there would keep that error in the converged lift.
 
 Run ``python -m gpueularsolver2d_gb300.warmstart --help``.
 """
@@ -234,20 +239,20 @@ def main(argv=None):
     ap.add_argument("--ntrain", type=int, default=256)
     ap.add_argument("--nheld", type=int, default=32)
     ap.add_argument("--neval", type=int, default=8, help="held-out conditions timed one by one")
-    ap.add_argument("--gen-iters", type=int, default=20000)
-    ap.add_argument("--steps", type=int, default=20000)
+    ap.add_argument("--gen-iters", type=int, default=80000)
+    ap.add_argument("--steps", type=int, default=60000)
     ap.add_argument("--batch", type=int, default=65536)
-    ap.add_argument("--nhidden", type=int, default=5, help="hidden layers of width 256")
+    ap.add_argument("--nhidden", type=int, default=8, help="hidden layers of width 256")
     ap.add_argument("--lr", type=float, default=1e-3)
-    ap.add_argument("--lr-final", type=float, default=None,
-                    help="cosine decay of the Adam step size down to this value (default: constant)")
+    ap.add_argument("--lr-final", type=float, default=1e-5,
+                    help="cosine decay of the Adam step size down to this value (<= 0: constant)")
     ap.add_argument("--target", type=float, default=1e-6)
     ap.add_argument("--maxit", type=int, default=120000)
     ap.add_argument("--mach", type=float, nargs=2, default=(0.575, 0.70))
     ap.add_argument("--alpha", type=float, nargs=2, default=(-1.0, 3.0))
     ap.add_argument("--eval", choices=["fp64", "switch"], default="fp64",
                     help="timed runs in FP64, or FP32 down to 2e-3 and FP64 below")
-    ap.add_argument("--refreeze", type=float, default=0.0,
+    ap.add_argument("--refreeze", type=float, default=1e-5,
                     help="freeze the limiter values again, from the state at this level (0: off)")
     ap.add_argument("--json", default=None)
     args = ap.parse_args(argv)
@@ -259,7 +264,7 @@ def main(argv=None):
     states, info = generate(mesh, train_c, gen, args.gen_iters, log=log)
     ds = Dataset(mesh, train_c, states)
     net, loss, t_train = train(ds, args.steps, args.batch, nhidden=args.nhidden, lr=args.lr,
-                               lr_final=args.lr_final, log=log)
+                               lr_final=args.lr_final if args.lr_final > 0 else None, log=log)
     # prediction error on the held-out conditions against their FP32 solutions
     held_states, _ = generate(mesh, held_c, gen, args.gen_iters, log=log)
     errs = []

@@ -10,7 +10,9 @@ between the two runs, so lift and drag agree within 5e-3 here; on the
 pipeline's 256 x 64 mesh they agree within 1e-4 (the pipeline reports the
 figure).  The residual is the density change of one iteration and
 understates the distance to the steady state (the slowest mode decays by
-~1e-4 per iteration), hence the 1e-8 drop."""
+~1e-4 per iteration), hence the 1e-8 drop.  Training follows the pipeline's
+cosine step-size schedule and both runs freeze the limiter values a second
+time from the state at 1e-5, as the pipeline does."""
 import numpy as np
 import pytest
 
@@ -27,17 +29,21 @@ def test_warm_start_small(lib):
     held = ws.conditions(1, 4, (0.58, 0.68), (-1.0, 3.0))
     states, _ = ws.generate(mesh, train_c + held, gen, 3000, log=lambda s: None)
     ds = ws.Dataset(mesh, train_c, states[:-1])
-    net, loss, _ = ws.train(ds, 600, batch=8192, nhidden=3, lr=2e-3, log=lambda s: None)
+    net, loss, _ = ws.train(ds, 600, batch=8192, nhidden=3, lr=2e-3, lr_final=1e-4, chunk=100,
+                            log=lambda s: None)
+    assert len(loss) == 600
     assert loss[-50:].mean() < 0.2 * loss[:10].mean()
     (m, a), w_true = held[0], states[-1]
     p = ws.predict(net, ds, mesh, m, a)
     err_pred = np.abs(p - w_true).mean()
     err_free = np.abs(ws.freestream(m, a, p.shape[0]) - w_true).mean()
     assert err_pred < 0.5 * err_free, (err_pred, err_free)
-    ev = ws.SolverSettings(cfl=3.0, precision=e2d.E2D_FP64)
+    ev = ws.SolverSettings(cfl=3.0, precision=e2d.E2D_FP64, refreeze_resd=1e-5)
     free = ws.run_to_drop(mesh, m, a, ev, 1e-8, 80000)
     warm = ws.run_to_drop(mesh, m, a, ev, 1e-8, 80000, w0=p, epsm=free["epsm"])
     assert free["converged"] and warm["converged"]
+    for r in (free, warm):  # one history across the two solvers, through 1e-5 to 1e-8
+        assert r["iterations_to"]["1e-05"] is not None and r["iterations_to"]["1e-05"] < r["iterations"]
     assert warm["first_resd"] < 0.5
     assert abs(warm["cl"] - free["cl"]) < 5e-3
     assert abs(warm["cd"] - free["cd"]) < 5e-3
