@@ -65,6 +65,8 @@ template <typename T> struct BatchT : BatchBase {
         const int n = ntot, ncase = (int)L->size();
         bool freeze = false;
         for (auto &p : P) freeze = freeze || p.limiter_freeze > 0 || p.limiter_freeze_resd > 0.0;
+        plan.options = freeze;
+        for (auto &p : P) plan.options = plan.options || p.limiter == 1 || p.global_dt != 0;
         int nmax = 0;
         for (auto &l : *L) nmax = std::max(nmax, l.n);
         const int maxtiles = (n + 31) / 32;

@@ -108,6 +108,7 @@ template <typename T> struct BPlan {
     T rk[8];
     int sweeps;
     int block;               // cells per tile = threads per CTA
+    bool options = true;     // some case uses a scheme option (pass-A option variant)
     int grid;                // CTAs per launch (persistent when < tiles)
 };
 

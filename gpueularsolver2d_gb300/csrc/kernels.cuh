@@ -340,8 +340,11 @@ __device__ __forceinline__ float cell_area<float>(const MeshDev<float> &m, const
     return 0.5f * fmaf(S[1].x, S[2].y, -(S[1].y * S[2].x));
 }
 
-// Returns the cell's local time step (also stored in dt[i]).
-template <typename T>
+// Returns the cell's local time step (also stored in dt[i]).  OPT compiles in
+// the scheme options (smooth limiter, frozen limiter values); without them the
+// reference configuration runs in fewer registers (no spills at the FP32
+// occupancy target) with the same arithmetic.
+template <typename T, bool OPT>
 __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, const int i,
                                         const V4<T> *__restrict__ W, V4<T> *__restrict__ FS,
                                         T *__restrict__ dt, V4<T> *__restrict__ phi, const int frozen) {
@@ -390,7 +393,7 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
         V4<T> o = U;
         if (code[k] >= 0) {
             const V2<T> r = face_offset(m, S, k, i);
-            const bool reuse = phi && frozen;
+            const bool reuse = OPT && phi && frozen;
             V4<T> pf;
             if (reuse) pf = phi[k * n + i];
             T fi = T(1.0), d[4], ph[4];
@@ -399,7 +402,7 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
                 T delt2 = madd(gx[q], r.x, gy[q] * r.y);
                 T u = comp(U, q);
                 if (reuse) fi = comp(pf, q);
-                else if (f.limiter == 1) {
+                else if (OPT && f.limiter == 1) {
                     // Venkatakrishnan on the per-face differences (option)
                     const T e2 = f.venk_k3 * A * tsqrt(A);
                     const T d1 = delt2 > T(0) ? umax[q] - u : umin[q] - u;
@@ -407,15 +410,18 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
                                        : (d1 * d1 + e2 + T(2) * delt2 * d1) /
                                              (d1 * d1 + T(2) * delt2 * delt2 + d1 * delt2 + e2);
                 } else {
-                    if (delt2 > T(0)) fi = tmin((umax[q] - u) / delt2, T(1.0));
-                    if (delt2 < T(0)) fi = tmin((umin[q] - u) / delt2, T(1.0));
-                    if (delt2 == T(0)) fi = T(1.0);
+                    // min(1, (Umax - U) / delt2) for delt2 > 0, min(1, (Umin - U) / delt2)
+                    // for delt2 < 0, 1 for delt2 == 0: the bound is selected first so a
+                    // warp divides once whatever the signs of its lanes.  (A NaN delt2
+                    // makes the face state NaN whatever fi is.)
+                    const T bound = delt2 > T(0) ? umax[q] : umin[q];
+                    fi = delt2 == T(0) ? T(1.0) : tmin((bound - u) / delt2, T(1.0));
                 }
                 ph[q] = fi;
                 d[q] = madd(delt2, fi, u);
             }
             o.x = d[0]; o.y = d[1]; o.z = d[2]; o.w = d[3];
-            if (phi && !frozen) {
+            if (OPT && phi && !frozen) {
                 V4<T> pw;
                 pw.x = ph[0]; pw.y = ph[1]; pw.z = ph[2]; pw.w = ph[3];
                 phi[k * n + i] = pw;
@@ -447,21 +453,28 @@ __device__ __forceinline__ void block_min_dt(double v, unsigned long long *slot)
     }
 }
 
-template <typename T>
+// OPT: the variant with the scheme options (smooth limiter, limiter freezing,
+// global time step); faces_options picks it.
+template <typename T, bool OPT>
 __global__ void E2D_LB_FACES k_faces(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ W,
                                      V4<T> *__restrict__ FS, T *__restrict__ dt,
                                      Ctl *__restrict__ ctl, V4<T> *__restrict__ phi, const int st) {
     wait_prior_grid();
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!f.global_dt) {
+    if (!OPT || !f.global_dt) {
         if (i >= m.n) return;
-        faces_cell(m, f, i, W, FS, dt, phi, phi ? ctl->frozen : 0);
+        faces_cell<T, OPT>(m, f, i, W, FS, dt, phi, OPT && phi ? ctl->frozen : 0);
         return;
     }
     double v = __longlong_as_double((long long)kDtNone);
-    if (i < m.n) v = (double)faces_cell(m, f, i, W, FS, dt, phi, phi ? ctl->frozen : 0);
+    if (i < m.n) v = (double)faces_cell<T, OPT>(m, f, i, W, FS, dt, phi, phi ? ctl->frozen : 0);
     block_min_dt(v, &ctl->dtmin[st]);
+}
+
+// True when a pass-A launch needs the option variant.
+template <typename T> inline bool faces_options(const Flow<T> &f, const void *phi) {
+    return phi != nullptr || f.limiter == 1 || f.global_dt != 0;
 }
 
 // Time step of cell i in RK stage st: its own, or with the global option the
@@ -756,7 +769,7 @@ __device__ __forceinline__ bool batch_cell(const BatchDev<T> &b, const int n, co
     return i < b.case_end[c] && !b.ctl[c].halt;
 }
 
-template <typename T>
+template <typename T, bool OPT>
 __global__ void E2D_LB_FACES kb_faces(MeshDev<T> m, BatchDev<T> b, int ntiles, const V4<T> *__restrict__ W,
                                       V4<T> *__restrict__ FS, T *__restrict__ dt, V4<T> *__restrict__ phi,
                                       const int st) {
@@ -768,9 +781,9 @@ __global__ void E2D_LB_FACES kb_faces(MeshDev<T> m, BatchDev<T> b, int ntiles, c
         int c;
         if (batch_cell(b, m.n, i, c)) {
             const Flow<T> f = b.flows[c];
-            v = (double)faces_cell(m, f, i, W, FS, dt, phi, phi ? b.ctl[c].frozen : 0);
+            v = (double)faces_cell<T, OPT>(m, f, i, W, FS, dt, phi, OPT && phi ? b.ctl[c].frozen : 0);
         }
-        if (b.flows[tc].global_dt) block_min_dt(v, &b.ctl[tc].dtmin[st]);  // uniform over the block
+        if (OPT && b.flows[tc].global_dt) block_min_dt(v, &b.ctl[tc].dtmin[st]);  // uniform over the block
     }
 }
 
@@ -833,7 +846,8 @@ template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream
         const bool last = st == p.stages - 1;
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
-        launch_chained(kb_faces<T>, G, B, s, p.m, p.b, NT, Wcur, p.FS, p.dt, p.phi, st);
+        if (p.options) launch_chained(kb_faces<T, true>, G, B, s, p.m, p.b, NT, Wcur, p.FS, p.dt, p.phi, st);
+        else launch_chained(kb_faces<T, false>, G, B, s, p.m, p.b, NT, Wcur, p.FS, p.dt, p.phi, st);
         launch_chained(kb_flux<T>, G, B, s, p.m, p.b, NT, p.FS, p.res);
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
@@ -888,11 +902,13 @@ void enqueue_export(int n, const int *perm, const V4<T> *W, double *wfile, cudaS
 // next iteration's W0.
 template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
     const int n = p.m.n, B = p.block, G = (n + B - 1) / B;
+    const bool opt = faces_options(p.f, p.phi);
     for (int st = 0; st < p.stages; st++) {
         const bool last = st == p.stages - 1;
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
-        launch_chained(k_faces<T>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
+        if (opt) launch_chained(k_faces<T, true>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
+        else launch_chained(k_faces<T, false>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
         if (FluxTiled<T>::value) launch_chained(k_flux_tile<T>, G, B, s, p.m, p.f, p.FS, p.res, p.ctl);
         else launch_chained(k_flux<T>, G, B, s, p.m, p.f, p.FS, p.res, p.ctl);
         const V4<T> *src = p.res;
@@ -913,6 +929,7 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
 template <typename T>
 int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, int *kind) {
     const int n = p.m.n, B = p.block, G = (n + B - 1) / B;
+    const bool opt = faces_options(p.f, p.phi);
     int j = 0;
     auto mark = [&](int k) { kind[j] = k; cudaEventRecord(ev[2 * j], s); };
     auto done = [&]() { cudaEventRecord(ev[2 * j + 1], s); j++; };
@@ -920,7 +937,10 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
         const bool last = st == p.stages - 1;
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
-        mark(0); k_faces<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st); done();
+        mark(0);
+        if (opt) k_faces<T, true><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
+        else k_faces<T, false><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
+        done();
         mark(1);
         if (FluxTiled<T>::value) k_flux_tile<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
         else k_flux<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
