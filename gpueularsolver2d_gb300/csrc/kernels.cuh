@@ -29,15 +29,18 @@ namespace e2d {
 
 // Occupancy targets (minimum resident 256-thread blocks per SM) of the two
 // gather kernels; the register budget follows from them.  Build-time knobs.
-// 0 leaves the choice to the compiler.  Default 6 (40 registers): the
-// kernels are latency bound, and on the 4.2M-cell mesh 6 beat the compiler's
-// own 48-register choice by 12 % (sweep over 1, 4, 5, 6 at 128 and 256
-// threads per block).
+// 0 leaves the choice to the compiler.  Both kernels are latency bound.
+// Pass A: 6 (40 registers); on the 4.2M-cell mesh 6 beat the compiler's own
+// 48-register choice by 12 % (sweep over 1, 4, 5, 6 at 128 and 256 threads
+// per block).  Pass B requests the inputs of all three faces before its
+// first flux, which needs 63 registers: 4 blocks (99.7 -> 89.2 us per launch
+// against the one-face-at-a-time form at 6 blocks; 94.4 us at 5 blocks,
+// where it spills).
 #ifndef E2D_MINB_FACES
 #define E2D_MINB_FACES 6
 #endif
 #ifndef E2D_MINB_FLUX
-#define E2D_MINB_FLUX 6
+#define E2D_MINB_FLUX 4
 #endif
 // The targets apply to the FP32 kernels; the FP64 (parity) kernels keep two
 // blocks, enough registers for their ~100 live doubles without spilling.
@@ -496,10 +499,19 @@ __device__ __forceinline__ void flux_cell(const MeshDev<T> &m, const Flow<T> &f,
     const int code[3] = {tp.x, tp.y, tp.z};
     V4<T> r;
     r.x = T(0.0); r.y = T(0.0); r.z = T(0.0); r.w = T(0.0);
+    // every input of the three faces is requested before the first flux
+    V2<T> S[3];
+    V4<T> own[3], oth[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        S[k] = m.S[k * n + i];
+        own[k] = FS[k * n + i];
+        if (code[k] >= 0) oth[k] = FS[(code[k] & 3) * n + (code[k] >> 3)];
+    }
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         bool right;
-        const V4<T> F = face_flux(m, f, i, k, code[k], FS, right);
+        const V4<T> F = face_flux_of(f, code[k], S[k], own[k], oth[k], right);
         if (right) { r.x -= F.x; r.y -= F.y; r.z -= F.z; r.w -= F.w; }
         else { r.x += F.x; r.y += F.y; r.z += F.z; r.w += F.w; }
     }
@@ -510,11 +522,8 @@ __device__ __forceinline__ void flux_cell(const MeshDev<T> &m, const Flow<T> &f,
 // reference's Res_e.left of gpu_solver.cu:738-745); *right tells whether cell
 // i is the edge's right cell.
 template <typename T>
-__device__ __forceinline__ V4<T> face_flux(const MeshDev<T> &m, const Flow<T> &f, const int i, const int k,
-                                           const int code, const V4<T> *__restrict__ FS, bool &right) {
-    const int n = m.n;
-    const V2<T> S = m.S[k * n + i];
-    const V4<T> own = FS[k * n + i];
+__device__ __forceinline__ V4<T> face_flux_of(const Flow<T> &f, const int code, const V2<T> S, const V4<T> own,
+                                              const V4<T> oth, bool &right) {
     const T vn = tsqrt(S.y * S.y + S.x * S.x);
     T nx = S.x / vn, ny = S.y / vn;
     // one Roe call site for every face, with the left state first: both cells
@@ -524,7 +533,6 @@ __device__ __forceinline__ V4<T> face_flux(const MeshDev<T> &m, const Flow<T> &f
     V4<T> a = own, b;
     right = false;
     if (code >= 0) {
-        const V4<T> oth = FS[(code & 3) * n + (code >> 3)];
         right = (code >> 2) & 1;
         if (right) { a = oth; b = own; nx = -nx; ny = -ny; }
         else b = oth;
@@ -534,6 +542,17 @@ __device__ __forceinline__ V4<T> face_flux(const MeshDev<T> &m, const Flow<T> &f
     V4<T> F = roe(a, b, nx, ny, f.gamma, f.eps_entropy);
     F.x *= vn; F.y *= vn; F.z *= vn; F.w *= vn;
     return F;
+}
+
+template <typename T>
+__device__ __forceinline__ V4<T> face_flux(const MeshDev<T> &m, const Flow<T> &f, const int i, const int k,
+                                           const int code, const V4<T> *__restrict__ FS, bool &right) {
+    const int n = m.n;
+    const V2<T> S = m.S[k * n + i];
+    const V4<T> own = FS[k * n + i];
+    V4<T> oth = own;
+    if (code >= 0) oth = FS[(code & 3) * n + (code >> 3)];
+    return face_flux_of(f, code, S, own, oth, right);
 }
 
 // Pass B for one tile of cells [base, base + nvalid) with each interior face
