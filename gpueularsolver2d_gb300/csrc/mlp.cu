@@ -512,19 +512,21 @@ int e2d_wall_distance(e2d_mesh *mesh, double wall_box, double *d) {
                                        mesh->y[t.en2[e] - 1]));
     const int n = mesh->ncell;
     if (seg.empty()) { for (int i = 0; i < n; i++) d[i] = 1e300; return E2D_OK; }
-    double *px, *py, *dd;
-    double4 *sg;
-    CK(cudaMalloc((void **)&px, sizeof(double) * n));
-    CK(cudaMalloc((void **)&py, sizeof(double) * n));
-    CK(cudaMalloc((void **)&dd, sizeof(double) * n));
-    CK(cudaMalloc((void **)&sg, sizeof(double4) * seg.size()));
-    CK(cudaMemcpy(px, t.cx.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(py, t.cy.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(sg, seg.data(), sizeof(double4) * seg.size(), cudaMemcpyHostToDevice));
-    k_wall_distance<<<(n + 255) / 256, 256>>>(n, px, py, (int)seg.size(), sg, dd);
-    cudaError_t e = cudaMemcpy(d, dd, sizeof(double) * n, cudaMemcpyDeviceToHost);
-    cudaFree(px); cudaFree(py); cudaFree(dd); cudaFree(sg);
-    if (e != cudaSuccess) { set_error(std::string("wall distance: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
+    struct Bufs {  // freed on every return path
+        double *px = nullptr, *py = nullptr, *dd = nullptr;
+        double4 *sg = nullptr;
+        ~Bufs() { cudaFree(px); cudaFree(py); cudaFree(dd); cudaFree(sg); }
+    } b;
+    CK(cudaMalloc((void **)&b.px, sizeof(double) * n));
+    CK(cudaMalloc((void **)&b.py, sizeof(double) * n));
+    CK(cudaMalloc((void **)&b.dd, sizeof(double) * n));
+    CK(cudaMalloc((void **)&b.sg, sizeof(double4) * seg.size()));
+    CK(cudaMemcpy(b.px, t.cx.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b.py, t.cy.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b.sg, seg.data(), sizeof(double4) * seg.size(), cudaMemcpyHostToDevice));
+    k_wall_distance<<<(n + 255) / 256, 256>>>(n, b.px, b.py, (int)seg.size(), b.sg, b.dd);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(d, b.dd, sizeof(double) * n, cudaMemcpyDeviceToHost));
     return E2D_OK;
 }
 

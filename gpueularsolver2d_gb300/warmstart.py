@@ -174,6 +174,7 @@ def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=N
         s.set_residual_norm(epsm)
     t0 = time.perf_counter()
     stop = max(target, settings.refreeze_resd)
+    h1 = np.zeros(0)  # history of the first solver once the second one runs
     try:
         if settings.switch_resd > 0.0:
             h = s.solve_mixed(maxit, stop, settings.switch_resd)
@@ -184,6 +185,7 @@ def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=N
             # second freeze: a new solver from the state reached, limiter
             # values frozen after its first iteration
             w, norm = s.state(), s.residual_norm()
+            h1 = np.asarray(h, np.float64)
             s.close()
             p2 = settings.params(mach, alpha, maxstep=maxit - len(h))
             p2.limiter_freeze_resd = 1.0
@@ -191,10 +193,10 @@ def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=N
             s.set_state(w)
             s.set_residual_norm(norm)
             h2 = s.solve(maxit - len(h), target)
-            h = np.concatenate([h, h2])
+            h = np.concatenate([h1, h2])
             ok = bool(len(h2) and h2[-1] <= target)
     except E2DError:
-        h, ok = s.history(), False
+        h, ok = np.concatenate([h1, s.history()]), False
     wall = time.perf_counter() - t0
     cl, cd = s.forces() if ok else (float("nan"), float("nan"))
     h = np.asarray(h, np.float64)
