@@ -345,7 +345,11 @@ int e2d_batch_create(e2d_mesh **meshes, const e2d_params *params, int32_t ncase,
     const e2d_params &p0 = params[0];
     for (int c = 0; c < ncase; c++) {
         const e2d_params &p = params[c];
-        if (!meshes[c] || !valid_params(&p)) { set_error("invalid mesh or parameters of case " + std::to_string(c)); return E2D_ERR_ARG; }
+        if (!meshes[c]) { set_error("null mesh of case " + std::to_string(c)); return E2D_ERR_ARG; }
+        if (const char *why = param_error(&p)) {
+            set_error("invalid parameters of case " + std::to_string(c) + ": " + why);
+            return E2D_ERR_ARG;
+        }
         bool same = p.precision == p0.precision && p.rk_stages == p0.rk_stages && p.irs_sweeps == p0.irs_sweeps &&
                     p.irs_eps == p0.irs_eps && p.gamma == p0.gamma && p.entropy_eps == p0.entropy_eps &&
                     p.dt_cap == p0.dt_cap && std::memcmp(p.rk_coef, p0.rk_coef, sizeof p.rk_coef) == 0;
@@ -435,7 +439,7 @@ int e2d_batch_step(e2d_batch *b, int32_t n) {
 }
 
 int e2d_batch_solve(e2d_batch *b, int32_t max_steps, double epsl, int32_t *nsteps) {
-    if (!b || max_steps < 0) { set_error("bad argument"); return E2D_ERR_ARG; }
+    if (!b || max_steps < 0 || std::isnan(epsl)) { set_error("bad argument"); return E2D_ERR_ARG; }
     int maxstep = 0;
     for (int c = 0; c < b->ncase; c++) maxstep = std::max(maxstep, b->ctl_host[c].step);
     if (maxstep + max_steps > b->hist_cap) { set_error("iterations beyond the residual history capacity (maxstep)"); return E2D_ERR_CAPACITY; }

@@ -18,6 +18,7 @@
 
 #include "dev_types.h"
 #include "internal.h"
+#include "solver_internal.h"
 
 namespace {
 
@@ -71,9 +72,8 @@ extern "C" int e2d_step_noalloc(int32_t ncell, const int32_t *topo, const double
                        std::to_string(E2D_NOALLOC_MAX_CELLS) + " cells");
         return E2D_ERR_CAPACITY;
     }
-    if (p->rk_stages < 1 || p->rk_stages > 8 || p->irs_sweeps < 0 || p->irs_sweeps > 16 ||
-        !(p->gamma > 1.0) || !(p->ma > 0.0) || !(p->tin > 0.0)) {
-        e2d::set_error("e2d_step_noalloc: invalid parameters");
+    if (const char *why = e2d::param_error(p)) {
+        e2d::set_error(std::string("e2d_step_noalloc: invalid parameters: ") + why);
         return E2D_ERR_ARG;
     }
     if (((uintptr_t)topo | (uintptr_t)S | (uintptr_t)R) % 16 || (uintptr_t)w % 32 || (uintptr_t)area % 8 ||

@@ -143,18 +143,35 @@ void keep_in_l2(cudaGraph_t g, const void *base, size_t bytes) {
     cudaGetLastError();  // a GPU without the feature keeps the default policy
 }
 
-bool valid_params(const e2d_params *p) {
-    if (!(p->gamma > 1.0) || !(p->ma > 0.0) || !(p->tin > 0.0) || !(p->cfl > 0.0)) return false;
-    if (p->rk_stages < 1 || p->rk_stages > 8 || p->irs_sweeps < 0 || p->irs_sweeps > 16) return false;
-    if (p->precision != E2D_FP64 && p->precision != E2D_FP32) return false;
-    if (p->ordering != E2D_ORDER_FILE && p->ordering != E2D_ORDER_MORTON && p->ordering != E2D_ORDER_RCM) return false;
-    if (p->block_size != 0 && (p->block_size < 32 || p->block_size > 256 || p->block_size % 32)) return false;
-    if (p->graph_iters < 0 || p->graph_iters > 256) return false;
-    if (p->limiter_freeze < 0) return false;
-    if (p->limiter != E2D_LIMITER_REFERENCE && p->limiter != E2D_LIMITER_VENKAT) return false;
-    if (p->limiter == E2D_LIMITER_VENKAT && !(p->limiter_k > 0.0)) return false;
-    if ((p->global_dt != 0 && p->global_dt != 1) || (p->far_field_fix != 0 && p->far_field_fix != 1)) return false;
-    return true;
+// Null when the parameters are usable, else which one is not.
+const char *param_error(const e2d_params *p) {
+    if (!(p->gamma > 1.0)) return "gamma must be > 1";
+    if (!(p->ma > 0.0)) return "ma must be > 0";
+    if (!(p->tin > 0.0)) return "tin must be > 0";
+    if (!(p->cfl > 0.0)) return "cfl must be > 0";
+    if (std::isnan(p->epsl)) return "epsl must not be NaN";
+    if (p->maxstep < 0) return "maxstep must be >= 0";
+    if (p->rk_stages < 1 || p->rk_stages > 8) return "rk_stages must be 1..8";
+    for (int k = 0; k < p->rk_stages; k++)
+        if (!std::isfinite(p->rk_coef[k])) return "rk_coef must be finite";
+    if (p->irs_sweeps < 0 || p->irs_sweeps > 16) return "irs_sweeps must be 0..16";
+    if (!(p->irs_eps >= 0.0) || !std::isfinite(p->irs_eps)) return "irs_eps must be finite and >= 0";
+    if (!(p->dt_cap > 0.0)) return "dt_cap must be > 0";
+    if (!(p->entropy_eps > 0.0)) return "entropy_eps must be > 0";
+    if (!(p->wall_box > 0.0)) return "wall_box must be > 0";
+    if (p->precision != E2D_FP64 && p->precision != E2D_FP32) return "precision must be E2D_FP64 or E2D_FP32";
+    if (p->ordering != E2D_ORDER_FILE && p->ordering != E2D_ORDER_MORTON && p->ordering != E2D_ORDER_RCM)
+        return "ordering must be E2D_ORDER_FILE, _MORTON or _RCM";
+    if (p->block_size != 0 && (p->block_size < 32 || p->block_size > 256 || p->block_size % 32))
+        return "block_size must be 0 or a multiple of 32 in 32..256";
+    if (p->graph_iters < 0 || p->graph_iters > 256) return "graph_iters must be 0..256";
+    if (p->limiter_freeze < 0) return "limiter_freeze must be >= 0";
+    if (p->limiter != E2D_LIMITER_REFERENCE && p->limiter != E2D_LIMITER_VENKAT)
+        return "limiter must be E2D_LIMITER_REFERENCE or E2D_LIMITER_VENKAT";
+    if (p->limiter == E2D_LIMITER_VENKAT && !(p->limiter_k > 0.0)) return "limiter_k must be > 0";
+    if (p->global_dt != 0 && p->global_dt != 1) return "global_dt must be 0 or 1";
+    if (p->far_field_fix != 0 && p->far_field_fix != 1) return "far_field_fix must be 0 or 1";
+    return nullptr;
 }
 
 struct SolverBase {
@@ -445,7 +462,7 @@ extern "C" {
 int e2d_solver_create(e2d_mesh *m, const e2d_params *p, e2d_solver **out) {
     if (!m || !p || !out) { set_error("null argument"); return E2D_ERR_ARG; }
     *out = nullptr;
-    if (!valid_params(p)) { set_error("invalid parameters"); return E2D_ERR_ARG; }
+    if (const char *why = param_error(p)) { set_error(std::string("invalid parameters: ") + why); return E2D_ERR_ARG; }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
         cudaGetLastError();
@@ -492,7 +509,7 @@ int e2d_step(e2d_solver *s, int32_t n) {
 }
 
 int e2d_solve(e2d_solver *s, int32_t max_steps, double epsl, double *resid_history, int32_t *nsteps) {
-    if (!s || max_steps < 0) { set_error("bad argument"); return E2D_ERR_ARG; }
+    if (!s || max_steps < 0 || std::isnan(epsl)) { set_error("bad argument"); return E2D_ERR_ARG; }
     const int step0 = s->ctl_host->step;
     int rc = E2D_OK;
     // gpu_solver.cu:2200: while (step < MAXSTEP && Resd[step] > EPSL)

@@ -37,7 +37,8 @@ void forces_from_state(const HostLayout &L, const FreeStream &fs, double gamma, 
                        double *cl, double *cd);
 
 // Parameter checks shared by the solver constructors.
-bool valid_params(const e2d_params *p);
+// Null when the parameters are usable, else which one is not.
+const char *param_error(const e2d_params *p);
 
 // Marks [base, base + bytes) as persisting in L2 for every kernel node of a
 // captured graph (the cell topology, which all four passes read).

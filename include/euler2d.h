@@ -165,7 +165,10 @@ int e2d_mesh_order(e2d_mesh *m, int32_t ordering, int32_t *perm);
 /* ---- solver ----------------------------------------------------------- */
 /* Set-up + device upload + free-stream state (gpu_init.cu:63-93,
  * gpu_solver.cu:2187-2194); replaces Initialization, Cuda_Init and the
- * set-up half of ROE_SOLVER.  Uses the current CUDA device. */
+ * set-up half of ROE_SOLVER.  Uses the current CUDA device.  Parameters out
+ * of range (see e2d_params; also gamma <= 1, ma, tin, cfl, dt_cap,
+ * entropy_eps or wall_box <= 0, irs_eps < 0, a non-finite coefficient or a
+ * NaN epsl) give E2D_ERR_ARG, with the parameter named by e2d_last_error. */
 int e2d_solver_create(e2d_mesh *m, const e2d_params *p, e2d_solver **out);
 void e2d_solver_destroy(e2d_solver *s);
 /* Iterates like ROE_SOLVER (gpu_solver.cu:2200-2434): stops when

@@ -164,3 +164,45 @@ def test_truncated_mesh_file(lib):
         with pytest.raises(_lib.E2DError) as ei:
             e2d.Mesh.read(p)
         assert ei.value.code == -2
+
+
+@pytest.mark.parametrize("field,value,why", [
+    ("gamma", 1.0, "gamma"), ("ma", float("nan"), "ma"), ("cfl", 0.0, "cfl"),
+    ("epsl", float("nan"), "epsl"), ("maxstep", -1, "maxstep"), ("rk_stages", 0, "rk_stages"),
+    ("rk_coef", [0.25, float("inf"), 0.5, 1.0], "rk_coef"), ("irs_sweeps", 17, "irs_sweeps"),
+    ("irs_eps", -0.1, "irs_eps"), ("irs_eps", float("inf"), "irs_eps"), ("dt_cap", 0.0, "dt_cap"),
+    ("entropy_eps", 0.0, "entropy_eps"), ("wall_box", -2.0, "wall_box"), ("precision", 2, "precision"),
+    ("ordering", 3, "ordering"), ("block_size", 48, "block_size"), ("graph_iters", 300, "graph_iters"),
+    ("limiter_freeze", -1, "limiter_freeze"), ("limiter", 2, "limiter"), ("global_dt", 2, "global_dt"),
+    ("far_field_fix", -1, "far_field_fix"),
+])
+def test_invalid_parameters_are_named(lib, field, value, why):
+    """Every rejected parameter is reported by name, before any device work
+    (so these run without a GPU)."""
+    mesh = e2d.Mesh.ogrid(16, 4)
+    with pytest.raises(_lib.E2DError) as ei:
+        e2d.Solver(mesh, e2d.default_params(**{field: value}))
+    assert ei.value.code == -1 and f"invalid parameters: {why}" in str(ei.value)
+    with pytest.raises(_lib.E2DError) as ei:
+        e2d.Batch([mesh, mesh], [e2d.default_params(), e2d.default_params(**{field: value})])
+    assert ei.value.code == -1 and f"invalid parameters of case 1: {why}" in str(ei.value)
+
+
+def test_smooth_limiter_needs_positive_k(lib):
+    mesh = e2d.Mesh.ogrid(16, 4)
+    with pytest.raises(_lib.E2DError, match="limiter_k"):
+        e2d.Solver(mesh, e2d.default_params(limiter=1, limiter_k=0.0))
+
+
+def test_valid_parameters_pass_validation(lib):
+    """The reference defaults and the options at their documented values get
+    past validation: without a GPU the failure is then the missing device."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("checks the no-device error path")
+    mesh = e2d.Mesh.ogrid(16, 4)
+    for kw in [{}, dict(precision=e2d.E2D_FP32, ordering=e2d.E2D_ORDER_RCM, limiter=1, limiter_k=10.0,
+                        limiter_freeze_resd=1e-3, global_dt=1, far_field_fix=1, irs_eps=0.0, irs_sweeps=0)]:
+        with pytest.raises(_lib.E2DError) as ei:
+            e2d.Solver(mesh, e2d.default_params(**kw))
+        assert ei.value.code != -1, str(ei.value)
