@@ -206,3 +206,38 @@ def test_valid_parameters_pass_validation(lib):
         with pytest.raises(_lib.E2DError) as ei:
             e2d.Solver(mesh, e2d.default_params(**kw))
         assert ei.value.code != -1, str(ei.value)
+
+
+def test_ogrid_geometry(lib):
+    """NACA 0012 O-grid: wall nodes on the closed-trailing-edge thickness
+    curve, far-field nodes on the circle of radius 20 about mid-chord, first
+    radial spacing 2e-3 chord, geometric stretching (constant ratio of
+    consecutive radial steps), and interior nodes moved by the jitter at most
+    5 % of their smallest neighbour distance in each coordinate (wall and far
+    field not moved)."""
+    ni, nj = 128, 32
+    x, y, _ = e2d.Mesh.ogrid(ni, nj, seed=3, jitter=0.0).nodes()
+    X, Y = x.reshape(nj + 1, ni), y.reshape(nj + 1, ni)
+    xw = X[0]
+    thick = 0.6 * (0.2969 * np.sqrt(xw) - 0.1260 * xw - 0.3516 * xw ** 2 + 0.2843 * xw ** 3 - 0.1036 * xw ** 4)
+    assert xw.min() >= 0.0 and xw.max() <= 1.0
+    np.testing.assert_allclose(np.abs(Y[0]), np.where((np.arange(ni) == 0) | (2 * np.arange(ni) == ni), 0.0, thick),
+                               atol=1e-15)
+    np.testing.assert_allclose(np.hypot(X[nj] - 0.5, Y[nj]), 20.0, rtol=1e-12)
+    step = np.hypot(np.diff(X, axis=0), np.diff(Y, axis=0))  # [nj, ni] radial steps
+    assert np.all(np.abs(step[0] - 2e-3) < 0.05 * 2e-3), (step[0].min(), step[0].max())
+    ratio = step[1:] / step[:-1]
+    np.testing.assert_allclose(ratio, ratio[0, 0], rtol=1e-9)
+    assert 1.0 < ratio[0, 0] < 1.5
+    xj, yj, _ = e2d.Mesh.ogrid(ni, nj, seed=3, jitter=0.05).nodes()
+    XJ, YJ = xj.reshape(nj + 1, ni), yj.reshape(nj + 1, ni)
+    assert np.array_equal(XJ[[0, nj]], X[[0, nj]]) and np.array_equal(YJ[[0, nj]], Y[[0, nj]])
+    # smallest distance to the four structured neighbours of each interior node
+    h = np.full((nj - 1, ni), np.inf)
+    for di, dj in [(1, 0), (-1, 0), (0, 1), (0, -1)]:
+        xs = np.roll(X, -di, axis=1)[1 + dj:nj + dj]
+        ys = np.roll(Y, -di, axis=1)[1 + dj:nj + dj]
+        h = np.minimum(h, np.hypot(xs - X[1:nj], ys - Y[1:nj]))
+    dx, dy = np.abs(XJ[1:nj] - X[1:nj]), np.abs(YJ[1:nj] - Y[1:nj])
+    assert np.all(dx <= 0.05 * h * (1 + 1e-12)) and np.all(dy <= 0.05 * h * (1 + 1e-12))
+    assert dx.max() > 0.02 * h[np.unravel_index(dx.argmax(), dx.shape)]  # the jitter is there
