@@ -6,7 +6,8 @@ C++ host code (csrc/), their build (build.py) and a thin ctypes view of the
 C ABI (api.py) used by the tests and the benchmark.
 """
 from .api import (E2D_FP32, E2D_FP64, E2D_ORDER_FILE, E2D_ORDER_MORTON, E2D_ORDER_RCM, MLP, Batch, Mesh, Params,
-                  Solver, default_params, read_input)
+                  Solver, default_params, read_input, state_integrals)
 
-__all__ = ["Mesh", "Solver", "Batch", "MLP", "Params", "default_params", "read_input", "E2D_FP32", "E2D_FP64",
+__all__ = ["Mesh", "Solver", "Batch", "MLP", "Params", "default_params", "read_input", "state_integrals",
+           "E2D_FP32", "E2D_FP64",
            "E2D_ORDER_FILE", "E2D_ORDER_MORTON", "E2D_ORDER_RCM"]

@@ -45,6 +45,14 @@ class MeshInfo(ctypes.Structure):
                 ("nwall", ctypes.c_int32), ("nfar", ctypes.c_int32)]
 
 
+class Integrals(ctypes.Structure):
+    """Mirror of ``e2d_integrals`` in include/euler2d.h."""
+    _fields_ = [(n, ctypes.c_double) for n in ("cl", "cd", "mass", "mass_flux_far", "mass_flux_wall")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int32
 _D = ctypes.c_double
@@ -79,6 +87,8 @@ SIGNATURES = {
     "e2d_get_state": (_I, [_P, _PD]),
     "e2d_set_state": (_I, [_P, _PD]),
     "e2d_forces": (_I, [_P, _PD, _PD]),
+    "e2d_solver_integrals": (_I, [_P, ctypes.POINTER(Integrals)]),
+    "e2d_state_integrals": (_I, [_P, ctypes.POINTER(Params), _PD, ctypes.POINTER(Integrals)]),
     "e2d_write_residual_plt": (_I, [_P, ctypes.c_char_p]),
     "e2d_write_field_plt": (_I, [_P, _P, ctypes.c_char_p]),
     "e2d_write_wall_cp_plt": (_I, [_P, _P, ctypes.c_char_p]),

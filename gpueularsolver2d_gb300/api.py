@@ -40,6 +40,18 @@ def default_params(**kw) -> Params:
     return p
 
 
+def state_integrals(mesh: "Mesh", params: Params, w) -> dict:
+    """FP64 integrals (cl, cd, mass, mass_flux_far, mass_flux_wall) of a state
+    [ncell, 4] in the mesh's cell order, computed on the host (no GPU)."""
+    from ._lib import Integrals
+    w = np.ascontiguousarray(w, np.float64)
+    if w.size != 4 * mesh.info(params.wall_box).ncell:
+        raise ValueError("need a [ncell, 4] state")
+    out = Integrals()
+    check(load().e2d_state_integrals(mesh._h, ctypes.byref(params), _dp(w), ctypes.byref(out)))
+    return out.as_dict()
+
+
 def read_input(path: str, p: Params | None = None) -> Params:
     p = p or default_params()
     check(load().e2d_input_read(path.encode(), ctypes.byref(p)))
@@ -194,6 +206,14 @@ class Solver:
         cd = ctypes.c_double()
         check(load().e2d_forces(self._h, ctypes.byref(cl), ctypes.byref(cd)))
         return cl.value, cd.value
+
+    def integrals(self) -> dict:
+        """FP64 integrals of the current state: cl, cd, mass, mass_flux_far,
+        mass_flux_wall (e2d_integrals)."""
+        from ._lib import Integrals
+        out = Integrals()
+        check(load().e2d_solver_integrals(self._h, ctypes.byref(out)))
+        return out.as_dict()
 
     def write_residual_plt(self, path: str) -> None:
         check(load().e2d_write_residual_plt(self._h, path.encode()))

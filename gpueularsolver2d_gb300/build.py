@@ -36,6 +36,7 @@ UNITS = {
     "batch.o": ("batch.cu", ["nvcc", *NVCC_COMMON]),
     "mlp.o": ("mlp.cu", ["nvcc", *NVCC_COMMON]),
     "resid.o": ("resid.cu", ["nvcc", *NVCC_COMMON]),
+    "integrals.o": ("integrals.cu", ["nvcc", *NVCC_COMMON]),  # host code only
     "kernels_f64.o": ("kernels_f64.cu", ["nvcc", *NVCC_COMMON, "--fmad=false"]),
     "noalloc.o": ("noalloc.cu", ["nvcc", *NVCC_COMMON, "--fmad=false"]),
     # FP32 stencil: no multiply-add contraction either, so every inlined copy

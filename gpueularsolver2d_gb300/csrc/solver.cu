@@ -596,6 +596,15 @@ int e2d_forces(e2d_solver *s, double *cl, double *cd) {
     return E2D_OK;
 }
 
+int e2d_solver_integrals(e2d_solver *s, e2d_integrals *out) {
+    if (!s || !out) { set_error("null argument"); return E2D_ERR_ARG; }
+    std::vector<double> w(4 * (size_t)s->L.n);
+    int rc = e2d_get_state(s, w.data());
+    if (rc) return rc;
+    integrals_from_state(s->L, s->fs, s->prm, w.data(), out);
+    return E2D_OK;
+}
+
 int e2d_write_residual_plt(e2d_solver *s, const char *path) {
     if (!s || !path) { set_error("null argument"); return E2D_ERR_ARG; }
     FILE *fp = std::fopen(path, "w");

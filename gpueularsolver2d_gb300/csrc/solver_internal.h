@@ -36,6 +36,11 @@ int build_layout(e2d_mesh *m, const e2d_params &p, HostLayout &L);
 void forces_from_state(const HostLayout &L, const FreeStream &fs, double gamma, const double *w_file,
                        double *cl, double *cd);
 
+// CL, CD, total mass and boundary mass fluxes of a file-order state (see
+// e2d_integrals), all in FP64.
+void integrals_from_state(const HostLayout &L, const FreeStream &fs, const e2d_params &p, const double *w_file,
+                          e2d_integrals *out);
+
 // Parameter checks shared by the solver constructors.
 // Null when the parameters are usable, else which one is not.
 const char *param_error(const e2d_params *p);

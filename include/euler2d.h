@@ -194,6 +194,27 @@ int e2d_set_state(e2d_solver *s, const double *w);
  * 0.5 rho_inf V_inf^2 c = 0.5), accumulated in FP64.  No reference
  * counterpart. */
 int e2d_forces(e2d_solver *s, double *cl, double *cd);
+/* FP64 integrals of a conserved state.  No reference counterpart.
+ *   cl, cd          as e2d_forces;
+ *   mass            sum over cells of rho * area;
+ *   mass_flux_far   mass leaving through the far-field faces per unit time:
+ *                   the scheme's first-order boundary flux (far-field ghost,
+ *                   gpu_solver.cu:62-135, and the Roe flux, 569-647) times
+ *                   the face length, summed;
+ *   mass_flux_wall  the same through the wall faces (slip-wall ghost,
+ *                   gpu_solver.cu:188-221).
+ * Interior faces cancel in the sum of the cell residuals, so the mass
+ * residual summed over the cells is mass_flux_far + mass_flux_wall, which
+ * tends to zero as the solution becomes steady. */
+typedef struct e2d_integrals {
+    double cl, cd, mass, mass_flux_far, mass_flux_wall;
+} e2d_integrals;
+/* Of the solver's current state. */
+int e2d_solver_integrals(e2d_solver *s, e2d_integrals *out);
+/* Of a state w [ncell * 4] in the file's cell order on a mesh with the given
+ * parameters (free stream, gamma, entropy fix, wall box, far-field option);
+ * needs no GPU. */
+int e2d_state_integrals(e2d_mesh *m, const e2d_params *p, const double *w, e2d_integrals *out);
 /* unresidual.plt as the reference writes it (gpu_fvm.cu:165-175): every
  * 100th step. */
 int e2d_write_residual_plt(e2d_solver *s, const char *path);
