@@ -325,6 +325,10 @@ def run_gpu(args, rank: int, world: int):
             fp_err[key] = {"max_rel_linf": float(np.max(np.abs(w32 - w64)) / np.max(np.abs(w64))),
                            "median_rel": float(np.median(np.abs(w32 - w64) / np.abs(w64).max(axis=0))),
                            "resid_max_rel": float(np.max(np.abs(h32 - h64) / h64))}
+            try:
+                fp_err[key]["integrals"] = integral_errors(a32.integrals(), a64.integrals())
+            except Exception as exc:  # an auxiliary report: keep the bench line, say why it is missing
+                fp_err[key]["integrals"] = {"error": str(exc)}
         a32.close()
         a64.close()
 
@@ -447,6 +451,13 @@ def run_mlp(args):
                          "peak_source": f"{kind} bf16_tflops (MEASURED_PEAKS.json)", "traffic": None},
             "gpu_launches": (6 * L + 6) * args.steps}
     print(json.dumps(line), flush=True)
+
+
+def integral_errors(i32: dict, i64: dict) -> dict:
+    """FP64 integrals (e2d_integrals) of the FP32 run against those of the FP64
+    run: both values and their absolute difference."""
+    return {k: {"fp32": i32[k], "fp64": i64[k], "abs_err": abs(i32[k] - i64[k])}
+            for k in ("cl", "cd", "mass", "mass_flux_far", "mass_flux_wall")}
 
 
 def args_sweeps_count(params) -> int:

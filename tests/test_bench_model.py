@@ -49,3 +49,12 @@ def test_traffic_from_committed_profiles(kernel):
 
 def test_unknown_kernel_has_no_traffic():
     assert bench.traffic_from_profiles("nonexistent", 1000) is None
+
+
+def test_integral_errors():
+    i32 = {"cl": 0.25, "cd": 0.01, "mass": 1000.0, "mass_flux_far": 1e-3, "mass_flux_wall": 0.0}
+    i64 = {"cl": 0.2501, "cd": 0.0101, "mass": 1000.0, "mass_flux_far": 2e-3, "mass_flux_wall": 1e-17}
+    e = bench.integral_errors(i32, i64)
+    assert set(e) == set(i32)
+    assert e["cl"]["abs_err"] == pytest.approx(1e-4) and e["mass"]["abs_err"] == 0.0
+    assert e["mass_flux_far"] == {"fp32": 1e-3, "fp64": 2e-3, "abs_err": 1e-3}
