@@ -20,7 +20,10 @@ Pipeline (no reference counterpart; the plain solver stays the oracle):
    runs freeze the limiter values at Resd 1e-3 and again from the state at
    1e-5 (``refreeze_resd``): a warm run reaches 1e-3 within a few hundred
    iterations, on a state that still carries the prediction's error, and
-   values frozen there would keep that error in the converged lift.
+   values frozen there would keep that error in the converged lift.  The free
+   stream is the fallback (``run_warm``): a prediction that is not physical in
+   every cell is not used, and a warm run that diverges is run again from the
+   free stream, with the failed attempt's cost counted.
 
 Run ``python -m gpueularsolver2d_gb300.warmstart --help``.
 """
@@ -175,6 +178,7 @@ def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=N
     t0 = time.perf_counter()
     stop = max(target, settings.refreeze_resd)
     h1 = np.zeros(0)  # history of the first solver once the second one runs
+    error = None
     try:
         if settings.switch_resd > 0.0:
             h = s.solve_mixed(maxit, stop, settings.switch_resd)
@@ -195,8 +199,8 @@ def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=N
             h2 = s.solve(maxit - len(h), target)
             h = np.concatenate([h1, h2])
             ok = bool(len(h2) and h2[-1] <= target)
-    except E2DError:
-        h, ok = np.concatenate([h1, s.history()]), False
+    except E2DError as exc:
+        h, ok, error = np.concatenate([h1, s.history()]), False, str(exc)
     wall = time.perf_counter() - t0
     cl, cd = s.forces() if ok else (float("nan"), float("nan"))
     h = np.asarray(h, np.float64)
@@ -205,7 +209,7 @@ def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=N
         k = np.flatnonzero(h <= level)
         return int(k[0]) + 1 if len(k) else None
 
-    out = {"iterations": int(len(h)), "wall_s": wall, "converged": ok, "cl": cl, "cd": cd,
+    out = {"iterations": int(len(h)), "wall_s": wall, "converged": ok, "error": error, "cl": cl, "cd": cd,
            "first_resd": float(h[0]) if len(h) else float("nan"), "epsm": s.residual_norm(),
            "start_cl": cl0, "start_cd": cd0,
            "iterations_to": {f"{lv:.0e}": first_below(lv) for lv in (1e-2, 1e-3, 1e-4, 1e-5)},
@@ -214,12 +218,43 @@ def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=N
     return out
 
 
+def physical(w, gamma: float = GAMMA) -> bool:
+    """Every cell finite with positive density and pressure."""
+    w = np.asarray(w, np.float64)
+    if not np.all(np.isfinite(w)) or not np.all(w[:, 0] > 0):
+        return False
+    p = (gamma - 1.0) * (w[:, 3] - 0.5 * (w[:, 1] ** 2 + w[:, 2] ** 2) / w[:, 0])
+    return bool(np.all(p > 0))
+
+
+def run_warm(mesh, mach, alpha, settings: SolverSettings, target, maxit, w_pred, epsm=None):
+    """The plain solver from a predicted state, with the free stream as the
+    fallback: a prediction that is not physical in every cell is not used, and
+    a warm run that stops with an error (diverged) is run again from the free
+    stream, its iterations and time counted with the fallback's.  ``fallback``
+    in the result says which, or is None."""
+    if not physical(w_pred):
+        out = run_to_drop(mesh, mach, alpha, settings, target, maxit, epsm=epsm)
+        out["fallback"] = "prediction not physical"
+        return out
+    warm = run_to_drop(mesh, mach, alpha, settings, target, maxit, w0=w_pred, epsm=epsm)
+    if warm["error"] is None:
+        warm["fallback"] = None
+        return warm
+    free = run_to_drop(mesh, mach, alpha, settings, target, maxit, epsm=epsm)
+    free["iterations"] += warm["iterations"]
+    free["wall_s"] += warm["wall_s"]
+    free["start_cl"], free["start_cd"] = warm["start_cl"], warm["start_cd"]
+    free["fallback"] = f"warm run failed: {warm['error']}"
+    return free
+
+
 def evaluate(net, ds, mesh, conds, settings: SolverSettings, target: float, maxit: int, log=print):
     rows = []
     for m, a in conds:
         free = run_to_drop(mesh, m, a, settings, target, maxit)
         warm_state = predict(net, ds, mesh, m, a)
-        warm = run_to_drop(mesh, m, a, settings, target, maxit, w0=warm_state, epsm=free["epsm"])
+        warm = run_warm(mesh, m, a, settings, target, maxit, warm_state, epsm=free["epsm"])
         r = {"mach": m, "alpha": a, "free": free, "warm": warm,
              "speedup_wall": free["wall_s"] / warm["wall_s"] if warm["converged"] else float("nan"),
              "speedup_iter": free["iterations"] / max(1, warm["iterations"]) if warm["converged"] else float("nan"),
@@ -230,7 +265,8 @@ def evaluate(net, ds, mesh, conds, settings: SolverSettings, target: float, maxi
             f"x{r['speedup_wall']:.2f} wall, dCL {r['dcl']:.1e} dCD {r['dcd']:.1e} | predicted CL error "
             f"{abs(warm['start_cl'] - free['cl']):.1e} | its to 1e-3/1e-4/1e-5 free "
             f"{'/'.join(str(v) for v in list(free['iterations_to'].values())[1:])} warm "
-            f"{'/'.join(str(v) for v in list(warm['iterations_to'].values())[1:])}")
+            f"{'/'.join(str(v) for v in list(warm['iterations_to'].values())[1:])}"
+            + (f" | fallback: {warm['fallback']}" if warm["fallback"] else ""))
     return rows
 
 
@@ -285,6 +321,7 @@ def main(argv=None):
         "train_seconds": t_train, "final_loss": float(loss[-100:].mean()),
         "heldout_pred_err_median": float(np.median(errs)), "target_drop": args.target,
         "eval_precision": args.eval, "refreeze": args.refreeze, "evaluated": len(rows), "both_converged": len(conv),
+        "fallbacks": sum(1 for r in rows if r["warm"]["fallback"]),
         "speedup_wall_median": float(np.median([r["speedup_wall"] for r in conv])) if conv else None,
         "speedup_iter_median": float(np.median([r["speedup_iter"] for r in conv])) if conv else None,
         "max_dcl": float(max(r["dcl"] for r in conv)) if conv else None,

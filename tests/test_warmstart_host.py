@@ -169,3 +169,47 @@ def test_constant_step_size_without_lr_final(lib, monkeypatch):
     monkeypatch.setattr(ws.e2d, "MLP", FakeMLP)
     net, loss, _ = ws.train(FakeDataset(), 700, batch=2048, lr=2e-3, log=lambda s: None)
     assert net.lrs == [] and net.chunks == [700] and net.lr0 == 2e-3 and len(loss) == 700
+
+
+def test_physical():
+    w = ws.freestream(0.6, 1.0, 10)
+    assert ws.physical(w)
+    for i, v in [(0, 0.0), (0, float("nan")), (3, 0.1), (1, float("inf"))]:
+        bad = w.copy()
+        bad[4, i] = v
+        assert not ws.physical(bad), (i, v)
+
+
+def test_warm_run_without_fallback(lib, fake_solver):
+    settings = ws.SolverSettings(precision=e2d.E2D_FP64)
+    out = ws.run_warm(None, 0.6, 1.0, settings, 1e-8, 5000, ws.freestream(0.6, 1.0, 4), epsm=2.0)
+    assert out["fallback"] is None and out["converged"]
+    assert len(fake_solver.created) == 1 and fake_solver.created[0].state_in is not None
+
+
+def test_unphysical_prediction_falls_back_to_the_free_stream(lib, fake_solver):
+    settings = ws.SolverSettings(precision=e2d.E2D_FP64)
+    w = ws.freestream(0.6, 1.0, 4)
+    w[2, 0] = -1.0
+    out = ws.run_warm(None, 0.6, 1.0, settings, 1e-8, 5000, w, epsm=2.0)
+    assert out["fallback"] == "prediction not physical" and out["converged"]
+    (only,) = fake_solver.created
+    assert only.state_in is None and only.norm == 2.0  # started from the free stream, same normalisation
+
+
+def test_diverged_warm_run_falls_back_and_counts_its_cost(lib, fake_solver, monkeypatch):
+    class DivergeFirst(FakeSolver):
+        def solve(self, max_steps, epsl):
+            if len(FakeSolver.created) == 1:  # the warm run: 40 iterations, then diverges
+                self.hist = [0.5] * 40
+                raise E2DError(DIVERGED, "diverged")
+            return super().solve(max_steps, epsl)
+
+    monkeypatch.setattr(ws.e2d, "Solver", DivergeFirst)
+    settings = ws.SolverSettings(precision=e2d.E2D_FP64)
+    out = ws.run_warm(None, 0.6, 1.0, settings, 1e-8, 5000, ws.freestream(0.6, 1.0, 4), epsm=2.0)
+    warm, free = FakeSolver.created
+    assert warm.state_in is not None and free.state_in is None
+    assert out["fallback"].startswith("warm run failed") and out["converged"]
+    assert out["iterations"] == 40 + len(free.hist)
+    assert out["start_cl"] == 0.25  # the prediction's, from the warm attempt
