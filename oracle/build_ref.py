@@ -21,10 +21,11 @@ accommodations and no edit to any source line:
 ``gpu_fvm.cu``'s ``main`` is renamed ``ref_main`` with ``-Dmain=ref_main`` so
 the harness can call the whole program.
 
-Sources are taken from ``$E2D_REFERENCE`` (default: the read-only reference
-checkout) and a byte-identical copy is kept under ``_ref/src`` (git-ignored)
-so that the same recipe can build the harness on a machine without the
-checkout.
+Sources are taken from the directory named by ``$E2D_REFERENCE`` or, when
+that is unset, from a reference checkout beside the repository
+(``../reference``); a byte-identical copy is kept under ``_ref/src``
+(git-ignored) so that the same recipe can build the harness on a machine
+without the checkout.  ``source_dir()`` is the one place that resolves it.
 """
 from __future__ import annotations
 
@@ -44,8 +45,16 @@ REF_MESHES = ["2822-3k.dat", "2822-1w.dat", "2822-5w.dat"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
-def _source_dir() -> str | None:
-    ref = os.environ.get("E2D_REFERENCE", "/root/reference")
+def checkout_dir() -> str:
+    """The reference checkout: ``$E2D_REFERENCE``, else ``../reference``
+    beside the repository."""
+    return os.environ.get("E2D_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
+def source_dir() -> str | None:
+    """Directory holding the reference sources: the checkout when present
+    (staging a copy under ``_ref/src``), else that staged copy, else None."""
+    ref = checkout_dir()
     if all(os.path.exists(os.path.join(ref, f)) for f in REF_FILES):
         stage = os.path.join(OUT, "src")
         os.makedirs(stage, exist_ok=True)
@@ -100,7 +109,7 @@ def _compile(src: str, obj: str, flags: list[str], keep: str) -> None:
 
 def build(force: bool = False) -> str | None:
     """Build ``oracle/_ref/ref_harness``; returns its path or None without sources."""
-    src_dir = _source_dir()
+    src_dir = source_dir()
     if src_dir is None:
         return None
     exe = os.path.join(OUT, "ref_harness")
@@ -119,11 +128,18 @@ def build(force: bool = False) -> str | None:
         "gpu_fvm.o": (os.path.join(src_dir, "gpu_fvm.cu"), common + ["-Dmain=ref_main"]),
         "gpu_solver.o": (os.path.join(src_dir, "gpu_solver.cu"), common),
     }
-    with ThreadPoolExecutor(len(jobs)) as ex:
-        futs = [ex.submit(_compile, s, os.path.join(OUT, o), fl, os.path.join(OUT, "tmp_" + o[:-2]))
-                for o, (s, fl) in jobs.items()]
-        for fu in futs:
-            fu.result()
+    keeps = [os.path.join(OUT, "tmp_" + o[:-2]) for o in jobs]
+    try:
+        with ThreadPoolExecutor(len(jobs)) as ex:
+            futs = [ex.submit(_compile, s, os.path.join(OUT, o), fl, k)
+                    for (o, (s, fl)), k in zip(jobs.items(), keeps)]
+            for fu in futs:
+                fu.result()
+    finally:
+        # nvcc's intermediates (preprocessed text, compiler-written device
+        # code) are needed only while the objects are made: none stays behind
+        for k in keeps:
+            shutil.rmtree(k, ignore_errors=True)
     harness_o = os.path.join(OUT, "ref_harness.o")
     subprocess.run(["nvcc", *ARCH, "-O2", f"-I{src_dir}", "-Xcompiler", "-ffp-contract=off", "-w",
                     "-c", os.path.join(HERE, "ref_harness.cu"), "-o", harness_o], check=True)

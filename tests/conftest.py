@@ -7,7 +7,6 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-REFERENCE = os.environ.get("E2D_REFERENCE", "/root/reference")
 
 
 def pytest_configure(config):
@@ -31,7 +30,8 @@ def oracle():
 
 def reference_mesh(name: str) -> str | None:
     """A mesh shipped with the reference checkout, if it is present here."""
-    for d in (REFERENCE, os.path.join(ROOT, "oracle", "_ref", "src")):
+    import build_ref  # oracle/build_ref.py: resolves the checkout or its staged copy
+    for d in (build_ref.checkout_dir(), os.path.join(ROOT, "oracle", "_ref", "src")):
         p = os.path.join(d, name)
         if os.path.exists(p):
             return p

@@ -85,11 +85,8 @@ def test_compat_missing_mesh_exits_like_reference(lib):
 
 @pytest.mark.gpu
 def test_reference_main_runs_on_gb300_solver(lib):
-    src = None
-    for cand in ("/root/reference", os.path.join(ROOT, "oracle", "_ref", "src")):
-        if os.path.exists(os.path.join(cand, "gpu_fvm.cu")):
-            src = cand
-            break
+    import build_ref  # oracle/build_ref.py
+    src = build_ref.source_dir()
     if src is None:
         pytest.skip("reference sources not available")
     mesh = e2d.Mesh.ogrid(48, 12, seed=8)
