@@ -56,6 +56,23 @@ __global__ void k_noalloc_ctl(Ctl *ctl, int target, double epsm) {
     for (int k = 0; k < 8; k++) ctl->dtmin[k] = kDtNone;
 }
 
+// Every face code of the caller's topology must name a cell of this mesh (or
+// be -1 / -2) before any pass gathers through it: a code out of range sets
+// halt = 3, which makes every later kernel of the call return at once.
+__global__ void k_noalloc_check(int n, const int4 *__restrict__ topo, Ctl *ctl) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int4 t = topo[i];
+    bool bad = t.w < 0 || t.w > 3;
+    const int code[3] = {t.x, t.y, t.z};
+    for (int k = 0; k < 3; k++) {
+        const int c = code[k];
+        if (c >= 0) bad = bad || (c >> 3) >= n || (c & 3) > 2;
+        else bad = bad || (c != -1 && c != -2);
+    }
+    if (bad) ctl->halt = 3;
+}
+
 size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 }  // namespace
@@ -76,10 +93,28 @@ extern "C" int e2d_step_noalloc(int32_t ncell, const int32_t *topo, const double
         e2d::set_error(std::string("e2d_step_noalloc: invalid parameters: ") + why);
         return E2D_ERR_ARG;
     }
+    // options this entry point does not carry: refused rather than ignored, so
+    // that a call never silently computes something other than e2d_step
+    if (p->precision != E2D_FP64) {
+        e2d::set_error("e2d_step_noalloc: only precision E2D_FP64 is supported");
+        return E2D_ERR_ARG;
+    }
+    if (p->limiter_freeze > 0 || p->limiter_freeze_resd > 0.0) {
+        e2d::set_error("e2d_step_noalloc: limiter_freeze and limiter_freeze_resd are not supported (must be 0)");
+        return E2D_ERR_ARG;
+    }
     if (((uintptr_t)topo | (uintptr_t)S | (uintptr_t)R) % 16 || (uintptr_t)w % 32 || (uintptr_t)area % 8 ||
         (uintptr_t)resid % 8) {
-        e2d::set_error("e2d_step_noalloc: topo, S and R must be 16-byte aligned and w 32-byte aligned");
+        e2d::set_error("e2d_step_noalloc: topo, S and R must be 16-byte aligned, w 32-byte aligned, "
+                       "area and resid 8-byte aligned");
         return E2D_ERR_ARG;
+    }
+    // an error left pending by earlier work belongs to its caller: report it
+    // without clearing it, and do not take it for one of this call's launches
+    if (cudaError_t pending = cudaPeekAtLastError()) {
+        e2d::set_error(std::string("e2d_step_noalloc: a CUDA error was pending before the call: ") +
+                       cudaGetErrorString(pending));
+        return E2D_ERR_CUDA;
     }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
@@ -135,6 +170,7 @@ extern "C" int e2d_step_noalloc(int32_t ncell, const int32_t *topo, const double
     plan.sweeps = p->irs_sweeps;
     plan.block = block;
     k_noalloc_ctl<<<1, 1, 0, s>>>(plan.ctl, iterations, *epsm);
+    k_noalloc_check<<<G, block, 0, s>>>(n, plan.m.topo, plan.ctl);
     for (int it = 0; it < iterations; it++) e2d::enqueue_iteration<double>(plan, s);
     cudaError_t e = cudaGetLastError();
     Ctl c;
@@ -143,6 +179,12 @@ extern "C" int e2d_step_noalloc(int32_t ncell, const int32_t *topo, const double
     if (e != cudaSuccess) {
         e2d::set_error(std::string("e2d_step_noalloc: ") + cudaGetErrorString(e));
         return E2D_ERR_CUDA;
+    }
+    if (c.halt == 3) {
+        e2d::set_error("e2d_step_noalloc: topo holds a face code out of range (a neighbour outside [0, ncell), "
+                       "a slot above 2, a negative code other than -1 / -2, or a neighbour count outside 0..3); "
+                       "nothing was computed");
+        return E2D_ERR_ARG;
     }
     *epsm = c.epsm;
     if (c.halt == 2) {

@@ -365,9 +365,21 @@ int e2d_wall_distance(e2d_mesh *m, double wall_box, double *d);
  *   S    [6n] double, 16-byte aligned: S[2(k n + i) + {0,1}] = (vectory,
  *        vectorx) of face k in cell i's own node order (gpu_init.cu:153-154);
  *   R    [6n] double, 16-byte aligned: face midpoint minus cell centroid;
- *   area [n]  double;
+ *   area [n]  double, 8-byte aligned;
+ * every neighbour index nb must lie in [0, ncell) and every slot in 0..2: the
+ * call checks the codes on the GPU before any pass reads through them and
+ * returns E2D_ERR_ARG, with nothing computed, when one is out of range;
  * the state w [4n] (rho, rho u, rho v, rho E per cell, 32-byte aligned),
- * advanced in place, and resid [iterations] receiving Resd of each iteration.
+ * advanced in place, and resid [iterations] (8-byte aligned) receiving Resd of
+ * each iteration.
+ *
+ * Parameters: the scheme fields of e2d_params act as in e2d_step, except
+ * that precision must be E2D_FP64 and limiter_freeze / limiter_freeze_resd
+ * must be 0 (E2D_ERR_ARG otherwise: the limiter-freeze buffer is not part of
+ * the fixed array).  ordering, block_size and graph_iters are not used: the
+ * cells stay in the caller's order and every pass runs 128 threads per block
+ * (launch shapes do not change the result).  A CUDA error left pending by earlier work is reported as
+ * E2D_ERR_CUDA before anything is launched, and is not cleared.
  * *epsm is the residual normalisation: <= 0 on entry takes drou of this call's
  * first iteration (gpu_solver.cu:2428); the value used is returned in *epsm,
  * so passing it back continues one residual history across calls.

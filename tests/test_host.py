@@ -241,3 +241,32 @@ def test_ogrid_geometry(lib):
     dx, dy = np.abs(XJ[1:nj] - X[1:nj]), np.abs(YJ[1:nj] - Y[1:nj])
     assert np.all(dx <= 0.05 * h * (1 + 1e-12)) and np.all(dy <= 0.05 * h * (1 + 1e-12))
     assert dx.max() > 0.02 * h[np.unravel_index(dx.argmax(), dx.shape)]  # the jitter is there
+
+
+@pytest.mark.parametrize("kw,why", [
+    (dict(precision=1), "only precision E2D_FP64"),
+    (dict(limiter_freeze=3), "limiter_freeze and limiter_freeze_resd are not supported"),
+    (dict(limiter_freeze_resd=1e-3), "limiter_freeze and limiter_freeze_resd are not supported"),
+    (dict(cfl=0.0), "invalid parameters: cfl"),
+])
+def test_step_noalloc_refuses_options_it_does_not_carry(lib, kw, why):
+    """The allocation-free entry point refuses, by name and before touching
+    any pointer or device, the options that it cannot honour (FP32 stencil,
+    limiter freezing) instead of ignoring them; the pointers here are never
+    dereferenced."""
+    import ctypes
+    p = e2d.default_params(**kw)
+    fake = ctypes.c_void_p(1 << 20)  # non-null and aligned; refused before any use
+    epsm = ctypes.c_double(0.0)
+    rc = lib.e2d_step_noalloc(64, fake, fake, fake, fake, ctypes.byref(p), 1, fake, fake, ctypes.byref(epsm), None)
+    assert rc == -1 and why in lib.e2d_last_error().decode()
+
+
+def test_step_noalloc_names_every_alignment(lib):
+    import ctypes
+    p = e2d.default_params()
+    ok, odd = ctypes.c_void_p(1 << 20), ctypes.c_void_p((1 << 20) + 4)
+    epsm = ctypes.c_double(0.0)
+    rc = lib.e2d_step_noalloc(64, ok, ok, ok, odd, ctypes.byref(p), 1, ok, ok, ctypes.byref(epsm), None)
+    msg = lib.e2d_last_error().decode()
+    assert rc == -1 and "area and resid 8-byte aligned" in msg
