@@ -231,8 +231,10 @@ def run_warm(mesh, mach, alpha, settings: SolverSettings, target, maxit, w_pred,
     """The plain solver from a predicted state, with the free stream as the
     fallback: a prediction that is not physical in every cell is not used, and
     a warm run that stops with an error (diverged) is run again from the free
-    stream, its iterations and time counted with the fallback's.  ``fallback``
-    in the result says which, or is None."""
+    stream, its iterations and time counted with the fallback's (in
+    ``iterations``, ``wall_s`` and every ``iterations_to`` entry; the attempt
+    alone in ``failed_attempt``).  ``fallback`` in the result says which, or
+    is None."""
     if not physical(w_pred):
         out = run_to_drop(mesh, mach, alpha, settings, target, maxit, epsm=epsm)
         out["fallback"] = "prediction not physical"
@@ -242,8 +244,13 @@ def run_warm(mesh, mach, alpha, settings: SolverSettings, target, maxit, w_pred,
         warm["fallback"] = None
         return warm
     free = run_to_drop(mesh, mach, alpha, settings, target, maxit, epsm=epsm)
+    # every count of the result includes the failed attempt's cost; the
+    # attempt's own figures are kept beside them
+    free["failed_attempt"] = {"iterations": warm["iterations"], "wall_s": warm["wall_s"]}
     free["iterations"] += warm["iterations"]
     free["wall_s"] += warm["wall_s"]
+    free["iterations_to"] = {k: (v + warm["iterations"] if v is not None else None)
+                             for k, v in free["iterations_to"].items()}
     free["start_cl"], free["start_cd"] = warm["start_cl"], warm["start_cd"]
     free["fallback"] = f"warm run failed: {warm['error']}"
     return free

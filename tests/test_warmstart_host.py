@@ -212,4 +212,8 @@ def test_diverged_warm_run_falls_back_and_counts_its_cost(lib, fake_solver, monk
     assert warm.state_in is not None and free.state_in is None
     assert out["fallback"].startswith("warm run failed") and out["converged"]
     assert out["iterations"] == 40 + len(free.hist)
+    assert out["failed_attempt"]["iterations"] == 40
+    # levels reached count the failed attempt's iterations too
+    assert all(v is None or v > 40 for v in out["iterations_to"].values())
+    assert out["iterations_to"]["1e-05"] > 40
     assert out["start_cl"] == 0.25  # the prediction's, from the warm attempt
