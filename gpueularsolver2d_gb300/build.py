@@ -1,9 +1,12 @@
 """Build ``libeuler2d.so`` (and the ``e2d_solve`` command) for sm_103a in-tree.
 
 nvcc cross-compiles without a GPU, so this runs on any machine with the CUDA
-13 toolkit.  Translation units are compiled in parallel; the FP64 kernels are
-compiled without FMA contraction so that they reproduce the CPU oracle bit for
-bit, the FP32 kernels with contraction and fast division / square root.
+13 toolkit.  Translation units are compiled in parallel.  Both stencil
+precisions are compiled without multiply-add contraction (``--fmad=false``):
+the FP64 kernels so that they reproduce the CPU oracle bit for bit, the FP32
+kernels so that every inlined copy of a device function rounds alike (their
+fused multiply-adds are explicit ``fmaf`` calls); the FP32 kernels use fast
+division / square root and flush denormals.
 Host code is compiled with ``-ffp-contract=off`` so the set-up geometry is the
 same IEEE arithmetic on x86-64 and aarch64.
 """

@@ -1,7 +1,11 @@
 // kernels_f32.cu -- FP32-stencil instantiation of the solve-path kernels
 // (geometry is computed in FP64 on the host and stored as float; the
-// residual norm is accumulated in FP64).  Built with FMA contraction and
-// fast (non-IEEE) division and square root.
+// residual norm is accumulated in FP64).  Built without multiply-add
+// contraction (--fmad=false: every inlined copy of a device function rounds
+// the same way, so both cells of a face and a batched case and its
+// single-case run get the same bits); the FP32 flux and spectral radius fuse
+// explicitly with fmaf.  Division and square root are the fast (non-IEEE)
+// forms, denormals flush to zero.
 #include "kernels.cuh"
 
 namespace e2d {
