@@ -949,3 +949,114 @@ void or_rcm_perm(const or_case *c, int *perm) {
     for (int k = 0; k < N; k++) perm[k] = order[N - 1 - k];
     free(order); free(seen); free(cand);
 }
+
+/* ------------------------------------------------------------------ */
+/* NACA 0012 O-grid (no reference counterpart: it writes the reference's */
+/* mesh format, gpu_init.cu:16-32).  A second statement of the          */
+/* library's generator, so that the CPU arm of the benchmark and tests  */
+/* can make the same mesh without loading the product library.          */
+/* ------------------------------------------------------------------ */
+
+/* splitmix64 finaliser */
+static uint64_t og_mix(uint64_t z) {
+    z += 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+/* uniform [0, 1) with 53 random bits; stream 1/2 jitter x/y, 3 diagonals */
+static double og_unit(uint64_t seed, uint64_t stream, uint64_t idx) {
+    const uint64_t h = og_mix(seed ^ og_mix(stream * 0x632be59bd9b4e019ULL + idx));
+    return (double)(h >> 11) * (1.0 / 9007199254740992.0);
+}
+
+/* half thickness of NACA 0012 with the closed trailing edge (a4 = -0.1036) */
+static double og_thick(double x) {
+    if (x < 0.0) x = 0.0;
+    if (x > 1.0) x = 1.0;
+    return 0.6 * (0.2969 * sqrt(x) - 0.1260 * x - 0.3516 * x * x + 0.2843 * x * x * x -
+                  0.1036 * x * x * x * x);
+}
+
+/* total of nj geometric steps of first size ds0 and ratio r */
+static double og_total(double ds0, double r, int nj) { return ds0 * (pow(r, nj) - 1.0) / (r - 1.0); }
+
+int or_ogrid_naca0012(int ni, int nj, double r_far, double dy_wall, double jitter, uint64_t seed,
+                      double *x, double *y, int *tri) {
+    if (ni < 8 || nj < 1 || r_far <= 1.0 || dy_wall <= 0 || jitter < 0 || jitter >= 0.25) {
+        set_err("ogrid: need ni>=8, nj>=1, r_far>1, dy_wall>0, 0<=jitter<0.25");
+        return -1;
+    }
+    const double pi = 3.14159265358979323846;
+    double *wx = xcalloc(ni, sizeof(double)), *wy = xcalloc(ni, sizeof(double));
+    double *fx = xcalloc(ni, sizeof(double)), *fy = xcalloc(ni, sizeof(double));
+    double *s = xcalloc(nj + 1, sizeof(double));
+    /* wall points from the trailing edge around the upper surface, far-field
+       circle about mid-chord at the same angles */
+    for (int i = 0; i < ni; i++) {
+        const double th = 2.0 * pi * i / ni, xw = 0.5 * (1.0 + cos(th));
+        wx[i] = xw;
+        wy[i] = (i == 0 || 2 * i == ni) ? 0.0 : (2 * i <= ni ? 1.0 : -1.0) * og_thick(xw);
+        fx[i] = 0.5 + r_far * cos(th);
+        fy[i] = r_far * sin(th);
+    }
+    /* radial fractions: geometric steps whose first is dy_wall/(r_far-0.5),
+       ratio found by 200 bisections */
+    double ds0 = dy_wall / (r_far - 0.5), ratio = 1.0;
+    if (ds0 * nj < 1.0) {
+        double lo = 1.0, hi = 2.0;
+        while (og_total(ds0, hi, nj) < 1.0) hi *= 2.0;
+        for (int it = 0; it < 200; it++) {
+            const double mid = 0.5 * (lo + hi);
+            if (og_total(ds0, mid, nj) < 1.0) lo = mid; else hi = mid;
+        }
+        ratio = 0.5 * (lo + hi);
+    } else {
+        ds0 = 1.0 / nj;
+    }
+    s[0] = 0.0;
+    for (int j = 1; j <= nj; j++) s[j] = s[j - 1] + ds0 * pow(ratio, j - 1);
+    for (int j = 0; j <= nj; j++) s[j] /= s[nj];
+    /* nodes: row j = ni points; interior rows jittered by up to `jitter`
+       times the distance to the nearest structured neighbour */
+    for (int j = 0; j <= nj; j++)
+        for (int i = 0; i < ni; i++) {
+            double px = wx[i] + s[j] * (fx[i] - wx[i]);
+            double py = wy[i] + s[j] * (fy[i] - wy[i]);
+            if (j > 0 && j < nj && jitter > 0) {
+                const int di[4] = {1, -1, 0, 0}, dj[4] = {0, 0, 1, -1};
+                double h = 1e300;
+                for (int q = 0; q < 4; q++) {
+                    const int ii = (i + di[q] + ni) % ni, jj = j + dj[q];
+                    const double qx = wx[ii] + s[jj] * (fx[ii] - wx[ii]);
+                    const double qy = wy[ii] + s[jj] * (fy[ii] - wy[ii]);
+                    const double d = hypot(qx - px, qy - py);
+                    if (d < h) h = d;
+                }
+                const uint64_t idx = (uint64_t)j * ni + i;
+                px += jitter * h * (2.0 * og_unit(seed, 1, idx) - 1.0);
+                py += jitter * h * (2.0 * og_unit(seed, 2, idx) - 1.0);
+            }
+            x[(size_t)j * ni + i] = px;
+            y[(size_t)j * ni + i] = py;
+        }
+    /* two counter-clockwise triangles per quad, split along a seeded diagonal */
+    int *t = tri;
+    for (int j = 0; j < nj; j++)
+        for (int i = 0; i < ni; i++) {
+            const int a = j * ni + i + 1, b = j * ni + (i + 1) % ni + 1;
+            const int c = (j + 1) * ni + (i + 1) % ni + 1, d = (j + 1) * ni + i + 1;
+            const int q[2][6] = {{a, d, c, a, c, b}, {a, d, b, b, d, c}};
+            const int pick = og_unit(seed, 3, (uint64_t)j * ni + i) < 0.5 ? 0 : 1;
+            memcpy(t, q[pick], sizeof q[pick]);
+            t += 6;
+        }
+    free(wx); free(wy); free(fx); free(fy); free(s);
+    for (int cc = 0; cc < 2 * ni * nj; cc++) {
+        const int *p = tri + 3 * cc;
+        const double ar = calc_area(x[p[0] - 1], y[p[0] - 1], x[p[1] - 1], y[p[1] - 1], x[p[2] - 1], y[p[2] - 1]);
+        if (!(ar > 0.0)) { set_err("ogrid: generated a non-positive cell; lower the jitter"); return -2; }
+    }
+    return 0;
+}

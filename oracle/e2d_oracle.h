@@ -20,6 +20,8 @@
 #ifndef E2D_ORACLE_H
 #define E2D_ORACLE_H
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -113,6 +115,16 @@ void or_roe_flux(const double lw[4], const double rw[4], double nx, double ny,
                  double gamma, double entropy_eps, double flux[4]);
 void or_far_ghost(const double dw[4], double vectorx, double vectory,
                   const or_case *c, double out[4]);
+
+/* NACA 0012 O-grid of ni (around) x nj (radial) quads, each split into two
+ * counter-clockwise triangles along a seeded diagonal; far-field circle of
+ * radius r_far about mid-chord, first radial spacing dy_wall, interior nodes
+ * jittered by up to `jitter` of their nearest-neighbour distance.  Writes
+ * x, y [ni*(nj+1)] and tri [6*ni*nj] (1-based node ids).  Returns 0, or < 0
+ * with or_last_error() set.  The same mesh, bit for bit, as the library's
+ * e2d_mesh_ogrid_naca0012 with the same arguments. */
+int or_ogrid_naca0012(int ni, int nj, double r_far, double dy_wall, double jitter, uint64_t seed,
+                      double *x, double *y, int *tri);
 
 /* Threads used by OpenMP loops (1 when built without OpenMP). */
 int or_threads(void);

@@ -59,6 +59,8 @@ def lib() -> ctypes.CDLL:
             "or_far_ghost": [dp, ctypes.c_double, ctypes.c_double, vp, dp],
         }.items():
             getattr(L, name).argtypes = args
+        L.or_ogrid_naca0012.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_uint64, dp, dp, ip]
         L.or_pis.restype = ctypes.c_double
         L.or_pis.argtypes = [vp]
         L.or_step_count.argtypes = [vp]
@@ -178,6 +180,18 @@ class Case:
                 self._h = None
         except Exception:
             pass
+
+
+def ogrid(ni: int, nj: int, r_far: float = 20.0, dy_wall: float = 2e-3, jitter: float = 0.05,
+          seed: int = 1):
+    """The NACA 0012 O-grid (x, y, tri with 1-based node ids), the same mesh as
+    the library's generator with the same arguments, made without it."""
+    x = np.zeros(ni * (nj + 1))
+    y = np.zeros(ni * (nj + 1))
+    tri = np.zeros((2 * ni * nj, 3), np.int32)
+    if lib().or_ogrid_naca0012(ni, nj, r_far, dy_wall, jitter, seed, _dp(x), _dp(y), _ip(tri)) != 0:
+        raise ValueError(lib().or_last_error().decode())
+    return x, y, tri
 
 
 def set_threads(n: int) -> None:

@@ -270,3 +270,15 @@ def test_step_noalloc_names_every_alignment(lib):
     rc = lib.e2d_step_noalloc(64, ok, ok, ok, odd, ctypes.byref(p), 1, ok, ok, ctypes.byref(epsm), None)
     msg = lib.e2d_last_error().decode()
     assert rc == -1 and "area and resid 8-byte aligned" in msg
+
+
+@pytest.mark.parametrize("ni,nj,seed,jitter", [(8, 1, 1, 0.05), (64, 16, 5, 0.05), (128, 32, 1, 0.05),
+                                               (256, 64, 9, 0.0), (512, 128, 1, 0.05), (2048, 1024, 1, 0.05)])
+def test_oracle_ogrid_equals_library_ogrid(lib, oracle, ni, nj, seed, jitter):
+    """The oracle's statement of the O-grid generator (used by the CPU arm of
+    the benchmark, which must not load the product library) makes the same
+    mesh bit for bit, up to the large-mesh configuration's 2048 x 1024."""
+    a = e2d.Mesh.ogrid(ni, nj, seed=seed, jitter=jitter).nodes()
+    b = oracle.ogrid(ni, nj, seed=seed, jitter=jitter)
+    for u, v in zip(a, b):
+        assert np.array_equal(np.asarray(u).ravel(), np.asarray(v).ravel())
