@@ -36,17 +36,47 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    # name: (ni, nj, mach, alpha, cfl, precision, ordering, description)
+    # name: mesh size, flow conditions and description; the arithmetic type of
+    # a run (FP32 stencil with FP64 geometry / norms, or FP64 throughout) is
+    # the line's "dtype", not part of the workload
     "large": dict(ni=2048, nj=1024, ma=0.78, alpha=2.0, cfl=2.0,
-                  desc="NACA0012 O-grid 2048x1024 (4194304 tri), Morton, M0.78 a2.0, FP32 stencil, "
+                  desc="NACA0012 O-grid 2048x1024 (4194304 tri), Morton, M0.78 a2.0, CFL 2, "
                        "IRS 2 sweeps eps 0.8, 4-stage RK"),
     "medium": dict(ni=1024, nj=512, ma=0.78, alpha=2.0, cfl=2.0,
-                   desc="NACA0012 O-grid 1024x512 (1048576 tri), Morton, M0.78 a2.0, FP32 stencil, "
+                   desc="NACA0012 O-grid 1024x512 (1048576 tri), Morton, M0.78 a2.0, CFL 2, "
                         "IRS 2 sweeps eps 0.8, 4-stage RK"),
     "transonic": dict(ni=512, nj=128, ma=0.80, alpha=1.25, cfl=2.0,
-                      desc="NACA0012 O-grid 512x128 (131072 tri), Morton, M0.80 a1.25, FP32 stencil, "
+                      desc="NACA0012 O-grid 512x128 (131072 tri), Morton, M0.80 a1.25, CFL 2, "
                            "IRS 2 sweeps eps 0.8, 4-stage RK"),
 }
+
+def l2_note(ncell: int) -> str:
+    """How the timed iterations avoid a warm L2: the large meshes' working set
+    (~270 B per cell in FP32) is several times the 129 MB L2."""
+    if ncell * 270 > 4 * 129e6:
+        return f"inputs larger than L2 (working set ~{ncell * 270 / 1e9:.1f} GB), no flush"
+    return "working set fits in L2 (not a roofline case), no flush"
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), for the CPU baseline records."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        fields = {k.strip(): v.strip() for k, _, v in (line.partition(":") for line in out.splitlines())}
+        name = " ".join(v for v in (fields.get("Vendor ID"), fields.get("Model name")) if v and v != "-")
+        if name:
+            return name
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
 PASS_NAMES = ["faces", "flux", "smooth", "update", "resid"]
 
@@ -167,15 +197,13 @@ def workload_desc(wl, ordering="morton") -> str:
     return wl["desc"].replace("Morton", ORDERINGS[ordering][1])
 
 
-def cpu_port_rate(wl, steps_wanted: float, threads: int | None = None, mesh=None):
-    """Oracle port of the reference loop on the host cores: returns
-    (cell-stage/s, iterations run, seconds, threads)."""
+def cpu_port_rate(wl, steps_wanted: float, threads: int | None = None):
+    """Oracle port of the reference loop on the host cores, on the oracle's
+    own statement of the same mesh: returns (cell-stage/s, iterations run,
+    seconds, threads)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    import gpueularsolver2d_gb300 as e2d
-    if mesh is None:
-        mesh = e2d.Mesh.ogrid(wl["ni"], wl["nj"], seed=1)
-    x, y, tri = mesh.nodes()
+    x, y, tri = pyoracle.ogrid(wl["ni"], wl["nj"], seed=1)
     p = pyoracle.params(ma=wl["ma"], alpha_deg=wl["alpha"], cfl=wl["cfl"])
     case = pyoracle.Case(x, y, tri, p)
     if threads:
@@ -189,15 +217,16 @@ def cpu_port_rate(wl, steps_wanted: float, threads: int | None = None, mesh=None
 
 
 def run_reference(args, rank: int, world: int):
-    """--impl reference: the reference scheme's CPU path on the host cores."""
+    """--impl reference: the reference scheme's CPU path on the host cores.
+    This arm loads only the oracle (its mesh comes from the oracle's statement
+    of the O-grid generator, equal bit for bit to the library's), never the
+    product library."""
     if rank != 0:
         return
     wl = WORKLOADS[args.workload]
-    import gpueularsolver2d_gb300 as e2d
-    mesh = e2d.Mesh.ogrid(wl["ni"], wl["nj"], seed=1)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    x, y, tri = mesh.nodes()
+    x, y, tri = pyoracle.ogrid(wl["ni"], wl["nj"], seed=1)
     p = pyoracle.params(ma=wl["ma"], alpha_deg=wl["alpha"], cfl=wl["cfl"])
     case = pyoracle.Case(x, y, tri, p)
     th = pyoracle.threads()
@@ -218,10 +247,12 @@ def run_reference(args, rank: int, world: int):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded NACA0012 O-grid)",
         "config": {"workload": workload_desc(wl, args.ordering), "cells": case.ncell, "stages": p.rk_stages,
-                   "parallelism": f"replicas{world}"},
-        "cpu_baseline": {"value": rate, "unit": "cell-stage/s", "cores": th, "kind": "port",
+                   "parallelism": f"replicas{world}", "l2": l2_note(case.ncell)},
+        "cpu_baseline": {"value": rate, "unit": "cell-stage/s", "cores": th, "cpu_model": cpu_model(),
+                         "kind": "port",
                          "sample": f"{k} of the {args.steps} requested iterations (capped at ~60 s of host "
-                                   f"time) of the full {case.ncell}-cell workload on {th} threads"},
+                                   f"time) of the full {case.ncell}-cell workload, FP64 (the reference's "
+                                   f"precision), cells in file order, on {th} threads"},
         "e2e": {"value": rate, "unit": "cell-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -332,14 +363,31 @@ def run_gpu(args, rank: int, world: int):
         a32.close()
         a64.close()
 
+    # the same workload with the FP64 stencil (the reference's precision):
+    # device time of a few iterations and the per-pass split
+    fp64 = None
+    if rank == 0 and prec == e2d.E2D_FP32 and not args.no_fp64:
+        solver = None
+        torch.cuda.synchronize()
+        s64 = e2d.Solver(mesh, make_params(e2d, wl, e2d.E2D_FP64, ordering=args.ordering))
+        k64 = max(1, min(args.fp64_steps, args.steps))
+        s64.step(2)
+        s64.step(k64)
+        t64 = s64.last_device_ms() / 1e3
+        ms64, nl64 = s64.profile_passes(1)
+        fp64 = {"value": ncell * stages * k64 / t64, "unit": "cell-stage/s", "steps": k64,
+                "ms_per_step": t64 / k64 * 1e3, "dtype": "f64",
+                "passes_ms_per_step": {name: float(ms64[j]) for j, name in enumerate(PASS_NAMES) if nl64[j]},
+                "launches_per_step": {name: int(nl64[j]) for j, name in enumerate(PASS_NAMES) if nl64[j]}}
+        s64.close()
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        del solver
+        solver = None
         torch.cuda.synchronize()
-        rate, k, dt, th = cpu_port_rate(wl, 2, mesh=mesh)
-        rate1, k1, dt1, _ = cpu_port_rate(wl, 1, threads=1, mesh=mesh)
-        cpu = {"value": rate, "unit": "cell-stage/s", "cores": th, "kind": "port",
-               "sample": f"{k} iterations of the full {ncell}-cell workload on {th} threads ({dt:.1f} s)",
+        rate, k, dt, th = cpu_port_rate(wl, 2)
+        rate1, k1, dt1, _ = cpu_port_rate(wl, 1, threads=1)
+        cpu = {"value": rate, "unit": "cell-stage/s", "cores": th, "cpu_model": cpu_model(), "kind": "port",
+               "sample": f"{k} iterations of the full {ncell}-cell workload, FP64, on {th} threads ({dt:.1f} s)",
                "single_thread_value": rate1,
                "single_thread_sample": f"{k1} iteration on 1 thread ({dt1:.1f} s)"}
     if rank == 0:
@@ -350,10 +398,9 @@ def run_gpu(args, rank: int, world: int):
             "dtype": "f64" if prec == e2d.E2D_FP64 else "f32",
             "data": "synthetic (seeded NACA0012 O-grid)",
             "config": {"workload": workload_desc(wl, args.ordering), "cells": ncell, "stages": stages,
-                       "parallelism": f"replicas{world}",
-                       "l2": "inputs larger than L2 (working set > 1 GB), no flush"},
+                       "parallelism": f"replicas{world}", "l2": l2_note(ncell)},
             "wall_ms_per_step": wall / args.steps * 1e3,
-            "roofline": roofline, "passes": per_pass, "fp32_error_vs_fp64": fp_err,
+            "roofline": roofline, "passes": per_pass, "fp32_error_vs_fp64": fp_err, "fp64": fp64,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_rate, "unit": "cell-stage/s", "steps": e2e_steps,
                     "h2d_bytes_per_step": int(pin_in.nbytes), "d2h_bytes_per_step": int(pin_out.nbytes)},
@@ -487,6 +534,8 @@ def main():
     ap.add_argument("--block", type=int, default=0, help="threads per CTA (0: library default)")
     ap.add_argument("--ordering", choices=sorted(ORDERINGS), default="morton", help="cell order in device memory")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-stencil record of the same workload")
+    ap.add_argument("--fp64-steps", type=int, default=10, help="timed iterations of the FP64-stencil record")
     ap.add_argument("--mlp-layers", type=int, default=8, help="hidden layers of the MLP workload")
     args = ap.parse_args()
     if args.warmup < 3:

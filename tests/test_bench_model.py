@@ -58,3 +58,20 @@ def test_integral_errors():
     assert set(e) == set(i32)
     assert e["cl"]["abs_err"] == pytest.approx(1e-4) and e["mass"]["abs_err"] == 0.0
     assert e["mass_flux_far"] == {"fp32": 1e-3, "fp64": 2e-3, "abs_err": 1e-3}
+
+
+def test_reference_arm_does_not_load_the_product_library():
+    """--impl reference times the oracle's CPU port on the oracle's own
+    statement of the mesh; the product package and its library stay
+    unloaded in that process."""
+    import subprocess
+    code = ("import sys, bench\n"
+            "sys.argv = ['bench.py', '--impl', 'reference', '--workload', 'transonic', '--steps', '1', '--warmup', '3']\n"
+            "bench.main()\n"
+            "assert 'gpueularsolver2d_gb300' not in sys.modules\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "assert 'libeuler2d' not in maps and 'liboracle' in maps\n")
+    res = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr[-2000:]
+    line = json.loads(res.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["dtype"] == "f64" and line["cpu_baseline"]["cpu_model"]
