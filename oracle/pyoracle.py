@@ -217,8 +217,12 @@ def ref_harness_path() -> str | None:
 
 
 def run_reference(mode: str, mesh_path: str, input_line: str, w_in: np.ndarray | None = None,
-                  workdir: str | None = None) -> dict:
-    """Run the reference harness in a scratch directory and read its dumps."""
+                  workdir: str | None = None, trace: bool = False, dump_at=()) -> dict:
+    """Run the reference harness in a scratch directory and read its dumps.
+
+    In "gpu" mode, ``trace`` adds ``drou`` (sum of (rho_n - rho_{n-1})^2 of
+    every iteration, from the program's own states) and ``dump_at`` adds
+    ``w_at`` = {k: state after k iterations}."""
     exe = ref_harness_path()
     if exe is None:
         raise FileNotFoundError("reference sources not available")
@@ -230,7 +234,14 @@ def run_reference(mode: str, mesh_path: str, input_line: str, w_in: np.ndarray |
             f.write(input_line + "\n")
         if w_in is not None:
             np.ascontiguousarray(w_in, np.float64).tofile(os.path.join(d, "w_in.bin"))
-        res = subprocess.run([exe, mode, d], capture_output=True, text=True)
+        env = dict(os.environ)
+        env.pop("E2D_REF_TRACE", None)
+        env.pop("E2D_REF_DUMP_AT", None)
+        if trace:
+            env["E2D_REF_TRACE"] = "1"
+        if dump_at:
+            env["E2D_REF_DUMP_AT"] = ",".join(str(int(k)) for k in dump_at)
+        res = subprocess.run([exe, mode, d], capture_output=True, text=True, env=env)
         if res.returncode != 0:
             raise RuntimeError(f"reference harness failed: {res.stderr[-2000:]}")
         out = {"stdout": res.stdout}
@@ -243,6 +254,14 @@ def run_reference(mode: str, mesh_path: str, input_line: str, w_in: np.ndarray |
             p = os.path.join(d, name + ".bin")
             if os.path.exists(p):
                 out[name] = np.fromfile(p, dt)
+        p = os.path.join(d, "drou_trace.bin")
+        if os.path.exists(p):
+            out["drou"] = np.fromfile(p, np.float64)
+        out["w_at"] = {}
+        for k in dump_at:
+            p = os.path.join(d, f"w_at_{int(k)}.bin")
+            if os.path.exists(p):
+                out["w_at"][int(k)] = np.fromfile(p, np.float64).reshape(-1, 4)
         return out
     finally:
         if own:

@@ -19,21 +19,32 @@
  *                             1043-1503) on the initial state
  *   ref_harness gpu   DIR  -- the whole reference program (main renamed
  *                             ref_main) on the GPU, then dump its final
- *                             state w_S (gpu_solver.cu:13, filled by copyD2H)
+ *                             state w_S (gpu_solver.cu:13, filled by copyD2H);
+ *                             optionally trace its states while it runs
+ *                             (E2D_REF_TRACE, E2D_REF_DUMP_AT, below)
  */
 #include "gpu_fvm.cuh"
 
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <unistd.h>
+#include <vector>
 
 /* gpu_solver.cu:10-13 and 1832: globals and set-up step of the reference */
 extern W *Wallw, *Farw;
 extern W_S w_S;
 void changeEdge();
 int ref_main();
+
+/* ---- dumps ----------------------------------------------------------- */
+static void dump_file(const char *name, const void *p, size_t bytes) {
+    FILE *f = fopen(name, "wb");
+    if (!f || fwrite(p, 1, bytes, f) != bytes) { fprintf(stderr, "cannot write %s\n", name); exit(3); }
+    fclose(f);
+}
 
 /* ---- allocation guard used by ref_shim.h ---------------------------- */
 #undef cudaMalloc
@@ -54,7 +65,76 @@ cudaError_t e2d_ref_malloc(void **ptr, size_t size) {
     return e;
 }
 
+/* ---- trace of the reference's own states ------------------------------
+ * The only device-to-device copies of the reference are the four W -> W0
+ * snapshots at the start of every iteration (gpu_solver.cu:2205-2208, density,
+ * density_U, density_V, density_E in that order), so copy q of them is
+ * component q % 4 of the state after q / 4 iterations.  With E2D_REF_TRACE
+ * set, the harness reads each density snapshot back and accumulates
+ * drou_n = sum_i (rho_n - rho_{n-1})^2 over all cells in FP64, in cell order
+ * (the quantity kernel_drou means to compute, gpu_solver.cu:968-1020), and with
+ * E2D_REF_DUMP_AT="k1,k2,..." it also writes the full state after each listed
+ * iteration count to w_at_<k>.bin.  The copies themselves are unchanged. */
+static bool g_trace = false;
+static std::vector<int> g_dump_at;
+static long g_d2d = 0;
+static std::vector<double> g_prev, g_cur, g_dump;
+static std::vector<double> g_drou;
+
+static void trace_init() {
+    g_trace = getenv("E2D_REF_TRACE") != nullptr;
+    if (const char *s = getenv("E2D_REF_DUMP_AT")) {
+        for (const char *q = s; *q;) {
+            char *e;
+            long v = strtol(q, &e, 10);
+            if (e == q) break;
+            g_dump_at.push_back((int)v);
+            q = *e == ',' ? e + 1 : e;
+        }
+    }
+}
+
+static void trace_copy(const void *src, size_t count) {
+    const long q = g_d2d++;
+    const int comp = (int)(q % 4), done = (int)(q / 4);
+    const size_t n1 = (size_t)Ncell + 1;
+    if (count != n1 * sizeof(double)) return;
+    const bool dump = std::find(g_dump_at.begin(), g_dump_at.end(), done) != g_dump_at.end();
+    if (!(g_trace && comp == 0) && !dump) return;
+    g_cur.resize(n1);
+    if (cudaMemcpy(g_cur.data(), src, count, cudaMemcpyDeviceToHost) != cudaSuccess) return;
+    if (dump) {
+        g_dump.resize(4 * (size_t)Ncell);
+        for (int i = 1; i <= Ncell; i++) g_dump[4 * (size_t)(i - 1) + comp] = g_cur[i];
+        if (comp == 3) {
+            char name[64];
+            snprintf(name, sizeof name, "w_at_%d.bin", done);
+            dump_file(name, g_dump.data(), sizeof(double) * g_dump.size());
+        }
+    }
+    if (g_trace && comp == 0) {
+        if (!g_prev.empty()) {
+            double s = 0.0;
+            for (int i = 1; i <= Ncell; i++) s += (g_cur[i] - g_prev[i]) * (g_cur[i] - g_prev[i]);
+            g_drou.push_back(s);
+        }
+        g_prev.swap(g_cur);
+    }
+}
+
+/* the last iteration's term, from the final state the program copied back */
+static void trace_finish(const double *rho_final) {
+    if (!g_trace) return;
+    if (!g_prev.empty()) {
+        double s = 0.0;
+        for (int i = 1; i <= Ncell; i++) s += (rho_final[i] - g_prev[i]) * (rho_final[i] - g_prev[i]);
+        g_drou.push_back(s);
+    }
+    dump_file("drou_trace.bin", g_drou.data(), sizeof(double) * g_drou.size());
+}
+
 cudaError_t e2d_ref_memcpy(void *dst, const void *src, size_t count, cudaMemcpyKind kind) {
+    if (kind == cudaMemcpyDeviceToDevice && in_alloc(src, count)) trace_copy(src, count);
     bool ok = true;
     if (kind == cudaMemcpyHostToDevice || kind == cudaMemcpyDeviceToDevice) ok = ok && in_alloc(dst, count);
     if (kind == cudaMemcpyDeviceToHost || kind == cudaMemcpyDeviceToDevice) ok = ok && in_alloc(src, count);
@@ -65,12 +145,7 @@ cudaError_t e2d_ref_memcpy(void *dst, const void *src, size_t count, cudaMemcpyK
     return cudaMemcpy(dst, src, count, kind);
 }
 
-/* ---- dumps ----------------------------------------------------------- */
-static void dump(const char *name, const void *p, size_t bytes) {
-    FILE *f = fopen(name, "wb");
-    if (!f || fwrite(p, 1, bytes, f) != bytes) { fprintf(stderr, "cannot write %s\n", name); exit(3); }
-    fclose(f);
-}
+static void dump(const char *name, const void *p, size_t bytes) { dump_file(name, p, bytes); }
 
 static void setup(bool partition = true) {
     /* gpu_fvm.cu:31-40 */
@@ -201,7 +276,9 @@ int main(int argc, char **argv) {
         return 0;
     }
     if (!strcmp(argv[1], "gpu")) {
+        trace_init();
         ref_main();
+        trace_finish(w_S.density);
         int counts[2] = {Ncell, step};
         dump("gpu_counts.bin", counts, sizeof counts);
         double *wf = (double *)malloc(sizeof(double) * 4 * Ncell);

@@ -180,3 +180,101 @@ def test_reference_residual_history_from_its_own_states(lib, oracle):
     s.step(n)
     np.testing.assert_allclose(s.history(), resd_ref, rtol=1e-9)
     assert len(printed) == n and printed[0] == 1.0
+
+
+def test_c1_configuration_2000_iterations_against_reference(lib, oracle):
+    """The small-mesh configuration at its configured iteration count: 128 x 32
+    O-grid (seed 1), M 0.5, alpha 1.25, CFL 2, the reference's 4-stage RK and
+    smoothing (eps 0.8, 2 sweeps), 2000 iterations of the reference's own GPU
+    program (ROE_SOLVER, gpu_solver.cu:2171-2434) against this library.
+
+    The reference run is traced (oracle/ref_harness.cu): its states after 50
+    and 200 iterations are read from its own W -> W0 snapshots, and its
+    residual history is rebuilt from every snapshot as
+    Resd_n = sqrt(sum (rho_n - rho_{n-1})^2 / sum (rho_1 - rho_0)^2).
+
+    At 50 iterations the FP64 states agree to 1e-8 of the largest conserved
+    value.  Later the limiter and the smoothing clamp switch on rounding-level
+    differences, so the measure of agreement is this library's own
+    sensitivity: three runs whose start state is moved by one unit in the last
+    place (rho E up, rho u down, rho up) give d_ulp, the median of their
+    distances from the unperturbed run, and the reference must lie within
+    2 d_ulp -- in the state, in CL and CD, and in the residual history's log
+    distance.  The FP32 stencil is reported beside it."""
+    import json
+    if oracle.ref_harness_path() is None:
+        pytest.skip("reference sources not available")
+    N, cps = 2000, (50, 200, 2000)
+    mesh = e2d.Mesh.ogrid(128, 32, seed=1)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "mesh.dat")
+        mesh.write(path)
+        out = oracle.run_reference("gpu", path, f"0.5 1.25 1.4 101325 288.15 2.0 1e-12 {N}", trace=True,
+                                   dump_at=cps[:-1])
+    assert out["gpu_counts"][1] == N and len(out["drou"]) == N
+    w_ref = dict(out["w_at"])
+    w_ref[N] = out["gpu_w"].reshape(-1, 4)
+    resd_ref = np.sqrt((out["drou"] + 1e-32) / out["drou"][0])
+
+    def run(prec, w0=None):
+        p = e2d.default_params(ma=0.5, alpha_deg=1.25, cfl=2.0, maxstep=N + 10, precision=prec)
+        s = e2d.Solver(mesh, p)
+        if w0 is not None:
+            s.set_state(w0)
+        states, done = {}, 0
+        for k in cps:
+            s.step(k - done)
+            done = k
+            states[k] = s.state()
+        return states, s.history(), p
+
+    lib64, hist64, p64 = run(e2d.E2D_FP64)
+    lib32, hist32, _ = run(e2d.E2D_FP32)
+    w_start = e2d.Solver(mesh, p64).state()
+    perturbed = []
+    for comp, direction in ((3, np.inf), (1, -np.inf), (0, np.inf)):
+        wp = w_start.copy()
+        wp[:, comp] = np.nextafter(wp[:, comp], direction)
+        perturbed.append(run(e2d.E2D_FP64, wp)[:2])
+
+    def integ(w):
+        r = e2d.state_integrals(mesh, p64, w)
+        return r["cl"], r["cd"]
+
+    def logdist(a, b):
+        return float(np.max(np.abs(np.log10(a) - np.log10(b))))
+
+    report = {"config": "128x32 O-grid seed 1, M0.5 a1.25 CFL2, 4-stage RK, IRS eps 0.8 x2", "iterations": {}}
+    for k in cps:
+        scale = np.max(np.abs(lib64[k]))
+        d_ref = float(np.max(np.abs(lib64[k] - w_ref[k])) / scale)
+        d_ps = [float(np.max(np.abs(ps[k] - lib64[k])) / scale) for ps, _ in perturbed]
+        cl, cd = integ(lib64[k])
+        cl_r, cd_r = integ(w_ref[k])
+        dcl_ps = [abs(integ(ps[k])[0] - cl) for ps, _ in perturbed]
+        dcd_ps = [abs(integ(ps[k])[1] - cd) for ps, _ in perturbed]
+        report["iterations"][k] = {
+            "state_rel_linf_fp64_vs_reference": d_ref,
+            "state_rel_linf_fp32_vs_reference": float(np.max(np.abs(lib32[k] - w_ref[k])) / scale),
+            "ulp_self_sensitivity": d_ps, "d_ulp_median": float(np.median(d_ps)),
+            "cl_lib": cl, "cl_reference": cl_r, "cd_lib": cd, "cd_reference": cd_r,
+            "dcl_vs_reference": abs(cl - cl_r), "dcd_vs_reference": abs(cd - cd_r),
+            "dcl_ulp": dcl_ps, "dcd_ulp": dcd_ps,
+            "resid_logdist_vs_reference": logdist(hist64[:k], resd_ref[:k]),
+            "resid_logdist_ulp": [logdist(h[:k], hist64[:k]) for _, h in perturbed],
+            "resid_logdist_fp32_vs_reference": logdist(hist32[:k], resd_ref[:k]),
+            "meets_1e-5": d_ref < 1e-5,
+        }
+    report["resid_first20_max_rel_vs_reference"] = float(np.max(np.abs(hist64[:20] / resd_ref[:20] - 1)))
+    print(json.dumps(report, indent=1))
+    if os.environ.get("E2D_C1_OUT"):
+        with open(os.environ["E2D_C1_OUT"], "w") as f:
+            json.dump(report, f, indent=1)
+    r = report["iterations"]
+    assert r[50]["state_rel_linf_fp64_vs_reference"] < 1e-8
+    assert report["resid_first20_max_rel_vs_reference"] < 1e-6
+    for k in cps[1:]:
+        assert r[k]["state_rel_linf_fp64_vs_reference"] <= 2 * r[k]["d_ulp_median"], r[k]
+        assert r[k]["dcl_vs_reference"] <= 2 * max(r[k]["dcl_ulp"]) + 1e-12, r[k]
+        assert r[k]["dcd_vs_reference"] <= 2 * max(r[k]["dcd_ulp"]) + 1e-12, r[k]
+        assert r[k]["resid_logdist_vs_reference"] <= 2 * max(r[k]["resid_logdist_ulp"]) + 1e-9, r[k]

@@ -86,3 +86,41 @@ def test_step_noalloc_rejects_too_many_cells(lib):
                               None)
     assert rc == -6
     assert "32768" in lib.e2d_last_error().decode()
+
+
+def test_step_noalloc_refuses_out_of_range_topology(lib):
+    """A face code that names a cell outside the mesh (or a slot above 2, or a
+    negative code other than -1 / -2) is caught on the GPU before any pass
+    gathers through it: the call returns E2D_ERR_ARG, the state and the
+    residual buffer are untouched, and the next valid call works."""
+    import torch
+    mesh = e2d.Mesh.ogrid(48, 12, seed=6)
+    p = e2d.default_params(ma=0.6, alpha_deg=1.5, cfl=1.5, ordering=e2d.E2D_ORDER_FILE)
+    ref = e2d.Solver(mesh, p)
+    topo, S, R, area = file_order_layout(mesh)
+    n = ref.ncell
+    dev = torch.device("cuda", torch.cuda.current_device())
+    t_S, t_R, t_area = (torch.from_numpy(a).to(dev) for a in (S, R, area))
+    w0 = ref.state().ravel().copy()
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    t4 = topo.reshape(n, 4)
+    i = int(np.flatnonzero(t4[:, 0] >= 0)[0])
+    for bad_code in ((n + 3) << 3 | (int(t4[i, 0]) & 7), (int(t4[i, 0]) & ~3) | 3, -5):
+        bad = t4.copy()
+        bad[i, 0] = bad_code
+        t_topo = torch.from_numpy(bad.ravel().copy()).to(dev)
+        t_w = torch.from_numpy(w0).to(dev)
+        t_res = torch.full((2,), -7.0, dtype=torch.float64, device=dev)
+        epsm = ctypes.c_double(0.0)
+        rc = lib.e2d_step_noalloc(n, ptr(t_topo), ptr(t_S), ptr(t_R), ptr(t_area), ctypes.byref(p), 2, ptr(t_w),
+                                  ptr(t_res), ctypes.byref(epsm), None)
+        assert rc == -1 and "out of range" in lib.e2d_last_error().decode(), bad_code
+        assert np.array_equal(t_w.cpu().numpy(), w0) and np.all(t_res.cpu().numpy() == -7.0)
+    t_topo = torch.from_numpy(topo).to(dev)
+    t_w = torch.from_numpy(w0).to(dev)
+    t_res = torch.zeros(2, dtype=torch.float64, device=dev)
+    epsm = ctypes.c_double(0.0)
+    _lib.check(lib.e2d_step_noalloc(n, ptr(t_topo), ptr(t_S), ptr(t_R), ptr(t_area), ctypes.byref(p), 2, ptr(t_w),
+                                    ptr(t_res), ctypes.byref(epsm), None))
+    ref.step(2)
+    assert np.array_equal(t_w.cpu().numpy().reshape(n, 4), ref.state())
