@@ -640,14 +640,119 @@ __global__ void E2D_LB_FLUX k_flux_tile(MeshDev<T> m, Flow<T> f, const V4<T> *__
     flux_tile(m, f, base, min((int)blockDim.x, m.n - base), FS, res);
 }
 
+// Pass B for the 32 consecutive cells of one warp with each interior face
+// between two of them evaluated once, by its left cell's lane, and handed to
+// the right cell through shared memory (warp-synchronous: no block barrier).
+// Faces to cells of other warps and boundary faces are evaluated by their own
+// cell, as in flux_cell.  In Morton order about three quarters of the interior
+// faces of a 4.2M-cell mesh lie inside a warp, so a warp evaluates about 1.9
+// fluxes per cell instead of 3.  The warp first lists the faces it must
+// evaluate, spreads them over its lanes, keeps the fluxes in shared memory,
+// and then every cell sums its three faces in face order with the reference's
+// signs.  The fluxes are the same bits as flux_cell's (face_flux_of with the
+// same inputs) summed in the same order, so the result is bit-identical.
+// Every lane of the warp must call it; `live` is false for lanes past the
+// last cell.
+template <typename T> struct WarpFlux {
+    V4<T> F[128];       // fluxes of the warp's evaluation list (at most 96)
+    int2 item[128];     // list entry: {(lane << 2) | face, face code}
+    int offmask[32];    // per lane: (first list index << 3) | mask of own entries
+};
+
+template <typename T>
+__device__ __forceinline__ void flux_warp(const MeshDev<T> &m, const Flow<T> &f, const int i, const bool live,
+                                          const V4<T> *__restrict__ FS, V4<T> *__restrict__ res,
+                                          WarpFlux<T> &w) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, base = i - lane;
+    const int4 tp = live ? m.topo[i] : make_int4(-3, -3, -3, 0);
+    const int code[3] = {tp.x, tp.y, tp.z};
+    // faces this lane evaluates: boundary faces, faces to other warps, and
+    // faces inside the warp of which this cell is the left cell
+    unsigned mask = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int c = code[k];
+        if (!live) continue;
+        if (c < 0) { mask |= 1u << k; continue; }
+        const bool inside = (unsigned)((c >> 3) - base) < 32u;
+        if (!inside || !((c >> 2) & 1)) mask |= 1u << k;
+    }
+    const int cnt = __popc(mask);
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(full, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(full, incl, 31);
+    const int off = incl - cnt;
+    w.offmask[lane] = (off << 3) | (int)mask;
+    {
+        int j = off;
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            if (mask & (1u << k)) w.item[j++] = make_int2((lane << 2) | k, code[k]);
+    }
+    __syncwarp();
+    for (int q = lane; q < total; q += 32) {
+        const int2 it = w.item[q];
+        bool right;
+        w.F[q] = face_flux(m, f, base + (it.x >> 2), it.x & 3, it.y, FS, right);
+    }
+    __syncwarp();
+    if (live) {
+        V4<T> r;
+        r.x = T(0.0); r.y = T(0.0); r.z = T(0.0); r.w = T(0.0);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const int c = code[k];
+            int idx;
+            bool right;
+            if (mask & (1u << k)) {
+                idx = off + __popc(mask & ((1u << k) - 1u));
+                right = c >= 0 && ((c >> 2) & 1);
+            } else {  // inside face evaluated by its left cell
+                const int om = w.offmask[(c >> 3) - base];
+                idx = (om >> 3) + __popc((unsigned)(om & 7) & ((1u << (c & 3)) - 1u));
+                right = true;
+            }
+            const V4<T> F = w.F[idx & 127];
+            if (right) { r.x -= F.x; r.y -= F.y; r.z -= F.z; r.w -= F.w; }
+            else { r.x += F.x; r.y += F.y; r.z += F.z; r.w += F.w; }
+        }
+        res[i] = r;
+    }
+    __syncwarp();  // w may be reused by this warp's next tile
+}
+
+// Pass-B form of the FP32 stencil: the warp form above (E2D_FLUX_WARP,
+// default) or flux_cell's three evaluations per cell.  The warp form takes
+// one WarpFlux of dynamic shared memory per warp of the block.
+#ifndef E2D_FLUX_WARP
+#define E2D_FLUX_WARP 1
+#endif
+
+extern __shared__ __align__(16) unsigned char dyn_smem[];
+
+// Dynamic shared memory of one pass-B launch of `block` threads.
+template <typename T> inline size_t flux_smem(int block) {
+    return (!FluxTiled<T>::value && E2D_FLUX_WARP != 0) ? sizeof(WarpFlux<T>) * (size_t)(block / 32) : 0;
+}
+
 template <typename T>
 __global__ void E2D_LB_FLUX k_flux(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ FS,
                                    V4<T> *__restrict__ res, const Ctl *__restrict__ ctl) {
     wait_prior_grid();
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.n) return;
-    flux_cell(m, f, i, FS, res);
+    if constexpr (E2D_FLUX_WARP != 0) {
+        WarpFlux<T> *wf = reinterpret_cast<WarpFlux<T> *>(dyn_smem);
+        flux_warp(m, f, i, i < m.n, FS, res, wf[threadIdx.x >> 5]);
+    } else {
+        if (i >= m.n) return;
+        flux_cell(m, f, i, FS, res);
+    }
 }
 
 // Sum of the interior neighbours' values in face order (gpu_solver.cu:1658-1666)
@@ -820,8 +925,12 @@ __global__ void E2D_LB_FLUX kb_flux(MeshDev<T> m, BatchDev<T> b, int ntiles, con
         const int tc = b.chunk_case[base / kChunk];  // every cell of a tile is in one case
         if (b.ctl[tc].halt) continue;                // uniform over the block
         const Flow<T> f = b.flows[tc];
-        if (FluxTiled<T>::value) {
+        if constexpr (FluxTiled<T>::value) {
             flux_tile(m, f, base, max(0, min((int)blockDim.x, b.case_end[tc] - base)), FS, res);
+        } else if constexpr (E2D_FLUX_WARP != 0) {
+            WarpFlux<T> *wf = reinterpret_cast<WarpFlux<T> *>(dyn_smem);
+            const int i = base + threadIdx.x;
+            flux_warp(m, f, i, i < b.case_end[tc], FS, res, wf[threadIdx.x >> 5]);
         } else {
             const int i = base + threadIdx.x;
             if (i < b.case_end[tc]) flux_cell(m, f, i, FS, res);
@@ -872,7 +981,7 @@ template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream
         V4<T> *Wout = last ? p.W[0] : p.W[1];
         if (p.options) launch_chained(kb_faces<T, true>, G, B, s, p.m, p.b, NT, Wcur, p.FS, p.dt, p.phi, st);
         else launch_chained(kb_faces<T, false>, G, B, s, p.m, p.b, NT, Wcur, p.FS, p.dt, p.phi, st);
-        launch_chained(kb_flux<T>, G, B, s, p.m, p.b, NT, p.FS, p.res);
+        launch_chained_smem(kb_flux<T>, G, B, flux_smem<T>(B), s, p.m, p.b, NT, p.FS, p.res);
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
             V4<T> *dst = p.sm[sw & 1];
@@ -934,7 +1043,7 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
         if (opt) launch_chained(k_faces<T, true>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
         else launch_chained(k_faces<T, false>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
         if (FluxTiled<T>::value) launch_chained(k_flux_tile<T>, G, B, s, p.m, p.f, p.FS, p.res, p.ctl);
-        else launch_chained(k_flux<T>, G, B, s, p.m, p.f, p.FS, p.res, p.ctl);
+        else launch_chained_smem(k_flux<T>, G, B, flux_smem<T>(B), s, p.m, p.f, p.FS, p.res, p.ctl);
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
             V4<T> *dst = p.sm[sw & 1];
@@ -967,7 +1076,7 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
         done();
         mark(1);
         if (FluxTiled<T>::value) k_flux_tile<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
-        else k_flux<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
+        else k_flux<T><<<G, B, flux_smem<T>(B), s>>>(p.m, p.f, p.FS, p.res, p.ctl);
         done();
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {

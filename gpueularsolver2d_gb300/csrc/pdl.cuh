@@ -18,11 +18,12 @@ namespace e2d {
 __device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 
 template <typename... KArgs, typename... Args>
-inline void launch_chained(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+inline void launch_chained_smem(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = block;
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -30,6 +31,11 @@ inline void launch_chained(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaSt
     cfg.attrs = at;
     cfg.numAttrs = 1;
     cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
+template <typename... KArgs, typename... Args>
+inline void launch_chained(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+    launch_chained_smem(kern, grid, block, 0, s, args...);
 }
 
 }  // namespace e2d

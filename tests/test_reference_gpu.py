@@ -115,42 +115,6 @@ def test_reference_diverges_on_the_transonic_case_too(lib, oracle):
     # library's to 1e-10 (test_reference_gpu_program_matches).
 
 
-def test_small_mesh_configuration_against_reference(lib, oracle):
-    """The 128 x 32 O-grid configuration (M 0.5, alpha 1.25, CFL 2, reference
-    4-stage RK and smoothing): after 50 iterations the reference's own GPU
-    program and this library's FP64 path agree to 1e-8 of the largest
-    conserved value (the 1e-5 relative L-infinity bar with room to spare).
-    Later in the start-up transient the limiter and smoothing-clamp switches
-    amplify any rounding difference: after 200 iterations the two differ by
-    about as much as this library differs from itself when its start state
-    is moved by one unit in the last place of rho E, so the difference is the
-    scheme's sensitivity, not a different computation."""
-    if oracle.ref_harness_path() is None:
-        pytest.skip("reference sources not available")
-    mesh = e2d.Mesh.ogrid(128, 32, seed=1)
-    p = e2d.default_params(ma=0.5, alpha_deg=1.25, cfl=2.0, maxstep=1000)
-    with tempfile.TemporaryDirectory() as d:
-        path = os.path.join(d, "mesh.dat")
-        mesh.write(path)
-        w50 = oracle.run_reference("gpu", path, "0.5 1.25 1.4 101325 288.15 2.0 1e-12 50")["gpu_w"].reshape(-1, 4)
-        w200 = oracle.run_reference("gpu", path, "0.5 1.25 1.4 101325 288.15 2.0 1e-12 200")["gpu_w"].reshape(-1, 4)
-    s = e2d.Solver(mesh, p)
-    w0 = s.state()
-    s.step(50)
-    assert np.max(np.abs(s.state() - w50)) / np.max(np.abs(w50)) < 1e-8
-    s.step(150)
-    w = s.state()
-    q = e2d.Solver(mesh, p)
-    wp = w0.copy()
-    wp[:, 3] = np.nextafter(wp[:, 3], np.inf)
-    q.set_state(wp)
-    q.step(200)
-    scale = np.max(np.abs(w))
-    d_ref = np.max(np.abs(w - w200)) / scale
-    d_ulp = np.max(np.abs(q.state() - w)) / scale
-    assert d_ulp > 1e-4 and d_ref < 10 * d_ulp, (d_ref, d_ulp)
-
-
 def test_reference_residual_history_from_its_own_states(lib, oracle):
     """Residual histories overlay: the reference's states after 0, 1, ..., 8
     iterations (one run of its program per count) give Resd_n =
@@ -204,7 +168,7 @@ def test_c1_configuration_2000_iterations_against_reference(lib, oracle):
     import json
     if oracle.ref_harness_path() is None:
         pytest.skip("reference sources not available")
-    N, cps = 2000, (50, 200, 2000)
+    N, cps = 2000, (50, 60, 70, 80, 100, 125, 150, 200, 500, 1000, 2000)
     mesh = e2d.Mesh.ogrid(128, 32, seed=1)
     with tempfile.TemporaryDirectory() as d:
         path = os.path.join(d, "mesh.dat")
@@ -266,14 +230,15 @@ def test_c1_configuration_2000_iterations_against_reference(lib, oracle):
             "meets_1e-5": d_ref < 1e-5,
         }
     report["resid_first20_max_rel_vs_reference"] = float(np.max(np.abs(hist64[:20] / resd_ref[:20] - 1)))
+    r = report["iterations"]
+    report["last_checkpoint_within_1e-5"] = max(k for k in cps if r[k]["meets_1e-5"])
     print(json.dumps(report, indent=1))
     if os.environ.get("E2D_C1_OUT"):
         with open(os.environ["E2D_C1_OUT"], "w") as f:
             json.dump(report, f, indent=1)
-    r = report["iterations"]
     assert r[50]["state_rel_linf_fp64_vs_reference"] < 1e-8
     assert report["resid_first20_max_rel_vs_reference"] < 1e-6
-    for k in cps[1:]:
+    for k in (200, 500, 1000, 2000):
         assert r[k]["state_rel_linf_fp64_vs_reference"] <= 2 * r[k]["d_ulp_median"], r[k]
         assert r[k]["dcl_vs_reference"] <= 2 * max(r[k]["dcl_ulp"]) + 1e-12, r[k]
         assert r[k]["dcd_vs_reference"] <= 2 * max(r[k]["dcd_ulp"]) + 1e-12, r[k]
