@@ -271,9 +271,13 @@ def run_gpu(args, rank: int, world: int):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     wl = WORKLOADS[args.workload]
     prec = e2d.E2D_FP64 if args.fp64 else e2d.E2D_FP32
+    t_setup0 = time.perf_counter()
     mesh = e2d.Mesh.ogrid(wl["ni"], wl["nj"], seed=1)
+    t_setup1 = time.perf_counter()
     params = make_params(e2d, wl, prec, args.block, args.ordering)
-    solver = e2d.Solver(mesh, params)
+    solver = e2d.Solver(mesh, params)  # set-up: geometry, edges, tags, cell order, layout, upload
+    torch.cuda.synchronize()
+    setup = {"mesh_generation_s": t_setup1 - t_setup0, "solver_create_s": time.perf_counter() - t_setup1}
     ncell, stages = solver.ncell, params.rk_stages
     launches = solver.launches_per_iteration()
 
@@ -400,7 +404,7 @@ def run_gpu(args, rank: int, world: int):
             "config": {"workload": workload_desc(wl, args.ordering), "cells": ncell, "stages": stages,
                        "parallelism": f"replicas{world}", "l2": l2_note(ncell)},
             "wall_ms_per_step": wall / args.steps * 1e3,
-            "roofline": roofline, "passes": per_pass, "fp32_error_vs_fp64": fp_err, "fp64": fp64,
+            "roofline": roofline, "passes": per_pass, "fp32_error_vs_fp64": fp_err, "fp64": fp64, "setup": setup,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_rate, "unit": "cell-stage/s", "steps": e2e_steps,
                     "h2d_bytes_per_step": int(pin_in.nbytes), "d2h_bytes_per_step": int(pin_out.nbytes)},

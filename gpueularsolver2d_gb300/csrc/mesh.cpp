@@ -7,10 +7,14 @@
 // node id, partners are matched inside the (short) buckets, and edges are
 // numbered in (cell, face) order of first appearance.
 #include <algorithm>
+#include <array>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <thread>
 
 #include "internal.h"
 
@@ -25,6 +29,47 @@ static inline double tri_area(double x1, double y1, double x2, double y2, double
     return (0.5 * ((y3 - y1) * (x2 - x1) - (y2 - y1) * (x3 - x1)));
 }
 
+// ---- parallel loops of the set-up -----------------------------------------
+// The set-up runs on the host cores: a fixed split of [0, n) into one chunk
+// per worker (std::thread; the split depends only on n and the worker count,
+// so two passes over the same range see the same chunks).  Small ranges run
+// on the calling thread.
+static int setup_workers() {
+    static const int w = [] {
+        if (const char *e = std::getenv("E2D_SETUP_THREADS")) {
+            const int v = std::atoi(e);
+            if (v >= 1) return std::min(v, 256);
+        }
+        const unsigned h = std::thread::hardware_concurrency();
+        return (int)std::min(64u, std::max(1u, h));
+    }();
+    return w;
+}
+
+struct Split {
+    int64_t n;
+    int T;
+    explicit Split(int64_t n_) : n(n_), T(n_ < 32768 ? 1 : (int)std::min<int64_t>(setup_workers(), n_ / 16384)) {}
+    int64_t begin(int t) const { return n * t / T; }
+    int64_t end(int t) const { return n * (t + 1) / T; }
+    // fn(begin, end, chunk) for every chunk
+    template <class F> void run(F fn) const {
+        if (T == 1) { fn((int64_t)0, n, 0); return; }
+        std::vector<std::thread> th;
+        th.reserve(T - 1);
+        for (int t = 1; t < T; t++) th.emplace_back([&, t] { fn(begin(t), end(t), t); });
+        fn(begin(0), end(0), 0);
+        for (auto &x : th) x.join();
+    }
+};
+
+// Set-up of CalculationMeshGeo (gpu_init.cu:100-228) and changeEdge
+// (gpu_solver.cu:1832-1906) with the reference's numbering: edges numbered in
+// (cell, face) order of first appearance, boundary edges tagged wall or far by
+// the box rule and numbered in the same order, then a stable partition
+// interior / far / wall.  Each step is a parallel pass over cells or faces
+// followed by prefix sums over the chunks, so the result does not depend on
+// the number of workers.
 int build_topology(e2d_mesh *m, double wall_box) {
     MeshTopo &t = m->topo;
     if (t.wall_box == wall_box && !t.clog.empty()) return E2D_OK;
@@ -32,119 +77,167 @@ int build_topology(e2d_mesh *m, double wall_box) {
     const int N = m->ncell, NN = m->nnode;
     if (N < 1 || NN < 3) { set_error("empty mesh"); return E2D_ERR_MESH; }
     t.area.resize(N); t.cx.resize(N); t.cy.resize(N);
+    const Split cells(N), faces(3 * (int64_t)N);
+    // 1. area and centroid; a bad cell is reported by its smallest index
+    //    (1 node id out of range, 2 area <= 0)
+    std::vector<char> bad(N, 0);
+    const double *X = m->x.data() - 1, *Y = m->y.data() - 1;
+    cells.run([&](int64_t c0, int64_t c1, int) {
+        for (int64_t i = c0; i < c1; i++) {
+            const int *p = &m->tri[3 * i];
+            if (p[0] < 1 || p[0] > NN || p[1] < 1 || p[1] > NN || p[2] < 1 || p[2] > NN) { bad[i] = 1; continue; }
+            t.area[i] = tri_area(X[p[0]], Y[p[0]], X[p[1]], Y[p[1]], X[p[2]], Y[p[2]]);
+            if (!(t.area[i] > 0.0)) { bad[i] = 2; continue; }
+            t.cx[i] = (X[p[0]] + X[p[1]] + X[p[2]]) / 3.0;
+            t.cy[i] = (Y[p[0]] + Y[p[1]] + Y[p[2]]) / 3.0;
+        }
+    });
     for (int i = 0; i < N; i++) {
-        const int *p = &m->tri[3 * i];
-        for (int k = 0; k < 3; k++)
-            if (p[k] < 1 || p[k] > NN) { set_error("node id out of range in cell " + std::to_string(i + 1)); return E2D_ERR_MESH; }
-        const double *x = m->x.data() - 1, *y = m->y.data() - 1;
-        t.area[i] = tri_area(x[p[0]], y[p[0]], x[p[1]], y[p[1]], x[p[2]], y[p[2]]);
-        if (!(t.area[i] > 0.0)) {
+        if (bad[i] == 1) { set_error("node id out of range in cell " + std::to_string(i + 1)); return E2D_ERR_MESH; }
+        if (bad[i] == 2) {
             set_error("cell " + std::to_string(i + 1) + " has area <= 0 (cells must be counter-clockwise)");
             return E2D_ERR_MESH;
         }
-        t.cx[i] = (x[p[0]] + x[p[1]] + x[p[2]]) / 3.0;
-        t.cy[i] = (y[p[0]] + y[p[1]] + y[p[2]]) / 3.0;
     }
     // face f of a cell joins Point[(f+1)%3] and Point[(f+2)%3]
     auto fnodes = [&](int c, int f, int &a, int &b) {
         a = m->tri[3 * c + (f + 1) % 3];
         b = m->tri[3 * c + (f + 2) % 3];
     };
-    std::vector<int> cnt(NN + 2, 0);
-    for (int c = 0; c < N; c++)
-        for (int f = 0; f < 3; f++) {
-            int a, b; fnodes(c, f, a, b);
-            if (a == b) { set_error("degenerate cell " + std::to_string(c + 1)); return E2D_ERR_MESH; }
-            cnt[std::min(a, b) + 1]++;
+    // 2. faces bucketed by their lower node id (counting sort; inside a bucket
+    //    the faces are put back in (cell, face) order)
+    std::vector<std::atomic<int>> cnt(NN + 2);
+    for (auto &v : cnt) v.store(0, std::memory_order_relaxed);
+    faces.run([&](int64_t f0, int64_t f1, int) {
+        for (int64_t cf = f0; cf < f1; cf++) {
+            int a, b; fnodes((int)(cf / 3), (int)(cf % 3), a, b);
+            cnt[std::min(a, b) + 1].fetch_add(1, std::memory_order_relaxed);
         }
-    for (int i = 1; i < NN + 2; i++) cnt[i] += cnt[i - 1];
-    std::vector<int> bucket(3 * (size_t)N), fill(cnt.begin(), cnt.end() - 1);
-    for (int c = 0; c < N; c++)
-        for (int f = 0; f < 3; f++) {
-            int a, b; fnodes(c, f, a, b);
-            bucket[fill[std::min(a, b)]++] = 3 * c + f;  // (cell, face) order inside a bucket
+    });
+    std::vector<int> start(NN + 2, 0);
+    for (int i = 1; i < NN + 2; i++) start[i] = start[i - 1] + cnt[i].load(std::memory_order_relaxed);
+    for (int i = 0; i < NN + 2; i++) cnt[i].store(start[i], std::memory_order_relaxed);
+    std::vector<int> bucket(3 * (size_t)N);
+    faces.run([&](int64_t f0, int64_t f1, int) {
+        for (int64_t cf = f0; cf < f1; cf++) {
+            int a, b; fnodes((int)(cf / 3), (int)(cf % 3), a, b);
+            bucket[cnt[std::min(a, b)].fetch_add(1, std::memory_order_relaxed)] = (int)cf;
         }
+    });
+    // 3. partner face: the other face of the same node pair (one at most);
+    //    err[lo] marks a bucket with a degenerate face, a repeated edge or a
+    //    non-manifold edge, reported for the smallest node
     std::vector<int> partner(3 * (size_t)N, -1);
-    for (int lo = 1; lo <= NN; lo++) {
-        int s = cnt[lo], e = cnt[lo + 1];
-        for (int u = s; u < e; u++) {
-            int cf = bucket[u], a, b; fnodes(cf / 3, cf % 3, a, b);
-            int hi = std::max(a, b), found = 0;
-            for (int v = s; v < e; v++) {
-                if (v == u) continue;
-                int cg = bucket[v], a2, b2; fnodes(cg / 3, cg % 3, a2, b2);
-                if (std::max(a2, b2) != hi) continue;
-                if (cg / 3 == cf / 3) { set_error("cell " + std::to_string(cf / 3 + 1) + " repeats an edge"); return E2D_ERR_MESH; }
-                if (++found > 1) { set_error("non-manifold edge at node " + std::to_string(lo)); return E2D_ERR_MESH; }
-                partner[cf] = cg;
-            }
-        }
-    }
-    // discovery in (cell, face) order, as gpu_init.cu:121-222
-    std::vector<int> face_edge(3 * (size_t)N, 0);
-    std::vector<int> elog, el, er, ef, ew, n1, n2;
-    std::vector<double> vn, vx, vy, mx, my;
-    size_t cap = (size_t)N * 3 / 2 + 16;
-    for (auto *v : {&elog, &el, &er, &ef, &ew, &n1, &n2}) v->reserve(cap);
-    for (auto *v : {&vn, &vx, &vy, &mx, &my}) v->reserve(cap);
-    int nw = 0, nf = 0;
-    const double *X = m->x.data() - 1, *Y = m->y.data() - 1;
-    for (int c = 0; c < N; c++)
-        for (int f = 0; f < 3; f++) {
-            int cf = 3 * c + f, p = partner[cf];
-            if (p >= 0 && p / 3 < c) { face_edge[cf] = face_edge[p]; continue; }
-            int a, b; fnodes(c, f, a, b);
-            elog.push_back(0); el.push_back(c + 1); n1.push_back(a); n2.push_back(b);
-            double ex = X[a] - X[b], ey = Y[b] - Y[a];
-            vx.push_back(ex); vy.push_back(ey);
-            mx.push_back(0.5 * (X[a] + X[b])); my.push_back(0.5 * (Y[a] + Y[b]));
-            vn.push_back(std::sqrt(ex * ex + ey * ey));
-            int wid = 0, fid = 0;
-            if (p >= 0) er.push_back(p / 3 + 1);
-            else {
-                er.push_back(-1);
-                if (std::fabs(mx.back()) < wall_box && std::fabs(my.back()) < wall_box) {
-                    elog.back() = 2; wid = ++nw;
-                } else {
-                    elog.back() = 1; fid = ++nf;
+    std::vector<char> err(NN + 2, 0);
+    const Split nodes(NN);
+    nodes.run([&](int64_t n0, int64_t n1, int) {
+        for (int64_t lo = n0 + 1; lo <= n1; lo++) {
+            const int s0 = start[lo], e0 = start[lo + 1];
+            std::sort(bucket.begin() + s0, bucket.begin() + e0);
+            for (int u = s0; u < e0 && !err[lo]; u++) {
+                const int cf = bucket[u];
+                int a, b; fnodes(cf / 3, cf % 3, a, b);
+                if (a == b) { err[lo] = 1; break; }
+                const int hi = std::max(a, b);
+                int found = 0;
+                for (int v = s0; v < e0; v++) {
+                    if (v == u) continue;
+                    const int cg = bucket[v];
+                    int a2, b2; fnodes(cg / 3, cg % 3, a2, b2);
+                    if (std::max(a2, b2) != hi) continue;
+                    if (cg / 3 == cf / 3) { err[lo] = 2; break; }
+                    if (++found > 1) { err[lo] = 3; break; }
+                    partner[cf] = cg;
                 }
             }
-            ef.push_back(fid); ew.push_back(wid);
-            face_edge[cf] = (int)elog.size();
         }
-    const int NE = (int)elog.size();
-    // changeEdge: stable partition interior / far / wall
-    std::vector<int> newid(NE + 1, 0);
-    int j = 1;
-    for (int lg = 0; lg <= 2; lg++)
-        for (int e = 0; e < NE; e++)
-            if (elog[e] == lg) newid[e + 1] = j++;
-    t.nedge = NE; t.nwall = nw; t.nfar = nf;
-    t.pre2post = newid;
+    });
+    for (int lo = 1; lo <= NN; lo++) {
+        if (!err[lo]) continue;
+        const int cf = bucket[start[lo]];
+        if (err[lo] == 1) set_error("degenerate cell with node " + std::to_string(lo));
+        else if (err[lo] == 2) set_error("cell " + std::to_string(cf / 3 + 1) + " repeats an edge");
+        else set_error("non-manifold edge at node " + std::to_string(lo));
+        return E2D_ERR_MESH;
+    }
+    // 4. the face that creates each edge (the first in (cell, face) order) and
+    //    its class: 0 interior, 1 far field, 2 wall (the box rule of
+    //    gpu_init.cu:190); -1 for a face whose edge an earlier face created
+    std::vector<signed char> kind(3 * (size_t)N);
+    faces.run([&](int64_t f0, int64_t f1, int) {
+        for (int64_t cf = f0; cf < f1; cf++) {
+            const int c = (int)(cf / 3), p = partner[cf];
+            if (p >= 0) { kind[cf] = p / 3 < c ? -1 : 0; continue; }
+            int a, b; fnodes(c, (int)(cf % 3), a, b);
+            const double mx = 0.5 * (X[a] + X[b]), my = 0.5 * (Y[a] + Y[b]);
+            kind[cf] = (std::fabs(mx) < wall_box && std::fabs(my) < wall_box) ? 2 : 1;
+        }
+    });
+    // prefix sums of the three classes over the chunks
+    std::vector<std::array<int, 3>> chunk_cnt(faces.T), chunk_off(faces.T);
+    faces.run([&](int64_t f0, int64_t f1, int ch) {
+        std::array<int, 3> c3 = {0, 0, 0};
+        for (int64_t cf = f0; cf < f1; cf++)
+            if (kind[cf] >= 0) c3[kind[cf]]++;
+        chunk_cnt[ch] = c3;
+    });
+    std::array<int, 3> tot = {0, 0, 0};
+    for (int ch = 0; ch < faces.T; ch++)
+        for (int k = 0; k < 3; k++) { chunk_off[ch][k] = tot[k]; tot[k] += chunk_cnt[ch][k]; }
+    const int NI = tot[0], NF = tot[1], NW = tot[2], NE = NI + NF + NW;
+    t.nedge = NE; t.nwall = NW; t.nfar = NF;
     for (auto *v : {&t.elog, &t.eleft, &t.eright, &t.efar, &t.ewall, &t.en1, &t.en2}) v->assign(NE, 0);
     for (auto *v : {&t.evn, &t.evx, &t.evy, &t.emx, &t.emy}) v->assign(NE, 0.0);
-    for (int e = 0; e < NE; e++) {
-        int k = newid[e + 1] - 1;
-        t.elog[k] = elog[e]; t.eleft[k] = el[e]; t.eright[k] = er[e]; t.efar[k] = ef[e];
-        t.ewall[k] = ew[e]; t.en1[k] = n1[e]; t.en2[k] = n2[e];
-        t.evn[k] = vn[e]; t.evx[k] = vx[e]; t.evy[k] = vy[e]; t.emx[k] = mx[e]; t.emy[k] = my[e];
-    }
+    t.pre2post.assign(NE + 1, 0);
+    // 5. every new edge written at its place after the partition (interior,
+    //    then far, then wall; each in discovery order); face_edge = 1-based id
+    std::vector<int> face_edge(3 * (size_t)N, 0);
+    faces.run([&](int64_t f0, int64_t f1, int ch) {
+        std::array<int, 3> r = chunk_off[ch];
+        for (int64_t cf = f0; cf < f1; cf++) {
+            const int kd = kind[cf];
+            if (kd < 0) continue;
+            const int c = (int)(cf / 3), p = partner[cf];
+            const int pre = r[0] + r[1] + r[2];  // discovery order
+            const int k = kd == 0 ? r[0] : kd == 1 ? NI + r[1] : NI + NF + r[2];
+            int a, b; fnodes(c, (int)(cf % 3), a, b);
+            t.elog[k] = kd; t.eleft[k] = c + 1; t.en1[k] = a; t.en2[k] = b;
+            t.eright[k] = p >= 0 ? p / 3 + 1 : -1;
+            t.efar[k] = kd == 1 ? r[1] + 1 : 0;
+            t.ewall[k] = kd == 2 ? r[2] + 1 : 0;
+            const double ex = X[a] - X[b], ey = Y[b] - Y[a];
+            t.evx[k] = ex; t.evy[k] = ey;
+            t.emx[k] = 0.5 * (X[a] + X[b]); t.emy[k] = 0.5 * (Y[a] + Y[b]);
+            t.evn[k] = std::sqrt(ex * ex + ey * ey);
+            t.pre2post[pre + 1] = k + 1;
+            face_edge[cf] = k + 1;
+            r[kd]++;
+        }
+    });
+    faces.run([&](int64_t f0, int64_t f1, int) {
+        for (int64_t cf = f0; cf < f1; cf++)
+            if (kind[cf] < 0) face_edge[cf] = face_edge[partner[cf]];
+    });
+    // 6. per-cell tables
     t.celledge.resize(3 * (size_t)N); t.neicell.resize(3 * (size_t)N); t.clog.resize(N);
     t.nb.resize(3 * (size_t)N); t.nb_slot.resize(3 * (size_t)N); t.is_right.resize(3 * (size_t)N);
-    for (int c = 0; c < N; c++) {
-        int nn = 3;
-        for (int f = 0; f < 3; f++) {
-            int cf = 3 * c + f, e = newid[face_edge[cf]] - 1;
-            t.celledge[cf] = e + 1;
-            int nbr = t.eleft[e] == c + 1 ? t.eright[e] : t.eleft[e];
-            if (nbr == -1) { nbr *= t.elog[e]; nn--; }
-            t.neicell[cf] = nbr;
-            t.nb[cf] = nbr > 0 ? nbr - 1 : nbr;
-            t.nb_slot[cf] = partner[cf] >= 0 ? partner[cf] % 3 : 0;
-            t.is_right[cf] = (uint8_t)(t.eright[e] == c + 1);
+    cells.run([&](int64_t c0, int64_t c1, int) {
+        for (int64_t c = c0; c < c1; c++) {
+            int nn = 3;
+            for (int f = 0; f < 3; f++) {
+                const int64_t cf = 3 * c + f;
+                const int e = face_edge[cf] - 1;
+                t.celledge[cf] = e + 1;
+                int nbr = t.eleft[e] == c + 1 ? t.eright[e] : t.eleft[e];
+                if (nbr == -1) { nbr *= t.elog[e]; nn--; }
+                t.neicell[cf] = nbr;
+                t.nb[cf] = nbr > 0 ? nbr - 1 : nbr;
+                t.nb_slot[cf] = partner[cf] >= 0 ? partner[cf] % 3 : 0;
+                t.is_right[cf] = (uint8_t)(t.eright[e] == c + 1);
+            }
+            t.clog[c] = nn;
         }
-        t.clog[c] = nn;
-    }
+    });
     t.wall_box = wall_box;
     return E2D_OK;
 }

@@ -111,6 +111,30 @@ def test_reference_main_runs_on_gb300_solver(lib):
         # the field written by the reference's Output() is the converged one
         vals = np.loadtxt(os.path.join(d, "unresult.plt"), skiprows=6, max_rows=mesh.info().nnode)
         assert np.std(vals[:, 2]) > 1e-4  # density varies over the nodes
+        # content parity of the writers: the e2d_solve command on the same files
+        # writes unresult.plt and unairfoilpress.plt equal to what the
+        # reference's own Node_Computing / Output (gpu_fvm.cu:71-195) write from
+        # the same state, value for value at the printed precision
+        d2 = os.path.join(d, "cli")
+        os.makedirs(d2)
+        mesh.write(os.path.join(d2, "2822-3k.dat"))
+        with open(os.path.join(d2, "input.dat"), "w") as f:
+            f.write(INPUT + "\n")
+        res2 = subprocess.run([pkg_build.CLI], cwd=d2, capture_output=True, text=True, timeout=300)
+        assert res2.returncode == 0, res2.stdout[-2000:] + res2.stderr[-2000:]
+        for name in ("unresult.plt", "unairfoilpress.plt"):
+            ref_txt = open(os.path.join(d, name)).read().splitlines()
+            cli_txt = open(os.path.join(d2, name)).read().splitlines()
+            assert len(ref_txt) == len(cli_txt), name
+            hdr = 6 if name == "unresult.plt" else 3
+            assert ref_txt[:hdr] == cli_txt[:hdr], name
+            a = np.array([[float(v) for v in l.split()] for l in ref_txt[hdr:]], dtype=object)
+            b = np.array([[float(v) for v in l.split()] for l in cli_txt[hdr:]], dtype=object)
+            for ra, rb in zip(a, b):
+                np.testing.assert_allclose(np.array(rb, float), np.array(ra, float), rtol=0, atol=2e-10,
+                                           err_msg=name)
+            differing = sum(x != y for x, y in zip(ref_txt, cli_txt))
+            print(f"{name}: {len(ref_txt)} lines, {differing} differ in text (last printed digit)")
 
 
 @pytest.mark.gpu
