@@ -646,16 +646,25 @@ __global__ void E2D_LB_FLUX k_flux_tile(MeshDev<T> m, Flow<T> f, const V4<T> *__
 // Faces to cells of other warps and boundary faces are evaluated by their own
 // cell, as in flux_cell.  In Morton order about three quarters of the interior
 // faces of a 4.2M-cell mesh lie inside a warp, so a warp evaluates about 1.9
-// fluxes per cell instead of 3.  The warp first lists the faces it must
-// evaluate, spreads them over its lanes, keeps the fluxes in shared memory,
-// and then every cell sums its three faces in face order with the reference's
-// signs.  The fluxes are the same bits as flux_cell's (face_flux_of with the
-// same inputs) summed in the same order, so the result is bit-identical.
-// Every lane of the warp must call it; `live` is false for lanes past the
-// last cell.
+// fluxes per cell instead of 3.
+//   1. every lane requests its own cell's face vectors and face-side states
+//      (and the far side of faces to other warps) at once, and parks them in
+//      shared memory;
+//   2. the warp lists the faces it must evaluate (a prefix sum over lanes);
+//   3. the list is spread over the lanes, inputs read back from shared
+//      memory (the far side of a face inside the warp is its neighbour's own
+//      face-side state), fluxes kept in shared memory;
+//   4. every cell sums its three faces in face order with the reference's
+//      signs.
+// The fluxes are the same bits as flux_cell's (face_flux_of with the same
+// inputs) summed in the same order, so the result is bit-identical.  Every
+// lane of the warp must call it; `live` is false for lanes past the last cell.
 template <typename T> struct WarpFlux {
-    V4<T> F[128];       // fluxes of the warp's evaluation list (at most 96)
-    int2 item[128];     // list entry: {(lane << 2) | face, face code}
+    V4<T> own[3][32];   // face-side state of face k of each lane's cell
+    V4<T> oth[3][32];   // far side of the faces to cells outside the warp
+    V2<T> S[3][32];     // face vectors
+    V4<T> F[96];        // fluxes of the warp's evaluation list (at most 96)
+    int2 item[96];      // list entry: {(lane << 2) | face, face code}
     int offmask[32];    // per lane: (first list index << 3) | mask of own entries
 };
 
@@ -664,19 +673,36 @@ __device__ __forceinline__ void flux_warp(const MeshDev<T> &m, const Flow<T> &f,
                                           const V4<T> *__restrict__ FS, V4<T> *__restrict__ res,
                                           WarpFlux<T> &w) {
     const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31, base = i - lane;
+    const int n = m.n, lane = threadIdx.x & 31, base = i - lane;
     const int4 tp = live ? m.topo[i] : make_int4(-3, -3, -3, 0);
     const int code[3] = {tp.x, tp.y, tp.z};
     // faces this lane evaluates: boundary faces, faces to other warps, and
     // faces inside the warp of which this cell is the left cell
-    unsigned mask = 0;
+    unsigned mask = 0, cross = 0;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         const int c = code[k];
         if (!live) continue;
         if (c < 0) { mask |= 1u << k; continue; }
         const bool inside = (unsigned)((c >> 3) - base) < 32u;
+        if (!inside) cross |= 1u << k;
         if (!inside || !((c >> 2) & 1)) mask |= 1u << k;
+    }
+    if (live) {
+        V2<T> S[3];
+        V4<T> own[3], oth[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            S[k] = m.S[k * n + i];
+            own[k] = FS[k * n + i];
+            if (cross & (1u << k)) oth[k] = FS[(code[k] & 3) * n + (code[k] >> 3)];
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            w.S[k][lane] = S[k];
+            w.own[k][lane] = own[k];
+            if (cross & (1u << k)) w.oth[k][lane] = oth[k];
+        }
     }
     const int cnt = __popc(mask);
     int incl = cnt;
@@ -697,8 +723,14 @@ __device__ __forceinline__ void flux_warp(const MeshDev<T> &m, const Flow<T> &f,
     __syncwarp();
     for (int q = lane; q < total; q += 32) {
         const int2 it = w.item[q];
+        const int tt = it.x >> 2, k = it.x & 3, c = it.y;
+        V4<T> oth = w.own[k][tt];
+        if (c >= 0) {
+            const int nl = (c >> 3) - base;
+            oth = (unsigned)nl < 32u ? w.own[c & 3][nl] : w.oth[k][tt];
+        }
         bool right;
-        w.F[q] = face_flux(m, f, base + (it.x >> 2), it.x & 3, it.y, FS, right);
+        w.F[q] = face_flux_of(f, c, w.S[k][tt], w.own[k][tt], oth, right);
     }
     __syncwarp();
     if (live) {
@@ -717,7 +749,7 @@ __device__ __forceinline__ void flux_warp(const MeshDev<T> &m, const Flow<T> &f,
                 idx = (om >> 3) + __popc((unsigned)(om & 7) & ((1u << (c & 3)) - 1u));
                 right = true;
             }
-            const V4<T> F = w.F[idx & 127];
+            const V4<T> F = w.F[min(idx, 95)];
             if (right) { r.x -= F.x; r.y -= F.y; r.z -= F.z; r.w -= F.w; }
             else { r.x += F.x; r.y += F.y; r.z += F.z; r.w += F.w; }
         }
