@@ -300,6 +300,80 @@ __device__ __forceinline__ V4<float> roe<float>(const V4<float> &LW, const V4<fl
 }
 
 // ---------------------------------------------------------------------------
+// Packed FP32 arithmetic: two independent lanes per instruction (the f32x2
+// add / multiply / fused multiply-add of sm_100 and later), each lane
+// rounding exactly like the scalar operation it replaces.  The reciprocals and
+// square roots stay scalar per lane.
+__device__ __forceinline__ float2 p2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(1.0f / a.x, 1.0f / a.y); }
+__device__ __forceinline__ float2 sqrt2(float2 a) { return make_float2(sqrtf(a.x), sqrtf(a.y)); }
+
+// Harten's fix of one eigenvalue pair: (l^2 + eps^2) / (2 eps) inside the
+// band, |l| outside (as roe<float>).
+__device__ __forceinline__ float2 harten2(float2 l, float eps, float e2, float ie) {
+    const float2 q = mul2(fma2(l, l, p2(e2)), p2(ie));
+    return make_float2(fabsf(l.x) < eps ? q.x : fabsf(l.x), fabsf(l.y) < eps ? q.y : fabsf(l.y));
+}
+
+// Two Roe fluxes at once, lane j of every pair belonging to face j: the same
+// operations as roe<float> in the same order, packed, so each lane's result
+// has the bits the scalar form gives.  Lx..Lw / Rx..Rw are the components of
+// the left / right states of the two faces.
+struct Roe2In {
+    float2 Lx, Ly, Lz, Lw, Rx, Ry, Rz, Rw, nx, ny;
+};
+
+__device__ __forceinline__ void roe_pair(const Roe2In &q, float g, float epsilon, float2 F[4]) {
+    const float gm1 = g - 1.0f;
+    const float2 il = rcp2(q.Lx), ir = rcp2(q.Rx);
+    const float2 U0 = mul2(q.Ly, il), V0 = mul2(q.Lz, il), U1 = mul2(q.Ry, ir), V1 = mul2(q.Rz, ir);
+    const float2 P0 = mul2(p2(gm1), fma2(mul2(p2(-0.5f), q.Lx), fma2(U0, U0, mul2(V0, V0)), q.Lw));
+    const float2 P1 = mul2(p2(gm1), fma2(mul2(p2(-0.5f), q.Rx), fma2(U1, U1, mul2(V1, V1)), q.Rw));
+    const float2 H0 = mul2(add2(q.Lw, P0), il), H1 = mul2(add2(q.Rw, P1), ir);
+    const float2 M0 = fma2(U0, q.nx, mul2(V0, q.ny)), M1 = fma2(U1, q.nx, mul2(V1, q.ny));
+    const float2 DVC = sub2(M1, M0);
+    const float2 sl = sqrt2(q.Lx), sr = sqrt2(q.Rx);
+    const float2 ROUB = mul2(sl, sr), is = rcp2(add2(sl, sr));
+    const float2 UB = mul2(fma2(U0, sl, mul2(U1, sr)), is);
+    const float2 VB = mul2(fma2(V0, sl, mul2(V1, sr)), is);
+    const float2 HB = mul2(fma2(H0, sl, mul2(H1, sr)), is);
+    const float2 QB = fma2(UB, UB, mul2(VB, VB));
+    const float2 AB = sqrt2(mul2(p2(gm1), fma2(p2(-0.5f), QB, HB)));
+    const float2 VC = fma2(UB, q.nx, mul2(VB, q.ny));
+    const float e2 = epsilon * epsilon, ie = 0.5f / epsilon;
+    const float2 l0 = sub2(VC, AB), l2 = add2(VC, AB);
+    const float2 AD0 = harten2(l0, epsilon, e2, ie);
+    const float2 AD1 = harten2(VC, epsilon, e2, ie);
+    const float2 AD2 = harten2(l2, epsilon, e2, ie);
+    const float2 dP = sub2(P1, P0), ia2 = rcp2(mul2(AB, AB)), rad = mul2(mul2(ROUB, AB), DVC),
+                 h2 = mul2(p2(0.5f), ia2);
+    const float2 F00 = mul2(mul2(AD0, sub2(dP, rad)), h2);
+    const float2 F20 = mul2(mul2(AD2, add2(dP, rad)), h2);
+    const float2 F10 = mul2(AD1, fma2(neg2(dP), ia2, sub2(q.Rx, q.Lx)));
+    const float2 du = sub2(U1, U0), dv = sub2(V1, V0), aR = mul2(AD1, ROUB);
+    const float2 nAB = neg2(AB), nDVC = neg2(DVC);
+    const float2 F01 = mul2(F00, fma2(nAB, q.nx, UB)), F21 = mul2(F20, fma2(AB, q.nx, UB));
+    const float2 F02 = mul2(F00, fma2(nAB, q.ny, VB)), F22 = mul2(F20, fma2(AB, q.ny, VB));
+    const float2 F03 = mul2(F00, fma2(nAB, VC, HB)), F23 = mul2(F20, fma2(AB, VC, HB));
+    const float2 F11 = fma2(F10, UB, mul2(aR, fma2(nDVC, q.nx, du)));
+    const float2 F12 = fma2(F10, VB, mul2(aR, fma2(nDVC, q.ny, dv)));
+    const float2 F13 = fma2(mul2(F10, p2(0.5f)), QB, mul2(aR, fma2(UB, du, fma2(VB, dv, mul2(nDVC, VC)))));
+    const float2 WL0 = mul2(q.Lx, M0), WR0 = mul2(q.Rx, M1);
+    const float2 WL1 = fma2(U0, WL0, mul2(q.nx, P0)), WR1 = fma2(U1, WR0, mul2(q.nx, P1));
+    const float2 WL2 = fma2(V0, WL0, mul2(q.ny, P0)), WR2 = fma2(V1, WR0, mul2(q.ny, P1));
+    const float2 WL3 = mul2(WL0, H0), WR3 = mul2(WR0, H1);
+    F[0] = mul2(p2(0.5f), sub2(add2(WL0, WR0), add2(add2(F00, F10), F20)));
+    F[1] = mul2(p2(0.5f), sub2(add2(WL1, WR1), add2(add2(F01, F11), F21)));
+    F[2] = mul2(p2(0.5f), sub2(add2(WL2, WR2), add2(add2(F02, F12), F22)));
+    F[3] = mul2(p2(0.5f), sub2(add2(WL3, WR3), add2(add2(F03, F13), F23)));
+}
+
+// ---------------------------------------------------------------------------
 // Pass A: gpu_solver.cu:137-223 (kernel_Boundary), 225-383 (kernel_Gradient),
 // 385-454 (kernel_deltT), 456-549 (kernel_Limiter / kernel_LBJinterpolate),
 // and the dt part of 768-878 (kernel_Flux_e2c).
@@ -518,19 +592,21 @@ __device__ __forceinline__ void flux_cell(const MeshDev<T> &m, const Flow<T> &f,
     res[i] = r;
 }
 
-// Flux of face k of cell i, times |S|, in the edge's orientation (the
-// reference's Res_e.left of gpu_solver.cu:738-745); *right tells whether cell
-// i is the edge's right cell.
+// Inputs of the Roe flux of one face in the edge's orientation: left state a,
+// right state b (the ghost across a boundary face), unit normal (nx, ny) of
+// the edge and the face length vn; *right tells whether the cell is the
+// edge's right cell.
 template <typename T>
-__device__ __forceinline__ V4<T> face_flux_of(const Flow<T> &f, const int code, const V2<T> S, const V4<T> own,
-                                              const V4<T> oth, bool &right) {
-    const T vn = tsqrt(S.y * S.y + S.x * S.x);
-    T nx = S.x / vn, ny = S.y / vn;
-    // one Roe call site for every face, with the left state first: both cells
-    // of a face run the same instructions on the same inputs (their normals
-    // are exact negatives), so they get the same bits even where the
-    // compiler contracts multiply-adds
-    V4<T> a = own, b;
+__device__ __forceinline__ void face_inputs(const Flow<T> &f, const int code, const V2<T> S, const V4<T> own,
+                                            const V4<T> oth, V4<T> &a, V4<T> &b, T &nx, T &ny, T &vn,
+                                            bool &right) {
+    vn = tsqrt(S.y * S.y + S.x * S.x);
+    nx = S.x / vn;
+    ny = S.y / vn;
+    // the left state first: both cells of a face run the same instructions on
+    // the same inputs (their normals are exact negatives), so they get the
+    // same bits
+    a = own;
     right = false;
     if (code >= 0) {
         right = (code >> 2) & 1;
@@ -539,10 +615,83 @@ __device__ __forceinline__ V4<T> face_flux_of(const Flow<T> &f, const int code, 
     } else {
         b = ghost(code, own, S.x, S.y, f);
     }
+}
+
+// Flux of face k of cell i, times |S|, in the edge's orientation (the
+// reference's Res_e.left of gpu_solver.cu:738-745); *right tells whether cell
+// i is the edge's right cell.
+template <typename T>
+__device__ __forceinline__ V4<T> face_flux_of(const Flow<T> &f, const int code, const V2<T> S, const V4<T> own,
+                                              const V4<T> oth, bool &right) {
+    V4<T> a, b;
+    T nx, ny, vn;
+    face_inputs(f, code, S, own, oth, a, b, nx, ny, vn, right);
+    // one Roe call site for every face
     V4<T> F = roe(a, b, nx, ny, f.gamma, f.eps_entropy);
     F.x *= vn; F.y *= vn; F.z *= vn; F.w *= vn;
     return F;
 }
+
+// FP32: faces 0 and 1 as one packed pair, face 2 in the first lane of a
+// second pair (its second lane repeats it); every flux has the bits of the
+// scalar form, summed in the same order.  E2D_FLUX_PACKED=0 builds the scalar
+// form (flux_cell above) instead.
+#ifndef E2D_FLUX_PACKED
+#define E2D_FLUX_PACKED 1
+#endif
+#if E2D_FLUX_PACKED
+template <>
+__device__ __forceinline__ void flux_cell<float>(const MeshDev<float> &m, const Flow<float> &f, const int i,
+                                                 const V4<float> *__restrict__ FS, V4<float> *__restrict__ res) {
+    const int n = m.n;
+    const int4 tp = m.topo[i];
+    const int code[3] = {tp.x, tp.y, tp.z};
+    V2<float> S[3];
+    V4<float> own[3], oth[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        S[k] = m.S[k * n + i];
+        own[k] = FS[k * n + i];
+        if (code[k] >= 0) oth[k] = FS[(code[k] & 3) * n + (code[k] >> 3)];
+    }
+    V4<float> r;
+    r.x = 0.0f; r.y = 0.0f; r.z = 0.0f; r.w = 0.0f;
+#pragma unroll
+    for (int pr = 0; pr < 2; pr++) {
+        const int j0 = 2 * pr, j1 = pr == 0 ? 1 : 2;
+        V4<float> a0, b0, a1, b1;
+        float nx0, ny0, vn0, nx1, ny1, vn1;
+        bool r0, r1;
+        face_inputs(f, code[j0], S[j0], own[j0], oth[j0], a0, b0, nx0, ny0, vn0, r0);
+        if (pr == 0) face_inputs(f, code[j1], S[j1], own[j1], oth[j1], a1, b1, nx1, ny1, vn1, r1);
+        else { a1 = a0; b1 = b0; nx1 = nx0; ny1 = ny0; vn1 = vn0; r1 = r0; }
+        Roe2In q;
+        q.Lx = make_float2(a0.x, a1.x); q.Ly = make_float2(a0.y, a1.y);
+        q.Lz = make_float2(a0.z, a1.z); q.Lw = make_float2(a0.w, a1.w);
+        q.Rx = make_float2(b0.x, b1.x); q.Ry = make_float2(b0.y, b1.y);
+        q.Rz = make_float2(b0.z, b1.z); q.Rw = make_float2(b0.w, b1.w);
+        q.nx = make_float2(nx0, nx1); q.ny = make_float2(ny0, ny1);
+        float2 G[4];
+        roe_pair(q, f.gamma, f.eps_entropy, G);
+        const float2 v2 = make_float2(vn0, vn1);
+        float F0[4], F1[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const float2 h = mul2(G[c], v2);
+            F0[c] = h.x;
+            F1[c] = h.y;
+        }
+        // faces in order 0, 1, 2 with the reference's signs
+        if (r0) { r.x -= F0[0]; r.y -= F0[1]; r.z -= F0[2]; r.w -= F0[3]; }
+        else { r.x += F0[0]; r.y += F0[1]; r.z += F0[2]; r.w += F0[3]; }
+        if (pr == 0) {
+            if (r1) { r.x -= F1[0]; r.y -= F1[1]; r.z -= F1[2]; r.w -= F1[3]; }
+            else { r.x += F1[0]; r.y += F1[1]; r.z += F1[2]; r.w += F1[3]; }
+        }
+    }
+    res[i] = r;
+}
+#endif
 
 template <typename T>
 __device__ __forceinline__ V4<T> face_flux(const MeshDev<T> &m, const Flow<T> &f, const int i, const int k,
@@ -640,151 +789,14 @@ __global__ void E2D_LB_FLUX k_flux_tile(MeshDev<T> m, Flow<T> f, const V4<T> *__
     flux_tile(m, f, base, min((int)blockDim.x, m.n - base), FS, res);
 }
 
-// Pass B for the 32 consecutive cells of one warp with each interior face
-// between two of them evaluated once, by its left cell's lane, and handed to
-// the right cell through shared memory (warp-synchronous: no block barrier).
-// Faces to cells of other warps and boundary faces are evaluated by their own
-// cell, as in flux_cell.  In Morton order about three quarters of the interior
-// faces of a 4.2M-cell mesh lie inside a warp, so a warp evaluates about 1.9
-// fluxes per cell instead of 3.
-//   1. every lane requests its own cell's face vectors and face-side states
-//      (and the far side of faces to other warps) at once, and parks them in
-//      shared memory;
-//   2. the warp lists the faces it must evaluate (a prefix sum over lanes);
-//   3. the list is spread over the lanes, inputs read back from shared
-//      memory (the far side of a face inside the warp is its neighbour's own
-//      face-side state), fluxes kept in shared memory;
-//   4. every cell sums its three faces in face order with the reference's
-//      signs.
-// The fluxes are the same bits as flux_cell's (face_flux_of with the same
-// inputs) summed in the same order, so the result is bit-identical.  Every
-// lane of the warp must call it; `live` is false for lanes past the last cell.
-template <typename T> struct WarpFlux {
-    V4<T> own[3][32];   // face-side state of face k of each lane's cell
-    V4<T> oth[3][32];   // far side of the faces to cells outside the warp
-    V2<T> S[3][32];     // face vectors
-    V4<T> F[96];        // fluxes of the warp's evaluation list (at most 96)
-    int2 item[96];      // list entry: {(lane << 2) | face, face code}
-    int offmask[32];    // per lane: (first list index << 3) | mask of own entries
-};
-
-template <typename T>
-__device__ __forceinline__ void flux_warp(const MeshDev<T> &m, const Flow<T> &f, const int i, const bool live,
-                                          const V4<T> *__restrict__ FS, V4<T> *__restrict__ res,
-                                          WarpFlux<T> &w) {
-    const unsigned full = 0xffffffffu;
-    const int n = m.n, lane = threadIdx.x & 31, base = i - lane;
-    const int4 tp = live ? m.topo[i] : make_int4(-3, -3, -3, 0);
-    const int code[3] = {tp.x, tp.y, tp.z};
-    // faces this lane evaluates: boundary faces, faces to other warps, and
-    // faces inside the warp of which this cell is the left cell
-    unsigned mask = 0, cross = 0;
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const int c = code[k];
-        if (!live) continue;
-        if (c < 0) { mask |= 1u << k; continue; }
-        const bool inside = (unsigned)((c >> 3) - base) < 32u;
-        if (!inside) cross |= 1u << k;
-        if (!inside || !((c >> 2) & 1)) mask |= 1u << k;
-    }
-    if (live) {
-        V2<T> S[3];
-        V4<T> own[3], oth[3];
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            S[k] = m.S[k * n + i];
-            own[k] = FS[k * n + i];
-            if (cross & (1u << k)) oth[k] = FS[(code[k] & 3) * n + (code[k] >> 3)];
-        }
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            w.S[k][lane] = S[k];
-            w.own[k][lane] = own[k];
-            if (cross & (1u << k)) w.oth[k][lane] = oth[k];
-        }
-    }
-    const int cnt = __popc(mask);
-    int incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(full, incl, o);
-        if (lane >= o) incl += v;
-    }
-    const int total = __shfl_sync(full, incl, 31);
-    const int off = incl - cnt;
-    w.offmask[lane] = (off << 3) | (int)mask;
-    {
-        int j = off;
-#pragma unroll
-        for (int k = 0; k < 3; k++)
-            if (mask & (1u << k)) w.item[j++] = make_int2((lane << 2) | k, code[k]);
-    }
-    __syncwarp();
-    for (int q = lane; q < total; q += 32) {
-        const int2 it = w.item[q];
-        const int tt = it.x >> 2, k = it.x & 3, c = it.y;
-        V4<T> oth = w.own[k][tt];
-        if (c >= 0) {
-            const int nl = (c >> 3) - base;
-            oth = (unsigned)nl < 32u ? w.own[c & 3][nl] : w.oth[k][tt];
-        }
-        bool right;
-        w.F[q] = face_flux_of(f, c, w.S[k][tt], w.own[k][tt], oth, right);
-    }
-    __syncwarp();
-    if (live) {
-        V4<T> r;
-        r.x = T(0.0); r.y = T(0.0); r.z = T(0.0); r.w = T(0.0);
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            const int c = code[k];
-            int idx;
-            bool right;
-            if (mask & (1u << k)) {
-                idx = off + __popc(mask & ((1u << k) - 1u));
-                right = c >= 0 && ((c >> 2) & 1);
-            } else {  // inside face evaluated by its left cell
-                const int om = w.offmask[(c >> 3) - base];
-                idx = (om >> 3) + __popc((unsigned)(om & 7) & ((1u << (c & 3)) - 1u));
-                right = true;
-            }
-            const V4<T> F = w.F[min(idx, 95)];
-            if (right) { r.x -= F.x; r.y -= F.y; r.z -= F.z; r.w -= F.w; }
-            else { r.x += F.x; r.y += F.y; r.z += F.z; r.w += F.w; }
-        }
-        res[i] = r;
-    }
-    __syncwarp();  // w may be reused by this warp's next tile
-}
-
-// Pass-B form of the FP32 stencil: the warp form above (E2D_FLUX_WARP,
-// default) or flux_cell's three evaluations per cell.  The warp form takes
-// one WarpFlux of dynamic shared memory per warp of the block.
-#ifndef E2D_FLUX_WARP
-#define E2D_FLUX_WARP 1
-#endif
-
-extern __shared__ __align__(16) unsigned char dyn_smem[];
-
-// Dynamic shared memory of one pass-B launch of `block` threads.
-template <typename T> inline size_t flux_smem(int block) {
-    return (!FluxTiled<T>::value && E2D_FLUX_WARP != 0) ? sizeof(WarpFlux<T>) * (size_t)(block / 32) : 0;
-}
-
 template <typename T>
 __global__ void E2D_LB_FLUX k_flux(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ FS,
                                    V4<T> *__restrict__ res, const Ctl *__restrict__ ctl) {
     wait_prior_grid();
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if constexpr (E2D_FLUX_WARP != 0) {
-        WarpFlux<T> *wf = reinterpret_cast<WarpFlux<T> *>(dyn_smem);
-        flux_warp(m, f, i, i < m.n, FS, res, wf[threadIdx.x >> 5]);
-    } else {
-        if (i >= m.n) return;
-        flux_cell(m, f, i, FS, res);
-    }
+    if (i >= m.n) return;
+    flux_cell(m, f, i, FS, res);
 }
 
 // Sum of the interior neighbours' values in face order (gpu_solver.cu:1658-1666)
@@ -959,10 +971,6 @@ __global__ void E2D_LB_FLUX kb_flux(MeshDev<T> m, BatchDev<T> b, int ntiles, con
         const Flow<T> f = b.flows[tc];
         if constexpr (FluxTiled<T>::value) {
             flux_tile(m, f, base, max(0, min((int)blockDim.x, b.case_end[tc] - base)), FS, res);
-        } else if constexpr (E2D_FLUX_WARP != 0) {
-            WarpFlux<T> *wf = reinterpret_cast<WarpFlux<T> *>(dyn_smem);
-            const int i = base + threadIdx.x;
-            flux_warp(m, f, i, i < b.case_end[tc], FS, res, wf[threadIdx.x >> 5]);
         } else {
             const int i = base + threadIdx.x;
             if (i < b.case_end[tc]) flux_cell(m, f, i, FS, res);
@@ -1013,7 +1021,7 @@ template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream
         V4<T> *Wout = last ? p.W[0] : p.W[1];
         if (p.options) launch_chained(kb_faces<T, true>, G, B, s, p.m, p.b, NT, Wcur, p.FS, p.dt, p.phi, st);
         else launch_chained(kb_faces<T, false>, G, B, s, p.m, p.b, NT, Wcur, p.FS, p.dt, p.phi, st);
-        launch_chained_smem(kb_flux<T>, G, B, flux_smem<T>(B), s, p.m, p.b, NT, p.FS, p.res);
+        launch_chained(kb_flux<T>, G, B, s, p.m, p.b, NT, p.FS, p.res);
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
             V4<T> *dst = p.sm[sw & 1];
@@ -1075,7 +1083,7 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
         if (opt) launch_chained(k_faces<T, true>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
         else launch_chained(k_faces<T, false>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
         if (FluxTiled<T>::value) launch_chained(k_flux_tile<T>, G, B, s, p.m, p.f, p.FS, p.res, p.ctl);
-        else launch_chained_smem(k_flux<T>, G, B, flux_smem<T>(B), s, p.m, p.f, p.FS, p.res, p.ctl);
+        else launch_chained(k_flux<T>, G, B, s, p.m, p.f, p.FS, p.res, p.ctl);
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
             V4<T> *dst = p.sm[sw & 1];
@@ -1108,7 +1116,7 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
         done();
         mark(1);
         if (FluxTiled<T>::value) k_flux_tile<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
-        else k_flux<T><<<G, B, flux_smem<T>(B), s>>>(p.m, p.f, p.FS, p.res, p.ctl);
+        else k_flux<T><<<G, B, 0, s>>>(p.m, p.f, p.FS, p.res, p.ctl);
         done();
         const V4<T> *src = p.res;
         for (int sw = 0; sw + 1 < p.sweeps; sw++) {
