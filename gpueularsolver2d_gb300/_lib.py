@@ -36,7 +36,8 @@ class Params(ctypes.Structure):
         ("verbose", ctypes.c_int32), ("limiter_freeze", ctypes.c_int32),
         ("limiter", ctypes.c_int32), ("limiter_k", ctypes.c_double),
         ("limiter_freeze_resd", ctypes.c_double), ("global_dt", ctypes.c_int32),
-        ("far_field_fix", ctypes.c_int32),
+        ("far_field_fix", ctypes.c_int32), ("first_order_iters", ctypes.c_int32),
+        ("positivity_fix", ctypes.c_int32),
     ]
 
 

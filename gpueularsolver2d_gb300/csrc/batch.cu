@@ -66,7 +66,9 @@ template <typename T> struct BatchT : BatchBase {
         bool freeze = false;
         for (auto &p : P) freeze = freeze || p.limiter_freeze > 0 || p.limiter_freeze_resd > 0.0;
         plan.options = freeze;
-        for (auto &p : P) plan.options = plan.options || p.limiter == 1 || p.global_dt != 0;
+        for (auto &p : P)
+            plan.options = plan.options || p.limiter == 1 || p.global_dt != 0 || p.first_order_iters > 0 ||
+                           p.positivity_fix != 0;
         int nmax = 0;
         for (auto &l : *L) nmax = std::max(nmax, l.n);
         const int maxtiles = (n + 31) / 32;
@@ -129,6 +131,7 @@ template <typename T> struct BatchT : BatchBase {
             f.dt_cap = (T)p.dt_cap; f.eps_entropy = (T)p.entropy_eps; f.irs_eps = (T)p.irs_eps;
             f.venk_k3 = (T)(p.limiter_k * p.limiter_k * p.limiter_k); f.limiter = p.limiter;
             f.global_dt = p.global_dt;
+            f.first_order = p.first_order_iters; f.positivity = p.positivity_fix;
         }
         CK(cudaMemcpy(topo, ht.data(), sizeof(int4) * n, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(S, hS.data(), sizeof(T) * hS.size(), cudaMemcpyHostToDevice));

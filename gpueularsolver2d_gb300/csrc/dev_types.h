@@ -36,6 +36,8 @@ template <typename T> struct Flow {
     T venk_k3;    // K^3 of the Venkatakrishnan option
     int limiter;  // 0 reference, 1 Venkatakrishnan
     int global_dt;  // 1: every cell advances with the smallest local step (option)
+    int first_order;  // > 0: first-order faces while fewer iterations are done (option)
+    int positivity;   // 1: a non-physical reconstructed face side falls back to the cell state (option)
 };
 
 // Cell-local mesh data in internal order (n cells).

@@ -418,13 +418,15 @@ __device__ __forceinline__ float cell_area<float>(const MeshDev<float> &m, const
 }
 
 // Returns the cell's local time step (also stored in dt[i]).  OPT compiles in
-// the scheme options (smooth limiter, frozen limiter values); without them the
-// reference configuration runs in fewer registers (no spills at the FP32
-// occupancy target) with the same arithmetic.
+// the scheme options (smooth limiter, frozen limiter values, first-order
+// faces, positivity fallback); without them the reference configuration runs
+// in fewer registers (no spills at the FP32 occupancy target) with the same
+// arithmetic.  first: this iteration uses first-order faces (option).
 template <typename T, bool OPT>
 __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, const int i,
                                         const V4<T> *__restrict__ W, V4<T> *__restrict__ FS,
-                                        T *__restrict__ dt, V4<T> *__restrict__ phi, const int frozen) {
+                                        T *__restrict__ dt, V4<T> *__restrict__ phi, const int frozen,
+                                        const bool first = false) {
     const int n = m.n;
     const int4 tp = m.topo[i];
     const int code[3] = {tp.x, tp.y, tp.z};
@@ -468,7 +470,7 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         V4<T> o = U;
-        if (code[k] >= 0) {
+        if (code[k] >= 0 && !(OPT && first)) {
             const V2<T> r = face_offset(m, S, k, i);
             const bool reuse = OPT && phi && frozen;
             V4<T> pf;
@@ -498,6 +500,12 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
                 d[q] = madd(delt2, fi, u);
             }
             o.x = d[0]; o.y = d[1]; o.z = d[2]; o.w = d[3];
+            if (OPT && f.positivity) {
+                // positivity fallback (option): a face side with a density or
+                // pressure that is not positive takes the cell state
+                const T q = T(0.5) * (d[1] * d[1] + d[2] * d[2]) / d[0];
+                if (!(d[0] > T(0)) || !((f.gamma - T(1.0)) * (d[3] - q) > T(0))) o = U;
+            }
             if (OPT && phi && !frozen) {
                 V4<T> pw;
                 pw.x = ph[0]; pw.y = ph[1]; pw.z = ph[2]; pw.w = ph[3];
@@ -539,19 +547,20 @@ __global__ void E2D_LB_FACES k_faces(MeshDev<T> m, Flow<T> f, const V4<T> *__res
     wait_prior_grid();
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool first = OPT && ctl->step < f.first_order;
     if (!OPT || !f.global_dt) {
         if (i >= m.n) return;
-        faces_cell<T, OPT>(m, f, i, W, FS, dt, phi, OPT && phi ? ctl->frozen : 0);
+        faces_cell<T, OPT>(m, f, i, W, FS, dt, phi, OPT && phi ? ctl->frozen : 0, first);
         return;
     }
     double v = __longlong_as_double((long long)kDtNone);
-    if (i < m.n) v = (double)faces_cell<T, OPT>(m, f, i, W, FS, dt, phi, phi ? ctl->frozen : 0);
+    if (i < m.n) v = (double)faces_cell<T, OPT>(m, f, i, W, FS, dt, phi, phi ? ctl->frozen : 0, first);
     block_min_dt(v, &ctl->dtmin[st]);
 }
 
 // True when a pass-A launch needs the option variant.
 template <typename T> inline bool faces_options(const Flow<T> &f, const void *phi) {
-    return phi != nullptr || f.limiter == 1 || f.global_dt != 0;
+    return phi != nullptr || f.limiter == 1 || f.global_dt != 0 || f.first_order > 0 || f.positivity != 0;
 }
 
 // Time step of cell i in RK stage st: its own, or with the global option the
@@ -954,7 +963,8 @@ __global__ void E2D_LB_FACES kb_faces(MeshDev<T> m, BatchDev<T> b, int ntiles, c
         int c;
         if (batch_cell(b, m.n, i, c)) {
             const Flow<T> f = b.flows[c];
-            v = (double)faces_cell<T, OPT>(m, f, i, W, FS, dt, phi, OPT && phi ? b.ctl[c].frozen : 0);
+            v = (double)faces_cell<T, OPT>(m, f, i, W, FS, dt, phi, OPT && phi ? b.ctl[c].frozen : 0,
+                                           OPT && b.ctl[c].step < f.first_order);
         }
         if (OPT && b.flows[tc].global_dt) block_min_dt(v, &b.ctl[tc].dtmin[st]);  // uniform over the block
     }

@@ -163,6 +163,7 @@ extern "C" int e2d_step_noalloc(int32_t ncell, const int32_t *topo, const double
     f.eps_entropy = p->entropy_eps; f.irs_eps = p->irs_eps;
     f.venk_k3 = p->limiter_k * p->limiter_k * p->limiter_k; f.limiter = p->limiter;
     f.global_dt = p->global_dt;
+    f.first_order = p->first_order_iters; f.positivity = p->positivity_fix;
     plan.hist = resid;
     plan.hist_cap = iterations;
     plan.stages = p->rk_stages;

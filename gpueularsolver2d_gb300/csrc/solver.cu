@@ -171,6 +171,8 @@ const char *param_error(const e2d_params *p) {
     if (p->limiter == E2D_LIMITER_VENKAT && !(p->limiter_k > 0.0)) return "limiter_k must be > 0";
     if (p->global_dt != 0 && p->global_dt != 1) return "global_dt must be 0 or 1";
     if (p->far_field_fix != 0 && p->far_field_fix != 1) return "far_field_fix must be 0 or 1";
+    if (p->first_order_iters < 0) return "first_order_iters must be >= 0";
+    if (p->positivity_fix != 0 && p->positivity_fix != 1) return "positivity_fix must be 0 or 1";
     return nullptr;
 }
 
@@ -238,6 +240,7 @@ template <typename T> struct SolverT : SolverBase {
         f.eps_entropy = (T)p.entropy_eps; f.irs_eps = (T)p.irs_eps;
         f.venk_k3 = (T)(p.limiter_k * p.limiter_k * p.limiter_k); f.limiter = p.limiter;
         f.global_dt = p.global_dt;
+        f.first_order = p.first_order_iters; f.positivity = p.positivity_fix;
         plan.ctl = ctl;
         plan.hist = nullptr;
         plan.hist_cap = 0;

@@ -101,6 +101,16 @@ typedef struct e2d_params {
                             Un / AIN > 1 with the dimensional AIN, which never
                             holds (gpu_solver.cu:79); 1: compares with the
                             non-dimensional free-stream sound speed 1/M     */
+    int32_t first_order_iters; /* option, no reference counterpart: 0
+                            (default) reconstructs every interior face
+                            (gpu_solver.cu:496-549); k > 0 uses the cell
+                            states themselves (first order, as the
+                            reference's boundary faces, 689-725) during the
+                            first k iterations of the solver's history      */
+    int32_t positivity_fix; /* option, no reference counterpart: 0 (default)
+                            keeps every limited reconstruction; 1 replaces a
+                            face side whose reconstructed density or
+                            pressure is not positive by the cell state      */
 } e2d_params;
 
 #define E2D_LIMITER_REFERENCE 0

@@ -628,6 +628,14 @@ static void stage_gradient(or_case *c) {
 static void reconstruct(const or_case *c, int cell, double midx, double midy, wst *out, double *phi) {
     const wst *w = &c->w[cell];
     double UI[4] = {w->d, w->du, w->dv, w->de};
+    /* first-order faces option (no reference counterpart): the cell state
+       itself during the first first_order_iters iterations, as the
+       reference's boundary faces (gpu_solver.cu:689-725) */
+    if (c->p.first_order_iters > 0 && c->step <= c->p.first_order_iters) {
+        memset(out, 0, sizeof *out);
+        out->d = UI[0]; out->du = UI[1]; out->dv = UI[2]; out->de = UI[3];
+        return;
+    }
     double r0 = midx - c->cx[cell], r1 = midy - c->cy[cell];
     const double *du = c->du + 8 * (size_t)cell;
     double delt2[4], fi = 1.0;
@@ -655,6 +663,14 @@ static void reconstruct(const or_case *c, int cell, double midx, double midy, ws
     memset(out, 0, sizeof *out);
     out->d = UI[0] + delt2[0]; out->du = UI[1] + delt2[1];
     out->dv = UI[2] + delt2[2]; out->de = UI[3] + delt2[3];
+    /* positivity fallback option (no reference counterpart): a face side
+       whose density or pressure is not positive takes the cell state */
+    if (c->p.positivity_fix) {
+        double q = 0.5 * (out->du * out->du + out->dv * out->dv) / out->d;
+        if (!(out->d > 0) || !((c->p.gamma - 1.0) * (out->de - q) > 0)) {
+            out->d = UI[0]; out->du = UI[1]; out->dv = UI[2]; out->de = UI[3];
+        }
+    }
 }
 
 /* gpu_solver.cu:651-764 (kernel_Flux2) and 385-454 (kernel_deltT) */

@@ -46,6 +46,8 @@ typedef struct or_params {
     double limiter_freeze_resd; /* option: freeze once Resd <= this        */
     int global_dt;            /* option: every cell uses min_j dt_j         */
     int far_field_fix;        /* option: supersonic test against 1/M        */
+    int first_order_iters;    /* option: first-order faces while step <= k  */
+    int positivity_fix;       /* option: non-physical face side -> cell state */
 } or_params;
 
 typedef struct or_case or_case;

@@ -27,7 +27,8 @@ class OrParams(ctypes.Structure):
         ("entropy_eps", ctypes.c_double), ("wall_box", ctypes.c_double),
         ("limiter_freeze", ctypes.c_int), ("limiter", ctypes.c_int), ("limiter_k", ctypes.c_double),
         ("limiter_freeze_resd", ctypes.c_double), ("global_dt", ctypes.c_int),
-        ("far_field_fix", ctypes.c_int),
+        ("far_field_fix", ctypes.c_int), ("first_order_iters", ctypes.c_int),
+        ("positivity_fix", ctypes.c_int),
     ]
 
 

@@ -35,6 +35,8 @@ def run_pair(mesh, oracle, nsteps, **kw):
     dict(ma=0.5, alpha_deg=1.0, cfl=1.5, global_dt=1, ordering=e2d.E2D_ORDER_MORTON),
     dict(ma=1.5, alpha_deg=0.0, cfl=1.0, far_field_fix=1, ordering=e2d.E2D_ORDER_MORTON),
     dict(ma=0.6, alpha_deg=1.0, cfl=1.5, ordering=e2d.E2D_ORDER_RCM),
+    dict(ma=0.7, alpha_deg=2.0, cfl=1.5, first_order_iters=10, ordering=e2d.E2D_ORDER_MORTON),
+    dict(ma=0.8, alpha_deg=1.25, cfl=2.0, positivity_fix=1, first_order_iters=3, ordering=e2d.E2D_ORDER_MORTON),
 ])
 def test_fp64_bit_exact_vs_oracle(lib, oracle, kw):
     mesh = e2d.Mesh.ogrid(48, 12, seed=7)
@@ -182,3 +184,32 @@ def test_state_roundtrip_and_forces(lib):
     assert np.array_equal(s2.state(), w)
     cl, cd = s.forces()
     assert np.isfinite(cl) and np.isfinite(cd)
+
+
+@pytest.mark.parametrize("prec", [e2d.E2D_FP64, e2d.E2D_FP32])
+def test_positivity_fix_on_cold_cells(lib, oracle, prec):
+    """The positivity fallback on a start state with cold cells (faces with
+    negative reconstructed pressure): FP64 equals the oracle bit for bit over
+    10 iterations, FP32 runs to the same finite state within 1e-3; without the
+    option the solver reports the divergence."""
+    from test_oracle_options import cold_cells_state
+    mesh = e2d.Mesh.ogrid(48, 12, seed=7)
+    w0 = cold_cells_state(oracle, mesh)
+    p = e2d.default_params(ma=0.8, alpha_deg=1.25, cfl=1.0, positivity_fix=1, precision=prec)
+    s = e2d.Solver(mesh, p)
+    s.set_state(w0)
+    s.step(10)
+    x, y, tri = mesh.nodes()
+    c = oracle.Case(x, y, tri, oracle.params_from_e2d(e2d.default_params(ma=0.8, alpha_deg=1.25, cfl=1.0,
+                                                                        positivity_fix=1)))
+    c.set_state(w0)
+    c.run(10)
+    if prec == e2d.E2D_FP64:
+        assert np.array_equal(s.state(), c.state())
+    else:
+        assert np.max(np.abs(s.state() - c.state())) / np.max(np.abs(c.state())) < 1e-3
+    q = e2d.Solver(mesh, e2d.default_params(ma=0.8, alpha_deg=1.25, cfl=1.0, precision=prec))
+    q.set_state(w0)
+    with pytest.raises(Exception, match="diverged|non-positive|NaN"):
+        q.step(10)
+
