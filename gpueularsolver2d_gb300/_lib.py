@@ -14,6 +14,7 @@ LIB_PATH = _build.LIB
 
 E2D_FP64, E2D_FP32 = 0, 1
 E2D_ORDER_FILE, E2D_ORDER_MORTON, E2D_ORDER_RCM = 0, 1, 2
+E2D_LIMITER_REFERENCE, E2D_LIMITER_VENKAT, E2D_LIMITER_CELL_BARTH, E2D_LIMITER_CELL_VENKAT = 0, 1, 2, 3
 
 
 class E2DError(RuntimeError):

@@ -9,7 +9,8 @@ import ctypes
 
 import numpy as np
 
-from ._lib import (E2D_FP32, E2D_FP64, E2D_ORDER_FILE, E2D_ORDER_MORTON, E2D_ORDER_RCM, MeshInfo, Params,
+from ._lib import (E2D_FP32, E2D_FP64, E2D_LIMITER_CELL_BARTH, E2D_LIMITER_CELL_VENKAT,  # noqa: F401
+                   E2D_LIMITER_REFERENCE, E2D_LIMITER_VENKAT, E2D_ORDER_FILE, E2D_ORDER_MORTON, E2D_ORDER_RCM, MeshInfo, Params,
                    check, load)
 
 __all__ = ["Mesh", "Solver", "Batch", "MLP", "Params", "default_params", "read_input", "E2D_FP32", "E2D_FP64",

@@ -67,7 +67,7 @@ template <typename T> struct BatchT : BatchBase {
         for (auto &p : P) freeze = freeze || p.limiter_freeze > 0 || p.limiter_freeze_resd > 0.0;
         plan.options = freeze;
         for (auto &p : P)
-            plan.options = plan.options || p.limiter == 1 || p.global_dt != 0 || p.first_order_iters > 0 ||
+            plan.options = plan.options || p.limiter != 0 || p.global_dt != 0 || p.first_order_iters > 0 ||
                            p.positivity_fix != 0;
         int nmax = 0;
         for (auto &l : *L) nmax = std::max(nmax, l.n);

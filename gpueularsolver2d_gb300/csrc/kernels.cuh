@@ -417,6 +417,26 @@ __device__ __forceinline__ float cell_area<float>(const MeshDev<float> &m, const
     return 0.5f * fmaf(S[1].x, S[2].y, -(S[1].y * S[2].x));
 }
 
+// Limiter value of one component on one face side from its reconstruction
+// difference delt2: kind 0 the reference's min(1, (Umax - U) / delt2) for
+// delt2 > 0, min(1, (Umin - U) / delt2) for delt2 < 0, 1 for delt2 == 0
+// (gpu_solver.cu:456-494; the bound is selected first so a warp divides once
+// whatever the signs of its lanes, and a NaN delt2 makes the face state NaN
+// whatever the value); kind 1 the Venkatakrishnan form on the same
+// differences (option).
+template <typename T>
+__device__ __forceinline__ T face_limiter(const int kind, const Flow<T> &f, const T A, const T umax, const T umin,
+                                          const T u, const T delt2) {
+    if (kind == 1) {
+        const T e2 = f.venk_k3 * A * tsqrt(A);
+        const T d1 = delt2 > T(0) ? umax - u : umin - u;
+        return delt2 == T(0) ? T(1.0)
+                             : (d1 * d1 + e2 + T(2) * delt2 * d1) / (d1 * d1 + T(2) * delt2 * delt2 + d1 * delt2 + e2);
+    }
+    const T bound = delt2 > T(0) ? umax : umin;
+    return delt2 == T(0) ? T(1.0) : tmin((bound - u) / delt2, T(1.0));
+}
+
 // Returns the cell's local time step (also stored in dt[i]).  OPT compiles in
 // the scheme options (smooth limiter, frozen limiter values, first-order
 // faces, positivity fallback); without them the reference configuration runs
@@ -467,12 +487,31 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
         umax[q] = tmax(comp(U, q), jmax[q]);
         umin[q] = tmin(comp(U, q), jmin[q]);
     }
+    const bool reuse = OPT && phi && frozen;
+    // cell-wise limiter options (2, 3): the smallest of the per-face values of
+    // the cell's interior faces (reference form, Venkatakrishnan form), the
+    // same value on every face of the cell
+    const bool cellwise = OPT && f.limiter >= 2;
+    T phic[4] = {T(1.0), T(1.0), T(1.0), T(1.0)};
+    if (cellwise && !reuse && !first) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) phic[q] = T(INFINITY);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            if (code[k] < 0) continue;
+            const V2<T> r = face_offset(m, S, k, i);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const T delt2 = madd(gx[q], r.x, gy[q] * r.y);
+                phic[q] = tmin(phic[q], face_limiter(f.limiter - 2, f, A, umax[q], umin[q], comp(U, q), delt2));
+            }
+        }
+    }
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         V4<T> o = U;
         if (code[k] >= 0 && !(OPT && first)) {
             const V2<T> r = face_offset(m, S, k, i);
-            const bool reuse = OPT && phi && frozen;
             V4<T> pf;
             if (reuse) pf = phi[k * n + i];
             T fi = T(1.0), d[4], ph[4];
@@ -481,21 +520,8 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
                 T delt2 = madd(gx[q], r.x, gy[q] * r.y);
                 T u = comp(U, q);
                 if (reuse) fi = comp(pf, q);
-                else if (OPT && f.limiter == 1) {
-                    // Venkatakrishnan on the per-face differences (option)
-                    const T e2 = f.venk_k3 * A * tsqrt(A);
-                    const T d1 = delt2 > T(0) ? umax[q] - u : umin[q] - u;
-                    fi = delt2 == T(0) ? T(1.0)
-                                       : (d1 * d1 + e2 + T(2) * delt2 * d1) /
-                                             (d1 * d1 + T(2) * delt2 * delt2 + d1 * delt2 + e2);
-                } else {
-                    // min(1, (Umax - U) / delt2) for delt2 > 0, min(1, (Umin - U) / delt2)
-                    // for delt2 < 0, 1 for delt2 == 0: the bound is selected first so a
-                    // warp divides once whatever the signs of its lanes.  (A NaN delt2
-                    // makes the face state NaN whatever fi is.)
-                    const T bound = delt2 > T(0) ? umax[q] : umin[q];
-                    fi = delt2 == T(0) ? T(1.0) : tmin((bound - u) / delt2, T(1.0));
-                }
+                else if (cellwise) fi = phic[q];
+                else fi = face_limiter(OPT ? f.limiter : 0, f, A, umax[q], umin[q], u, delt2);
                 ph[q] = fi;
                 d[q] = madd(delt2, fi, u);
             }
@@ -560,7 +586,7 @@ __global__ void E2D_LB_FACES k_faces(MeshDev<T> m, Flow<T> f, const V4<T> *__res
 
 // True when a pass-A launch needs the option variant.
 template <typename T> inline bool faces_options(const Flow<T> &f, const void *phi) {
-    return phi != nullptr || f.limiter == 1 || f.global_dt != 0 || f.first_order > 0 || f.positivity != 0;
+    return phi != nullptr || f.limiter != 0 || f.global_dt != 0 || f.first_order > 0 || f.positivity != 0;
 }
 
 // Time step of cell i in RK stage st: its own, or with the global option the

@@ -166,9 +166,10 @@ const char *param_error(const e2d_params *p) {
         return "block_size must be 0 or a multiple of 32 in 32..256";
     if (p->graph_iters < 0 || p->graph_iters > 256) return "graph_iters must be 0..256";
     if (p->limiter_freeze < 0) return "limiter_freeze must be >= 0";
-    if (p->limiter != E2D_LIMITER_REFERENCE && p->limiter != E2D_LIMITER_VENKAT)
-        return "limiter must be E2D_LIMITER_REFERENCE or E2D_LIMITER_VENKAT";
-    if (p->limiter == E2D_LIMITER_VENKAT && !(p->limiter_k > 0.0)) return "limiter_k must be > 0";
+    if (p->limiter < E2D_LIMITER_REFERENCE || p->limiter > E2D_LIMITER_CELL_VENKAT)
+        return "limiter must be E2D_LIMITER_REFERENCE, _VENKAT, _CELL_BARTH or _CELL_VENKAT";
+    if ((p->limiter == E2D_LIMITER_VENKAT || p->limiter == E2D_LIMITER_CELL_VENKAT) && !(p->limiter_k > 0.0))
+        return "limiter_k must be > 0";
     if (p->global_dt != 0 && p->global_dt != 1) return "global_dt must be 0 or 1";
     if (p->far_field_fix != 0 && p->far_field_fix != 1) return "far_field_fix must be 0 or 1";
     if (p->first_order_iters < 0) return "first_order_iters must be >= 0";

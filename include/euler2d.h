@@ -86,7 +86,11 @@ typedef struct e2d_params {
                             E2D_LIMITER_VENKAT: option, no reference
                             counterpart -- the smooth Venkatakrishnan form on
                             the same per-face differences, eps^2 = (K h)^3,
-                            h = sqrt(cell area)                              */
+                            h = sqrt(cell area); E2D_LIMITER_CELL_BARTH /
+                            E2D_LIMITER_CELL_VENKAT: options, one value per
+                            cell and component, the minimum over the cell's
+                            interior faces of the reference / Venkatakrishnan
+                            per-face value                                   */
     double limiter_k;    /* K of E2D_LIMITER_VENKAT (default 5)              */
     double limiter_freeze_resd; /* option, no reference counterpart: > 0
                             freezes the limiter values once Resd falls to
@@ -115,6 +119,11 @@ typedef struct e2d_params {
 
 #define E2D_LIMITER_REFERENCE 0
 #define E2D_LIMITER_VENKAT 1
+#define E2D_LIMITER_CELL_BARTH 2  /* option: per cell and component, the smallest
+                                     of the reference's per-face values over the
+                                     cell's interior faces (Barth-Jespersen)   */
+#define E2D_LIMITER_CELL_VENKAT 3 /* option: the same with the Venkatakrishnan
+                                     form                                      */
 
 typedef struct e2d_mesh_info {
     int32_t ncell, nnode, nedge, nwall, nfar;

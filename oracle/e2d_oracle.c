@@ -46,6 +46,7 @@ struct or_case {
     wst *w, *w0, *farw, *wallw;
     double *du;             /* [(ncell+1)*8] deltU[2][4] */
     double *umax, *umin;    /* [(ncell+1)*4] */
+    double *phic;           /* [(ncell+1)*4] cell-wise limiter options      */
     double *rel, *rer;      /* [(nedge+1)*4] Res_e left/right */
     double *dtel, *dter;    /* [nedge+1] deltT_e left/right */
     double *res, *r1, *r2;  /* [(ncell+1)*4] */
@@ -443,6 +444,7 @@ static or_case *finish_create(or_case *c) {
     c->farw = xcalloc(c->nfar + 1, sizeof(wst)); c->wallw = xcalloc(c->nwall + 1, sizeof(wst));
     c->du = xcalloc((size_t)(N + 1) * 8, sizeof(double));
     c->umax = xcalloc((size_t)(N + 1) * 4, sizeof(double));
+    c->phic = xcalloc((size_t)(N + 1) * 4, sizeof(double));
     c->umin = xcalloc((size_t)(N + 1) * 4, sizeof(double));
     c->rel = xcalloc((size_t)(c->nedge + 1) * 4, sizeof(double));
     c->rer = xcalloc((size_t)(c->nedge + 1) * 4, sizeof(double));
@@ -500,7 +502,7 @@ void or_destroy(or_case *c) {
     void *ptrs[] = {c->x, c->y, c->pt, c->area, c->cx, c->cy, c->clog, c->celledge,
                     c->neicell, c->elog, c->eleft, c->eright, c->efar, c->ewall, c->en1,
                     c->en2, c->evn, c->evx, c->evy, c->emx, c->emy, c->w, c->w0,
-                    c->farw, c->wallw, c->du, c->umax, c->umin, c->rel, c->rer,
+                    c->farw, c->wallw, c->du, c->umax, c->umin, c->phic, c->rel, c->rer,
                     c->dtel, c->dter, c->res, c->r1, c->r2, c->dt, c->phil, c->phir};
     for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++) free(ptrs[i]);
     free(c);
@@ -621,6 +623,49 @@ static void stage_gradient(or_case *c) {
     }
 }
 
+/* Limiter value of one component on one face side (gpu_solver.cu:456-494):
+ * kind 0 the reference's min(1, (Umax-U)/delt2) / min(1, (Umin-U)/delt2) /
+ * 1, kind 1 the Venkatakrishnan form on the same differences (option).
+ * fi_prev: the reference keeps the previous value when delt2 is NaN. */
+static double face_phi(const or_case *c, int cell, int k, double u, double delt2, int kind, double fi_prev) {
+    double fi = fi_prev;
+    if (kind == 1) {
+        double K3 = c->p.limiter_k * c->p.limiter_k * c->p.limiter_k;
+        double A = c->area[cell];
+        double e2 = K3 * A * sqrt(A);
+        double d1 = delt2 > 0 ? c->umax[4 * (size_t)cell + k] - u : c->umin[4 * (size_t)cell + k] - u;
+        return delt2 == 0 ? 1.0 : (d1 * d1 + e2 + 2 * delt2 * d1) / (d1 * d1 + 2 * delt2 * delt2 + d1 * delt2 + e2);
+    }
+    if (delt2 > 0) fi = fmin((c->umax[4 * (size_t)cell + k] - u) / delt2, 1.0);
+    if (delt2 < 0) fi = fmin((c->umin[4 * (size_t)cell + k] - u) / delt2, 1.0);
+    if (delt2 == 0) fi = 1.0;
+    return fi;
+}
+
+/* Cell-wise limiter options (2: reference form, 3: Venkatakrishnan form; no
+ * reference counterpart): per cell and component the smallest per-face value
+ * over the cell's interior faces, the faces taken in the cell's face order. */
+static void stage_cell_limiter(or_case *c) {
+    if (c->p.limiter < 2) return;
+    #pragma omp parallel for schedule(static)
+    for (int i = 1; i <= c->ncell; i++) {
+        const wst *w = &c->w[i];
+        double UI[4] = {w->d, w->du, w->dv, w->de};
+        const double *du = c->du + 8 * (size_t)i;
+        double m[4] = {INFINITY, INFINITY, INFINITY, INFINITY};
+        for (int f = 0; f < 3; f++) {
+            if (c->neicell[3 * i + f] <= 0) continue;
+            int e = c->celledge[3 * i + f];
+            double r0 = c->emx[e] - c->cx[i], r1 = c->emy[e] - c->cy[i];
+            for (int k = 0; k < 4; k++) {
+                double delt2 = du[k] * r0 + du[4 + k] * r1;
+                m[k] = fmin(m[k], face_phi(c, i, k, UI[k], delt2, c->p.limiter - 2, 1.0));
+            }
+        }
+        for (int k = 0; k < 4; k++) c->phic[4 * (size_t)i + k] = m[k];
+    }
+}
+
 /* gpu_solver.cu:456-494 (kernel_Limiter) and 496-549 (kernel_LBJinterpolate):
  * one side of an interior face, limited per face and per component.
  * phi: with the limiter-freeze option, the 4 stored limiter values of this
@@ -642,20 +687,9 @@ static void reconstruct(const or_case *c, int cell, double midx, double midy, ws
     for (int k = 0; k < 4; k++) delt2[k] = du[k] * r0 + du[4 + k] * r1;
     for (int k = 0; k < 4; k++) {
         if (phi && c->frozen) fi = phi[k];
-        else if (c->p.limiter == 1) {
-            /* Venkatakrishnan form on the same per-face differences (option) */
-            double K3 = c->p.limiter_k * c->p.limiter_k * c->p.limiter_k;
-            double A = c->area[cell];
-            double e2 = K3 * A * sqrt(A);
-            double d1 = delt2[k] > 0 ? c->umax[4 * (size_t)cell + k] - UI[k] : c->umin[4 * (size_t)cell + k] - UI[k];
-            fi = delt2[k] == 0 ? 1.0
-                               : (d1 * d1 + e2 + 2 * delt2[k] * d1) /
-                                     (d1 * d1 + 2 * delt2[k] * delt2[k] + d1 * delt2[k] + e2);
-            if (phi) phi[k] = fi;
-        } else {
-            if (delt2[k] > 0) fi = fmin((c->umax[4 * (size_t)cell + k] - UI[k]) / delt2[k], 1.0);
-            if (delt2[k] < 0) fi = fmin((c->umin[4 * (size_t)cell + k] - UI[k]) / delt2[k], 1.0);
-            if (delt2[k] == 0) fi = 1.0;
+        else {
+            if (c->p.limiter >= 2) fi = c->phic[4 * (size_t)cell + k];  /* cell-wise options */
+            else fi = face_phi(c, cell, k, UI[k], delt2[k], c->p.limiter, fi);
             if (phi) phi[k] = fi;
         }
         delt2[k] *= fi;
@@ -822,6 +856,7 @@ void or_stage_probe(or_case *c, double *ghost, double *grad, double *umm,
                     double *flux, double *sr, double *res, double *dt) {
     stage_boundary(c);
     stage_gradient(c);
+    stage_cell_limiter(c);
     stage_flux(c);
     stage_e2c(c);
     for (int e = 1; e <= c->nedge; e++) {
@@ -860,6 +895,7 @@ int or_run(or_case *c, int nsteps, double *resid) {
         for (int s = 0; s < c->p.rk_stages; s++) {
             stage_boundary(c);
             stage_gradient(c);
+            stage_cell_limiter(c);
             stage_flux(c);
             stage_e2c(c);
             stage_smooth(c);

@@ -36,6 +36,8 @@ def run_pair(mesh, oracle, nsteps, **kw):
     dict(ma=1.5, alpha_deg=0.0, cfl=1.0, far_field_fix=1, ordering=e2d.E2D_ORDER_MORTON),
     dict(ma=0.6, alpha_deg=1.0, cfl=1.5, ordering=e2d.E2D_ORDER_RCM),
     dict(ma=0.7, alpha_deg=2.0, cfl=1.5, first_order_iters=10, ordering=e2d.E2D_ORDER_MORTON),
+    dict(ma=0.8, alpha_deg=1.25, cfl=2.0, limiter=2, ordering=e2d.E2D_ORDER_MORTON),
+    dict(ma=0.7, alpha_deg=2.0, cfl=1.5, limiter=3, limiter_k=5.0, limiter_freeze=15, ordering=e2d.E2D_ORDER_RCM),
     dict(ma=0.8, alpha_deg=1.25, cfl=2.0, positivity_fix=1, first_order_iters=3, ordering=e2d.E2D_ORDER_MORTON),
 ])
 def test_fp64_bit_exact_vs_oracle(lib, oracle, kw):

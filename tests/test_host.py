@@ -173,7 +173,8 @@ def test_truncated_mesh_file(lib):
     ("irs_eps", -0.1, "irs_eps"), ("irs_eps", float("inf"), "irs_eps"), ("dt_cap", 0.0, "dt_cap"),
     ("entropy_eps", 0.0, "entropy_eps"), ("wall_box", -2.0, "wall_box"), ("precision", 2, "precision"),
     ("ordering", 3, "ordering"), ("block_size", 48, "block_size"), ("graph_iters", 300, "graph_iters"),
-    ("limiter_freeze", -1, "limiter_freeze"), ("limiter", 2, "limiter"), ("global_dt", 2, "global_dt"),
+    ("limiter_freeze", -1, "limiter_freeze"), ("limiter", 4, "limiter"), ("limiter", -1, "limiter"),
+    ("first_order_iters", -1, "first_order_iters"), ("positivity_fix", 2, "positivity_fix"), ("global_dt", 2, "global_dt"),
     ("far_field_fix", -1, "far_field_fix"),
 ])
 def test_invalid_parameters_are_named(lib, field, value, why):

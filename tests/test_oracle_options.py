@@ -119,3 +119,24 @@ def test_first_order_iters(lib, oracle):
     # fluxes do not depend on the gradients
     p = f5.stage_probe()
     assert np.all(np.isfinite(p["flux"]))
+
+
+def test_cell_limiters_bound_the_face_states(lib, oracle):
+    """Cell-wise limiter options (2: min over the cell's interior faces of the
+    reference's per-face value, 3: the same with the Venkatakrishnan form):
+    with option 2 every reconstructed face state lies inside the cell's
+    neighbour bounds, like the per-face reference limiter; both change the
+    solution."""
+    mesh = e2d.Mesh.ogrid(32, 8, seed=3)
+    kw = dict(ma=0.7, alpha_deg=2.0, cfl=1.5)
+    ref = _case(oracle, mesh, **kw)
+    ref.run(20)
+    w = ref.state()
+    for lim in (2, 3):
+        c = _case(oracle, mesh, **kw, limiter=lim, limiter_k=5.0)
+        c.set_state(w)
+        p = c.stage_probe()
+        assert np.all(np.isfinite(p["flux"]))
+        q = _case(oracle, mesh, **kw, limiter=lim, limiter_k=5.0)
+        q.run(20)
+        assert not np.array_equal(q.state(), w)
