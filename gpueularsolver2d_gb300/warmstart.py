@@ -79,7 +79,11 @@ class SolverSettings:
     ``refreeze_resd`` > 0 stops at that level and continues from the state
     reached in a new solver whose limiter values are frozen after its first
     iteration, i.e. recomputed from a nearly converged state: a run then
-    depends less on the state it froze its limiter values on first."""
+    depends less on the state it froze its limiter values on first; that
+    second solver runs in ``tail_precision`` (None: ``precision``), which is
+    how a run goes below the FP32 floor with frozen limiter values.
+    ``irs_eps``, ``positivity_fix`` and ``first_order_iters`` are the solver
+    options of the same names."""
     cfl: float = 3.0
     freeze: int = 0
     freeze_resd: float = 1e-3
@@ -88,12 +92,18 @@ class SolverSettings:
     limiter_k: float = 10.0
     switch_resd: float = 0.0
     refreeze_resd: float = 0.0
+    tail_precision: int | None = None
+    irs_eps: float = 0.8
+    positivity_fix: int = 0
+    first_order_iters: int = 0
 
-    def params(self, mach, alpha, maxstep=100000):
-        return e2d.default_params(ma=mach, alpha_deg=alpha, cfl=self.cfl, precision=self.precision,
+    def params(self, mach, alpha, maxstep=100000, precision=None):
+        return e2d.default_params(ma=mach, alpha_deg=alpha, cfl=self.cfl,
+                                  precision=self.precision if precision is None else precision,
                                   ordering=e2d.E2D_ORDER_MORTON, limiter_freeze=self.freeze, maxstep=maxstep,
                                   limiter=self.limiter, limiter_k=self.limiter_k,
-                                  limiter_freeze_resd=self.freeze_resd)
+                                  limiter_freeze_resd=self.freeze_resd, irs_eps=self.irs_eps,
+                                  positivity_fix=self.positivity_fix, first_order_iters=self.first_order_iters)
 
 
 def generate(mesh, conds, settings: SolverSettings, iters: int, chunk: int = 128, log=print):
@@ -179,6 +189,7 @@ def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=N
     stop = max(target, settings.refreeze_resd)
     h1 = np.zeros(0)  # history of the first solver once the second one runs
     error = None
+    tail_wall = 0.0
     try:
         if settings.switch_resd > 0.0:
             h = s.solve_mixed(maxit, stop, settings.switch_resd)
@@ -191,12 +202,15 @@ def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=N
             w, norm = s.state(), s.residual_norm()
             h1 = np.asarray(h, np.float64)
             s.close()
-            p2 = settings.params(mach, alpha, maxstep=maxit - len(h))
+            p2 = settings.params(mach, alpha, maxstep=maxit - len(h), precision=settings.tail_precision)
             p2.limiter_freeze_resd = 1.0
+            p2.first_order_iters = 0
             s = e2d.Solver(mesh, p2)
             s.set_state(w)
             s.set_residual_norm(norm)
+            t_tail = time.perf_counter()
             h2 = s.solve(maxit - len(h), target)
+            tail_wall = time.perf_counter() - t_tail
             h = np.concatenate([h1, h2])
             ok = bool(len(h2) and h2[-1] <= target)
     except E2DError as exc:
@@ -213,6 +227,8 @@ def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=N
            "first_resd": float(h[0]) if len(h) else float("nan"), "epsm": s.residual_norm(),
            "start_cl": cl0, "start_cd": cd0,
            "iterations_to": {f"{lv:.0e}": first_below(lv) for lv in (1e-2, 1e-3, 1e-4, 1e-5)},
+           "tail_iterations": int(len(h) - len(h1)) if len(h1) else 0, "tail_wall_s": tail_wall,
+           "reached": float(np.min(h)) if len(h) else None,
            "history_every_1000": [float(v) for v in h[999::1000]]}
     s.close()
     return out
