@@ -10,7 +10,9 @@ every one named on the command line and in the result:
 * a cell-wise limiter (``--limiter 3``: per cell and component the smallest
   Venkatakrishnan value over the cell's interior faces; ``2`` is the
   Barth-Jespersen form of the reference's values);
-* the limiter values frozen once Resd falls to ``--freeze``;
+* the limiter values frozen once Resd falls to ``--freeze`` (or at iteration
+  ``--freeze-after``, whichever comes first: on finer meshes the residual
+  can level off just above the freeze level);
 * the FP32 stencil down to ``--switch``, then a new FP64 solver from the state
   reached, its limiter values frozen after its first iteration, to
   ``--target`` (FP32 states stall near 1e-5).
@@ -30,7 +32,8 @@ from .warmstart import SolverSettings, run_to_drop
 
 
 def settings_from(args) -> SolverSettings:
-    return SolverSettings(cfl=args.cfl, freeze_resd=args.freeze, precision=e2d.E2D_FP32, limiter=args.limiter,
+    return SolverSettings(cfl=args.cfl, freeze=args.freeze_after, freeze_resd=args.freeze, precision=e2d.E2D_FP32,
+                          limiter=args.limiter,
                           limiter_k=args.limiter_k, refreeze_resd=args.switch, tail_precision=e2d.E2D_FP64,
                           irs_eps=args.irs_eps, positivity_fix=args.positivity_fix,
                           first_order_iters=args.first_order_iters)
@@ -48,6 +51,8 @@ def main(argv=None):
     ap.add_argument("--limiter", type=int, default=3)
     ap.add_argument("--limiter-k", type=float, default=5.0)
     ap.add_argument("--freeze", type=float, default=3e-3, help="freeze the limiter values at this Resd")
+    ap.add_argument("--freeze-after", type=int, default=0,
+                    help="freeze the limiter values at this iteration if Resd has not reached --freeze (0: never)")
     ap.add_argument("--switch", type=float, default=2e-5, help="FP32 down to this Resd, then FP64")
     ap.add_argument("--target", type=float, default=1e-6)
     ap.add_argument("--maxit", type=int, default=400000)
