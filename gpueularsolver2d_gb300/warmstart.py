@@ -234,6 +234,40 @@ def run_to_drop(mesh, mach, alpha, settings: SolverSettings, target, maxit, w0=N
     return out
 
 
+def run_budget(mesh, mach, alpha, settings: SolverSettings, budget: int, w0=None, epsm=None, every: int = 5000):
+    """A fixed number of iterations (in ``settings.precision``) from the free
+    stream or from w0, for cases whose drop is out of reach of the budget:
+    the residual history, the iterations at which it first reaches each level,
+    and CL / CD every ``every`` iterations."""
+    s = e2d.Solver(mesh, settings.params(mach, alpha, maxstep=budget + 10))
+    if w0 is not None:
+        s.set_state(w0)
+    if epsm is not None:
+        s.set_residual_norm(epsm)
+    forces, error = [], None
+    t0 = time.perf_counter()
+    try:
+        for k0 in range(0, budget, every):
+            s.step(min(every, budget - k0))
+            cl, cd = s.forces()
+            forces.append((k0 + min(every, budget - k0), cl, cd))
+    except E2DError as exc:
+        error = str(exc)
+    wall = time.perf_counter() - t0
+    h = s.history()
+
+    def first_below(level):
+        k = np.flatnonzero(h <= level)
+        return int(k[0]) + 1 if len(k) else None
+
+    out = {"iterations": int(len(h)), "wall_s": wall, "error": error, "epsm": s.residual_norm(),
+           "first_resd": float(h[0]) if len(h) else None, "final_resd": float(h[-1]) if len(h) else None,
+           "iterations_to": {f"{lv:.0e}": first_below(lv) for lv in (1e-1, 1e-2, 1e-3, 1e-4, 1e-5)},
+           "forces": forces, "history_every_1000": [float(v) for v in h[999::1000]]}
+    s.close()
+    return out
+
+
 def physical(w, gamma: float = GAMMA) -> bool:
     """Every cell finite with positive density and pressure."""
     w = np.asarray(w, np.float64)
@@ -311,45 +345,103 @@ def main(argv=None):
     ap.add_argument("--maxit", type=int, default=120000)
     ap.add_argument("--mach", type=float, nargs=2, default=(0.575, 0.70))
     ap.add_argument("--alpha", type=float, nargs=2, default=(-1.0, 3.0))
-    ap.add_argument("--eval", choices=["fp64", "switch"], default="fp64",
-                    help="timed runs in FP64, or FP32 down to 2e-3 and FP64 below")
+    ap.add_argument("--eval", choices=["fp64", "switch", "tail"], default="fp64",
+                    help="timed runs in FP64; FP32 down to 2e-3 and FP64 below; or FP32 down to the "
+                         "--refreeze level and a new FP64 solver (limiter values frozen again) below")
+    ap.add_argument("--limiter", type=int, default=1, help="limiter option of every solve (1: per-face "
+                    "Venkatakrishnan, 3: cell-wise Venkatakrishnan)")
+    ap.add_argument("--limiter-k", type=float, default=10.0)
+    ap.add_argument("--cfl", type=float, default=3.0)
+    ap.add_argument("--irs-eps", type=float, default=0.8)
+    ap.add_argument("--freeze", type=float, default=1e-3, help="limiter values frozen at this Resd")
+    ap.add_argument("--freeze-after", type=int, default=0,
+                    help="... or at this iteration, whichever comes first (0: level only)")
     ap.add_argument("--refreeze", type=float, default=1e-5,
                     help="freeze the limiter values again, from the state at this level (0: off)")
+    ap.add_argument("--eval-mesh", type=int, nargs=2, default=None, metavar=("NI", "NJ"),
+                    help="also predict on this finer O-grid and compare free and warm runs there")
+    ap.add_argument("--eval-cond", type=float, nargs=2, default=(0.78, 2.0), metavar=("MACH", "ALPHA"))
+    ap.add_argument("--budget", type=int, default=100000, help="FP32 iterations of each run on --eval-mesh")
+    ap.add_argument("--cache", default=None,
+                    help="npz file of the generated training / held-out states: loaded when it exists and "
+                         "matches the mesh and conditions, else written after generation")
     ap.add_argument("--json", default=None)
     args = ap.parse_args(argv)
     log = lambda s: print(s, file=sys.stderr, flush=True)  # noqa: E731
     mesh = e2d.Mesh.ogrid(args.ni, args.nj, seed=1)
     train_c = conditions(args.ntrain, 3, tuple(args.mach), tuple(args.alpha))
     held_c = conditions(args.nheld, 4, tuple(args.mach), tuple(args.alpha))
-    gen = SolverSettings(precision=e2d.E2D_FP32)
-    states, info = generate(mesh, train_c, gen, args.gen_iters, log=log)
+    scheme = dict(cfl=args.cfl, limiter=args.limiter, limiter_k=args.limiter_k, irs_eps=args.irs_eps,
+                  freeze_resd=args.freeze, freeze=args.freeze_after)
+    gen = SolverSettings(precision=e2d.E2D_FP32, **scheme)
+    key = np.array([args.ni, args.nj, args.gen_iters] + [v for c in train_c + held_c for v in c], np.float64)
+    cached = None
+    if args.cache:
+        try:
+            z = np.load(args.cache)
+            if z["key"].shape == key.shape and np.array_equal(z["key"], key):
+                cached = z
+        except (OSError, KeyError, ValueError):
+            cached = None
+    if cached is not None:
+        states = list(cached["train"])
+        info = []
+        log(f"generate: {len(states)} training states from {args.cache}")
+    else:
+        states, info = generate(mesh, train_c, gen, args.gen_iters, log=log)
     ds = Dataset(mesh, train_c, states)
     net, loss, t_train = train(ds, args.steps, args.batch, nhidden=args.nhidden, lr=args.lr,
                                lr_final=args.lr_final if args.lr_final > 0 else None, log=log)
     # prediction error on the held-out conditions against their FP32 solutions
-    held_states, _ = generate(mesh, held_c, gen, args.gen_iters, log=log)
+    if cached is not None:
+        held_states = list(cached["held"])
+    else:
+        held_states, _ = generate(mesh, held_c, gen, args.gen_iters, log=log)
+        if args.cache:
+            np.savez(args.cache, key=key, train=np.array(states), held=np.array(held_states))
     errs = []
     for (m, a), w in zip(held_c, held_states):
         p = predict(net, ds, mesh, m, a)
         errs.append(float(np.sqrt(np.mean((p - w) ** 2, axis=0)).max() / np.abs(w).max()))
     log(f"held-out prediction RMS error (max over components, rel. to max |W|): median {np.median(errs):.2e}")
-    ev = SolverSettings(precision=e2d.E2D_FP64, switch_resd=2e-3 if args.eval == "switch" else 0.0,
-                        refreeze_resd=args.refreeze)
-    rows = evaluate(net, ds, mesh, held_c[:args.neval], ev, args.target, args.maxit, log=log)
+    if args.eval == "tail":
+        ev = SolverSettings(precision=e2d.E2D_FP32, tail_precision=e2d.E2D_FP64, refreeze_resd=args.refreeze,
+                            **scheme)
+    else:
+        ev = SolverSettings(precision=e2d.E2D_FP64, switch_resd=2e-3 if args.eval == "switch" else 0.0,
+                            refreeze_resd=args.refreeze, **scheme)
+    rows = evaluate(net, ds, mesh, held_c[:args.neval], ev, args.target, args.maxit, log=log) if args.neval else []
     conv = [r for r in rows if r["warm"]["converged"] and r["free"]["converged"]]
+    large = None
+    if args.eval_mesh:
+        # the network trained on the coarse mesh evaluated at the centroids of
+        # a finer one; both runs take the same FP32 budget there
+        big = e2d.Mesh.ogrid(args.eval_mesh[0], args.eval_mesh[1], seed=1)
+        m, a = args.eval_cond
+        t0 = time.perf_counter()
+        w_pred = predict(net, ds, big, m, a)
+        t_pred = time.perf_counter() - t0
+        fine = SolverSettings(precision=e2d.E2D_FP32, **scheme)
+        free = run_budget(big, m, a, fine, args.budget)
+        warm = run_budget(big, m, a, fine, args.budget, w0=w_pred if physical(w_pred) else None, epsm=free["epsm"])
+        large = {"mesh": f"{args.eval_mesh[0]}x{args.eval_mesh[1]}", "mach": m, "alpha": a, "budget": args.budget,
+                 "predict_seconds": t_pred, "prediction_physical": physical(w_pred), "free": free, "warm": warm}
+        log(f"large mesh {large['mesh']} M{m} a{a}: free {free['iterations_to']} final {free['final_resd']:.2e} | "
+            f"warm {warm['iterations_to']} final {warm['final_resd']:.2e} (first {warm['first_resd']:.2e})")
     summary = {
         "mesh": f"{args.ni}x{args.nj}", "ntrain": args.ntrain, "nheld": args.nheld, "mach": list(args.mach),
         "alpha": list(args.alpha), "gen_iters": args.gen_iters, "train_steps": args.steps, "batch": args.batch, "nhidden": args.nhidden,
         "lr": args.lr, "lr_final": args.lr_final,
         "train_seconds": t_train, "final_loss": float(loss[-100:].mean()),
         "heldout_pred_err_median": float(np.median(errs)), "target_drop": args.target,
-        "eval_precision": args.eval, "refreeze": args.refreeze, "evaluated": len(rows), "both_converged": len(conv),
+        "eval_precision": args.eval, "refreeze": args.refreeze, "scheme": scheme,
+        "evaluated": len(rows), "both_converged": len(conv),
         "fallbacks": sum(1 for r in rows if r["warm"]["fallback"]),
         "speedup_wall_median": float(np.median([r["speedup_wall"] for r in conv])) if conv else None,
         "speedup_iter_median": float(np.median([r["speedup_iter"] for r in conv])) if conv else None,
         "max_dcl": float(max(r["dcl"] for r in conv)) if conv else None,
         "max_dcd": float(max(r["dcd"] for r in conv)) if conv else None,
-        "rows": rows,
+        "rows": rows, "large_mesh": large,
     }
     text = json.dumps(summary)
     print(text, flush=True)
