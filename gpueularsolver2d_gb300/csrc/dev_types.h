@@ -26,6 +26,7 @@ struct Ctl {
     // bits of a non-negative double (whose order is that of the integers), so
     // that blocks fold into it with atomicMin.  kDtNone between iterations.
     unsigned long long dtmin[8];
+    unsigned int fold_count;  // blocks of the residual fold done this iteration (0 between iterations)
 };
 
 constexpr unsigned long long kDtNone = 0x7FF0000000000000ULL;  // +inf
@@ -120,8 +121,9 @@ template <typename T> int launches_per_iteration(const BPlan<T> &p) {
 
 template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream_t s);
 
-void enqueue_batch_resid(const double *part, const int2 *case_tiles, int ncase, Ctl *ctl, double *hist,
-                         int hist_cap, cudaStream_t s);
+// pairs: the partials are float2 pairs (FP32 stencil) rather than doubles.
+void enqueue_batch_resid(double *part, const int2 *case_tiles, int ncase, Ctl *ctl, double *hist,
+                         int hist_cap, bool pairs, cudaStream_t s);
 
 // Enqueue one iteration (all RK stages + the residual) on a stream.
 // Instantiated for double in kernels_f64.cu and for float in kernels_f32.cu.
@@ -137,7 +139,7 @@ template <typename T>
 void enqueue_export(int n, const int *perm, const V4<T> *W, double *wfile, cudaStream_t s);
 
 // Residual kernel launcher (resid.cu).
-void enqueue_resid(const double *part, int nparts, Ctl *ctl, double *hist, int hist_cap,
+void enqueue_resid(double *part, int nparts, Ctl *ctl, double *hist, int hist_cap, bool pairs,
                    cudaStream_t s);
 
 }  // namespace e2d

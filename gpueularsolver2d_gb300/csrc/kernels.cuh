@@ -300,80 +300,6 @@ __device__ __forceinline__ V4<float> roe<float>(const V4<float> &LW, const V4<fl
 }
 
 // ---------------------------------------------------------------------------
-// Packed FP32 arithmetic: two independent lanes per instruction (the f32x2
-// add / multiply / fused multiply-add of sm_100 and later), each lane
-// rounding exactly like the scalar operation it replaces.  The reciprocals and
-// square roots stay scalar per lane.
-__device__ __forceinline__ float2 p2(float v) { return make_float2(v, v); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(1.0f / a.x, 1.0f / a.y); }
-__device__ __forceinline__ float2 sqrt2(float2 a) { return make_float2(sqrtf(a.x), sqrtf(a.y)); }
-
-// Harten's fix of one eigenvalue pair: (l^2 + eps^2) / (2 eps) inside the
-// band, |l| outside (as roe<float>).
-__device__ __forceinline__ float2 harten2(float2 l, float eps, float e2, float ie) {
-    const float2 q = mul2(fma2(l, l, p2(e2)), p2(ie));
-    return make_float2(fabsf(l.x) < eps ? q.x : fabsf(l.x), fabsf(l.y) < eps ? q.y : fabsf(l.y));
-}
-
-// Two Roe fluxes at once, lane j of every pair belonging to face j: the same
-// operations as roe<float> in the same order, packed, so each lane's result
-// has the bits the scalar form gives.  Lx..Lw / Rx..Rw are the components of
-// the left / right states of the two faces.
-struct Roe2In {
-    float2 Lx, Ly, Lz, Lw, Rx, Ry, Rz, Rw, nx, ny;
-};
-
-__device__ __forceinline__ void roe_pair(const Roe2In &q, float g, float epsilon, float2 F[4]) {
-    const float gm1 = g - 1.0f;
-    const float2 il = rcp2(q.Lx), ir = rcp2(q.Rx);
-    const float2 U0 = mul2(q.Ly, il), V0 = mul2(q.Lz, il), U1 = mul2(q.Ry, ir), V1 = mul2(q.Rz, ir);
-    const float2 P0 = mul2(p2(gm1), fma2(mul2(p2(-0.5f), q.Lx), fma2(U0, U0, mul2(V0, V0)), q.Lw));
-    const float2 P1 = mul2(p2(gm1), fma2(mul2(p2(-0.5f), q.Rx), fma2(U1, U1, mul2(V1, V1)), q.Rw));
-    const float2 H0 = mul2(add2(q.Lw, P0), il), H1 = mul2(add2(q.Rw, P1), ir);
-    const float2 M0 = fma2(U0, q.nx, mul2(V0, q.ny)), M1 = fma2(U1, q.nx, mul2(V1, q.ny));
-    const float2 DVC = sub2(M1, M0);
-    const float2 sl = sqrt2(q.Lx), sr = sqrt2(q.Rx);
-    const float2 ROUB = mul2(sl, sr), is = rcp2(add2(sl, sr));
-    const float2 UB = mul2(fma2(U0, sl, mul2(U1, sr)), is);
-    const float2 VB = mul2(fma2(V0, sl, mul2(V1, sr)), is);
-    const float2 HB = mul2(fma2(H0, sl, mul2(H1, sr)), is);
-    const float2 QB = fma2(UB, UB, mul2(VB, VB));
-    const float2 AB = sqrt2(mul2(p2(gm1), fma2(p2(-0.5f), QB, HB)));
-    const float2 VC = fma2(UB, q.nx, mul2(VB, q.ny));
-    const float e2 = epsilon * epsilon, ie = 0.5f / epsilon;
-    const float2 l0 = sub2(VC, AB), l2 = add2(VC, AB);
-    const float2 AD0 = harten2(l0, epsilon, e2, ie);
-    const float2 AD1 = harten2(VC, epsilon, e2, ie);
-    const float2 AD2 = harten2(l2, epsilon, e2, ie);
-    const float2 dP = sub2(P1, P0), ia2 = rcp2(mul2(AB, AB)), rad = mul2(mul2(ROUB, AB), DVC),
-                 h2 = mul2(p2(0.5f), ia2);
-    const float2 F00 = mul2(mul2(AD0, sub2(dP, rad)), h2);
-    const float2 F20 = mul2(mul2(AD2, add2(dP, rad)), h2);
-    const float2 F10 = mul2(AD1, fma2(neg2(dP), ia2, sub2(q.Rx, q.Lx)));
-    const float2 du = sub2(U1, U0), dv = sub2(V1, V0), aR = mul2(AD1, ROUB);
-    const float2 nAB = neg2(AB), nDVC = neg2(DVC);
-    const float2 F01 = mul2(F00, fma2(nAB, q.nx, UB)), F21 = mul2(F20, fma2(AB, q.nx, UB));
-    const float2 F02 = mul2(F00, fma2(nAB, q.ny, VB)), F22 = mul2(F20, fma2(AB, q.ny, VB));
-    const float2 F03 = mul2(F00, fma2(nAB, VC, HB)), F23 = mul2(F20, fma2(AB, VC, HB));
-    const float2 F11 = fma2(F10, UB, mul2(aR, fma2(nDVC, q.nx, du)));
-    const float2 F12 = fma2(F10, VB, mul2(aR, fma2(nDVC, q.ny, dv)));
-    const float2 F13 = fma2(mul2(F10, p2(0.5f)), QB, mul2(aR, fma2(UB, du, fma2(VB, dv, mul2(nDVC, VC)))));
-    const float2 WL0 = mul2(q.Lx, M0), WR0 = mul2(q.Rx, M1);
-    const float2 WL1 = fma2(U0, WL0, mul2(q.nx, P0)), WR1 = fma2(U1, WR0, mul2(q.nx, P1));
-    const float2 WL2 = fma2(V0, WL0, mul2(q.ny, P0)), WR2 = fma2(V1, WR0, mul2(q.ny, P1));
-    const float2 WL3 = mul2(WL0, H0), WR3 = mul2(WR0, H1);
-    F[0] = mul2(p2(0.5f), sub2(add2(WL0, WR0), add2(add2(F00, F10), F20)));
-    F[1] = mul2(p2(0.5f), sub2(add2(WL1, WR1), add2(add2(F01, F11), F21)));
-    F[2] = mul2(p2(0.5f), sub2(add2(WL2, WR2), add2(add2(F02, F12), F22)));
-    F[3] = mul2(p2(0.5f), sub2(add2(WL3, WR3), add2(add2(F03, F13), F23)));
-}
-
-// ---------------------------------------------------------------------------
 // Pass A: gpu_solver.cu:137-223 (kernel_Boundary), 225-383 (kernel_Gradient),
 // 385-454 (kernel_deltT), 456-549 (kernel_Limiter / kernel_LBJinterpolate),
 // and the dt part of 768-878 (kernel_Flux_e2c).
@@ -667,67 +593,6 @@ __device__ __forceinline__ V4<T> face_flux_of(const Flow<T> &f, const int code, 
     return F;
 }
 
-// FP32: faces 0 and 1 as one packed pair, face 2 in the first lane of a
-// second pair (its second lane repeats it); every flux has the bits of the
-// scalar form, summed in the same order.  E2D_FLUX_PACKED=0 builds the scalar
-// form (flux_cell above) instead.
-#ifndef E2D_FLUX_PACKED
-#define E2D_FLUX_PACKED 1
-#endif
-#if E2D_FLUX_PACKED
-template <>
-__device__ __forceinline__ void flux_cell<float>(const MeshDev<float> &m, const Flow<float> &f, const int i,
-                                                 const V4<float> *__restrict__ FS, V4<float> *__restrict__ res) {
-    const int n = m.n;
-    const int4 tp = m.topo[i];
-    const int code[3] = {tp.x, tp.y, tp.z};
-    V2<float> S[3];
-    V4<float> own[3], oth[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        S[k] = m.S[k * n + i];
-        own[k] = FS[k * n + i];
-        if (code[k] >= 0) oth[k] = FS[(code[k] & 3) * n + (code[k] >> 3)];
-    }
-    V4<float> r;
-    r.x = 0.0f; r.y = 0.0f; r.z = 0.0f; r.w = 0.0f;
-#pragma unroll
-    for (int pr = 0; pr < 2; pr++) {
-        const int j0 = 2 * pr, j1 = pr == 0 ? 1 : 2;
-        V4<float> a0, b0, a1, b1;
-        float nx0, ny0, vn0, nx1, ny1, vn1;
-        bool r0, r1;
-        face_inputs(f, code[j0], S[j0], own[j0], oth[j0], a0, b0, nx0, ny0, vn0, r0);
-        if (pr == 0) face_inputs(f, code[j1], S[j1], own[j1], oth[j1], a1, b1, nx1, ny1, vn1, r1);
-        else { a1 = a0; b1 = b0; nx1 = nx0; ny1 = ny0; vn1 = vn0; r1 = r0; }
-        Roe2In q;
-        q.Lx = make_float2(a0.x, a1.x); q.Ly = make_float2(a0.y, a1.y);
-        q.Lz = make_float2(a0.z, a1.z); q.Lw = make_float2(a0.w, a1.w);
-        q.Rx = make_float2(b0.x, b1.x); q.Ry = make_float2(b0.y, b1.y);
-        q.Rz = make_float2(b0.z, b1.z); q.Rw = make_float2(b0.w, b1.w);
-        q.nx = make_float2(nx0, nx1); q.ny = make_float2(ny0, ny1);
-        float2 G[4];
-        roe_pair(q, f.gamma, f.eps_entropy, G);
-        const float2 v2 = make_float2(vn0, vn1);
-        float F0[4], F1[4];
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-            const float2 h = mul2(G[c], v2);
-            F0[c] = h.x;
-            F1[c] = h.y;
-        }
-        // faces in order 0, 1, 2 with the reference's signs
-        if (r0) { r.x -= F0[0]; r.y -= F0[1]; r.z -= F0[2]; r.w -= F0[3]; }
-        else { r.x += F0[0]; r.y += F0[1]; r.z += F0[2]; r.w += F0[3]; }
-        if (pr == 0) {
-            if (r1) { r.x -= F1[0]; r.y -= F1[1]; r.z -= F1[2]; r.w -= F1[3]; }
-            else { r.x += F1[0]; r.y += F1[1]; r.z += F1[2]; r.w += F1[3]; }
-        }
-    }
-    res[i] = r;
-}
-#endif
-
 template <typename T>
 __device__ __forceinline__ V4<T> face_flux(const MeshDev<T> &m, const Flow<T> &f, const int i, const int k,
                                            const int code, const V4<T> *__restrict__ FS, bool &right) {
@@ -887,7 +752,7 @@ template <typename T>
 __device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &f, const T rk,
                                             const int smooth, const int i, const V4<T> *__restrict__ src,
                                             const V4<T> *__restrict__ res, const T dti,
-                                            const V4<T> *W0, V4<T> *Wout, const bool want, double &d2,
+                                            const V4<T> *W0, V4<T> *Wout, const bool want, T &drho,
                                             int &bad) {
     {
         const int4 tp = m.topo[i];
@@ -914,23 +779,26 @@ __device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &
         w.w = w0.w - RK * r.w / A;
         Wout[i] = w;
         if (want) {
-            // (rho - rho0)^2 in FP64: the difference of two T values is exact there
-            double dd = (double)w.x - (double)w0.x;
-            d2 = dd * dd;
-            // physical state (rho > 0, internal energy > 0) in the stencil's
-            // precision: with an FP64 division per cell the last stage's pass
-            // D took 225 us against 61 us for the others at 4.2M cells (FP64
-            // throughput is a small fraction of FP32 on this GPU)
+            // rho - rho0 in the stencil's precision: exact in FP32 as long as the
+            // two densities are within a factor of two (Sterbenz)
+            drho = w.x - w0.x;
             const T q = T(0.5) * (w.y * w.y + w.z * w.z) / w.x;
             bad = !(w.x > T(0)) || !(w.w - q > T(0));
         }
     }
 }
 
-// Deterministic block sum of d2 (fixed shuffle tree, then the warps in order)
-// into *slot, and the count of unphysical cells added to *nbad.  Every thread
-// of the block must call it.
-__device__ __forceinline__ void block_partial(double d2, int bad, double *slot, int *nbad) {
+// Deterministic block sum of (rho - rho0)^2 (fixed shuffle tree, then the
+// warps in order) into *slot, and the count of unphysical cells added to
+// *nbad.  Every thread of the block must call it.  FP64 stencil: an FP64 sum.
+// FP32 stencil: the squares and sums as unevaluated pairs of floats (exact
+// square by a fused multiply-add, two-sum additions), about 48 bits, so that
+// pass D issues no FP64 instruction (FP64 throughput is a small fraction of
+// FP32 on this GPU and the FP64 tree took ~25 us per iteration at 4.2M
+// cells); *slot then holds the pair as a float2 that the residual kernel
+// widens to FP64.
+__device__ __forceinline__ void block_partial(double drho, int bad, double *slot, int *nbad) {
+    double d2 = drho * drho;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) d2 += __shfl_down_sync(0xffffffffu, d2, o);
     unsigned badmask = __ballot_sync(0xffffffffu, bad);
@@ -949,6 +817,42 @@ __device__ __forceinline__ void block_partial(double d2, int bad, double *slot, 
     }
 }
 
+// a + b for unevaluated float pairs (a.x + a.y): two-sum of the leading
+// parts, the trailing parts and its error added, renormalised.  The terms
+// summed here are non-negative, so there is no cancellation.
+__device__ __forceinline__ void pair_add(float &ah, float &al, const float bh, const float bl) {
+    const float s = ah + bh;
+    const float bb = s - ah;
+    const float e = (ah - (s - bb)) + (bh - bb);
+    const float t = e + (al + bl);
+    ah = s + t;
+    al = t - (ah - s);
+}
+
+__device__ __forceinline__ void block_partial(float drho, int bad, double *slot, int *nbad) {
+    float hi = drho * drho;
+    float lo = fmaf(drho, drho, -hi);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float bh = __shfl_down_sync(0xffffffffu, hi, o), bl = __shfl_down_sync(0xffffffffu, lo, o);
+        pair_add(hi, lo, bh, bl);
+    }
+    unsigned badmask = __ballot_sync(0xffffffffu, bad);
+    __shared__ float2 wsf[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();  // wsf may still be read by the previous use in this block
+    if (lane == 0) {
+        wsf[wid] = make_float2(hi, lo);
+        if (badmask) atomicAdd(nbad, __popc(badmask));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float sh = 0.0f, sl = 0.0f;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) pair_add(sh, sl, wsf[k].x, wsf[k].y);
+        *reinterpret_cast<float2 *>(slot) = make_float2(sh, sl);
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, int smooth,
                                                 const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
@@ -957,12 +861,12 @@ __global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, i
     wait_prior_grid();
     if (ctl->halt) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double d2 = 0.0;
+    T drho = T(0.0);
     int bad = 0;
     if (i < m.n)
-        update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, ctl, st, dt, i), W0, Wout, part != nullptr, d2, bad);
+        update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, ctl, st, dt, i), W0, Wout, part != nullptr, drho, bad);
     if (!part) return;
-    block_partial(d2, bad, part + blockIdx.x, &ctl->nbad);
+    block_partial(drho, bad, part + blockIdx.x, &ctl->nbad);
 }
 
 // ---------------------------------------------------------------------------
@@ -1036,14 +940,14 @@ __global__ void __launch_bounds__(256) kb_update(MeshDev<T> m, BatchDev<T> b, in
         const int tc = b.chunk_case[(t * blockDim.x) / kChunk];  // the tile's case
         if (b.ctl[tc].halt) continue;                             // uniform over the block
         const int i = t * blockDim.x + threadIdx.x;
-        double d2 = 0.0;
+        T drho = T(0.0);
         int bad = 0, c;
         if (batch_cell(b, m.n, i, c)) {
             const Flow<T> f = b.flows[c];
             update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, &b.ctl[c], st, dt, i), W0, Wout,
-                        part != nullptr, d2, bad);
+                        part != nullptr, drho, bad);
         }
-        if (part) block_partial(d2, bad, part + t, &b.ctl[tc].nbad);
+        if (part) block_partial(drho, bad, part + t, &b.ctl[tc].nbad);
     }
 }
 
@@ -1067,7 +971,7 @@ template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream
         launch_chained(kb_update<T>, G, B, s, p.m, p.b, NT, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
                        p.W[0], Wout, last ? p.part : nullptr, st);
     }
-    enqueue_batch_resid(p.part, p.case_tiles, p.ncase, p.b.ctl, p.hist, p.hist_cap, s);
+    enqueue_batch_resid(p.part, p.case_tiles, p.ncase, p.b.ctl, p.hist, p.hist_cap, sizeof(T) == 4, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -1129,7 +1033,7 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
         launch_chained(k_update<T>, G, B, s, p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
                        p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
     }
-    enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, s);
+    enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, sizeof(T) == 4, s);
 }
 
 // Same launches as enqueue_iteration, with events recorded around each one.
@@ -1165,7 +1069,7 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
                                     p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
         done();
     }
-    mark(4); enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, s); done();
+    mark(4); enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, sizeof(T) == 4, s); done();
     return j;
 }
 

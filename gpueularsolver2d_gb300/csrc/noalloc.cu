@@ -54,6 +54,7 @@ __global__ void k_noalloc_ctl(Ctl *ctl, int target, double epsm) {
     ctl->frozen = 0;
     ctl->freeze_resd = 0.0;
     for (int k = 0; k < 8; k++) ctl->dtmin[k] = kDtNone;
+    ctl->fold_count = 0;
 }
 
 // Every face code of the caller's topology must name a cell of this mesh (or

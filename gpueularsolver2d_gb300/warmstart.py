@@ -362,6 +362,8 @@ def main(argv=None):
                     help="also predict on this finer O-grid and compare free and warm runs there")
     ap.add_argument("--eval-cond", type=float, nargs=2, default=(0.78, 2.0), metavar=("MACH", "ALPHA"))
     ap.add_argument("--budget", type=int, default=100000, help="FP32 iterations of each run on --eval-mesh")
+    ap.add_argument("--eval-freeze", type=float, default=None,
+                    help="limiter freeze level of the --eval-mesh runs (default --freeze; 0: never)")
     ap.add_argument("--cache", default=None,
                     help="npz file of the generated training / held-out states: loaded when it exists and "
                          "matches the mesh and conditions, else written after generation")
@@ -389,6 +391,13 @@ def main(argv=None):
         log(f"generate: {len(states)} training states from {args.cache}")
     else:
         states, info = generate(mesh, train_c, gen, args.gen_iters, log=log)
+    # a generated state that is not physical (a case that diverged) is not
+    # a training target
+    all_states = states
+    keep = [k for k, w in enumerate(states) if physical(w)]
+    if len(keep) < len(states):
+        log(f"generate: {len(states) - len(keep)} of {len(states)} training cases diverged and are left out")
+    train_c, states = [train_c[k] for k in keep], [states[k] for k in keep]
     ds = Dataset(mesh, train_c, states)
     net, loss, t_train = train(ds, args.steps, args.batch, nhidden=args.nhidden, lr=args.lr,
                                lr_final=args.lr_final if args.lr_final > 0 else None, log=log)
@@ -398,9 +407,11 @@ def main(argv=None):
     else:
         held_states, _ = generate(mesh, held_c, gen, args.gen_iters, log=log)
         if args.cache:
-            np.savez(args.cache, key=key, train=np.array(states), held=np.array(held_states))
+            np.savez(args.cache, key=key, train=np.array(all_states), held=np.array(held_states))
     errs = []
     for (m, a), w in zip(held_c, held_states):
+        if not physical(w):
+            continue
         p = predict(net, ds, mesh, m, a)
         errs.append(float(np.sqrt(np.mean((p - w) ** 2, axis=0)).max() / np.abs(w).max()))
     log(f"held-out prediction RMS error (max over components, rel. to max |W|): median {np.median(errs):.2e}")
@@ -421,7 +432,10 @@ def main(argv=None):
         t0 = time.perf_counter()
         w_pred = predict(net, ds, big, m, a)
         t_pred = time.perf_counter() - t0
-        fine = SolverSettings(precision=e2d.E2D_FP32, **scheme)
+        fine_scheme = dict(scheme)
+        if args.eval_freeze is not None:
+            fine_scheme.update(freeze_resd=args.eval_freeze, freeze=0)
+        fine = SolverSettings(precision=e2d.E2D_FP32, **fine_scheme)
         free = run_budget(big, m, a, fine, args.budget)
         warm = run_budget(big, m, a, fine, args.budget, w0=w_pred if physical(w_pred) else None, epsm=free["epsm"])
         large = {"mesh": f"{args.eval_mesh[0]}x{args.eval_mesh[1]}", "mach": m, "alpha": a, "budget": args.budget,
