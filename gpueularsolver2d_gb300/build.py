@@ -49,7 +49,7 @@ UNITS = {
                                           f"--fmad={os.environ.get('E2D_FP32_FMAD', 'false')}",
                                           "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
 }
-HEADERS = ["internal.h", "dev_types.h", "kernels.cuh", "pdl.cuh", "solver_internal.h", "mlp_kernels.cuh"]
+HEADERS = ["internal.h", "dev_types.h", "kernels.cuh", "pdl.cuh", "solver_internal.h", "mlp_kernels.cuh", "mlp_tma.cuh"]
 
 
 def _stale(target: str, deps: list[str]) -> bool:

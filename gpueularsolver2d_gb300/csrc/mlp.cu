@@ -9,12 +9,16 @@
 // CUDA graph; the step counter lives in device memory so the graph is static.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "mlp_kernels.cuh"
+#include "mlp_tma.cuh"
 #include "solver_internal.h"
 
 using namespace e2d;
@@ -42,10 +46,13 @@ __global__ void k_step_update(int *step, float beta1, float beta2, float *bc) {
     bc[1] = 1.f - powf(beta2, (float)s);
 }
 
-// wbf (may be null): the bf16 copy used by the GEMMs; lr (device, read at
-// run time so that the host can schedule it) null: gradient only.
+// wbf (may be null): the bf16 copy used by the GEMMs, wbfT (may be null) its
+// transpose ([cols][rows], the data-gradient GEMM's K-major operand); lr
+// (device, read at run time so that the host can schedule it) null: gradient
+// only.
 __global__ void __launch_bounds__(256) k_adam_dev(int count, const float *__restrict__ part, int nparts,
                                                   size_t pstride, float *__restrict__ w32, bf16 *__restrict__ wbf,
+                                                  bf16 *__restrict__ wbfT, int rows, int cols,
                                                   float *__restrict__ m, float *__restrict__ v,
                                                   const float *__restrict__ lr_dev,
                                                   float beta1, float beta2, float eps, const float *__restrict__ bc,
@@ -64,11 +71,16 @@ __global__ void __launch_bounds__(256) k_adam_dev(int count, const float *__rest
     const float w = w32[i] - lr * (mi / bc[0]) / (sqrtf(vi / bc[1]) + eps);
     w32[i] = w;
     if (wbf) wbf[i] = __float2bfloat16_rn(w);
+    if (wbfT) wbfT[(size_t)(i % cols) * rows + i / cols] = __float2bfloat16_rn(w);
 }
 
-__global__ void k_to_bf16(int n, const float *__restrict__ a, bf16 *__restrict__ b) {
+// bf16 copy of a [rows][cols] matrix, and (bT non-null) of its transpose
+__global__ void k_to_bf16(int n, const float *__restrict__ a, bf16 *__restrict__ b, bf16 *__restrict__ bT, int rows,
+                          int cols) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) b[i] = __float2bfloat16_rn(a[i]);
+    if (i >= n) return;
+    b[i] = __float2bfloat16_rn(a[i]);
+    if (bT) bT[(size_t)(i % cols) * rows + i / cols] = __float2bfloat16_rn(a[i]);
 }
 
 // Minimum distance from each point to a set of segments (wall faces).
@@ -100,7 +112,8 @@ __global__ void __launch_bounds__(256) k_wall_distance(int n, const double *__re
 struct Tensor {
     int rows, cols;
     float *w32 = nullptr, *m = nullptr, *v = nullptr;
-    bf16 *wbf = nullptr;  // hidden layers: [rows][cols]
+    bf16 *wbf = nullptr;   // hidden layers: [rows][cols]
+    bf16 *wbfT = nullptr;  // hidden layers after the first: [cols][rows]
     int count() const { return rows * cols; }
 };
 
@@ -131,6 +144,12 @@ struct e2d_mlp {
     std::vector<void *> allocs;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    // TMA tensor maps of the 256 x 256 GEMMs (ws::k_gemm_ws), per hidden layer
+    // l >= 1: forward A = Hh[l-1], W_l; data gradient A = dz[0] / dz[1], W_l^T
+    bool use_ws = false;
+    int nsm = 0;
+    std::vector<CUtensorMap> mapHf, mapW, mapWT;
+    CUtensorMap mapDz[2];
     std::vector<double> loss_host;
 
     ~e2d_mlp() {
@@ -149,6 +168,72 @@ struct e2d_mlp {
 };
 
 namespace {
+
+// cuTensorMapEncodeTiled of the driver, found through the runtime (no link
+// against the driver library)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }();
+    return fn;
+}
+
+// 2D map of a row-major [rows][cols] bf16 matrix, box 64 columns x box_rows,
+// 128-byte swizzle (the layout the ws kernel's descriptors describe)
+bool map_2d(CUtensorMap *map, const bf16 *ptr, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols * sizeof(bf16)};
+    const cuuint32_t box[2] = {(cuuint32_t)ws::KC, box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)ptr, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Tensor maps of the warp-specialised GEMMs once the batch buffers exist;
+// use_ws stays false (the per-tile kernel runs every layer) when the driver
+// entry point or a map is not available, or E2D_MLP_WS=0.
+void build_ws_maps(e2d_mlp *m) {
+    m->use_ws = false;
+    const char *env = std::getenv("E2D_MLP_WS");
+    if ((env && env[0] == '0') || m->nhidden < 2) return;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&m->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    m->mapHf.assign(m->nhidden, CUtensorMap{});
+    m->mapW.assign(m->nhidden, CUtensorMap{});
+    m->mapWT.assign(m->nhidden, CUtensorMap{});
+    bool ok = true;
+    for (int l = 1; l < m->nhidden && ok; l++) {
+        ok = ok && map_2d(&m->mapHf[l], m->Hh[l - 1], m->B, H, ws::BM);
+        ok = ok && map_2d(&m->mapW[l], m->W[l].wbf, H, H, ws::ND);
+        ok = ok && map_2d(&m->mapWT[l], m->W[l].wbfT, H, H, ws::ND);
+    }
+    for (int k = 0; k < 2 && ok; k++) ok = map_2d(&m->mapDz[k], m->dz[k], m->B, H, ws::BM);
+    if (ok && cudaFuncSetAttribute(ws::k_gemm_ws<EPI_BIAS_GELU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   ws::SMEM) == cudaSuccess &&
+        cudaFuncSetAttribute(ws::k_gemm_ws<EPI_GELU_BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, ws::SMEM) ==
+            cudaSuccess)
+        m->use_ws = true;
+    cudaGetLastError();
+}
+
+template <int EPI> void gemm_ws(e2d_mlp *m, const CUtensorMap &a, const CUtensorMap &w, ws::Args g, cudaStream_t s) {
+    g.flag = m->flag_dev;
+    const int ntiles = g.M / ws::BM, grid = ntiles < m->nsm ? ntiles : m->nsm;
+    ws::k_gemm_ws<EPI><<<grid, ws::THREADS, ws::SMEM, s>>>(a, w, g);
+}
 
 size_t param_count(const e2d_mlp *m) {
     size_t c = 0;
@@ -180,15 +265,16 @@ int ensure_batch(e2d_mlp *m, int B) {
     if ((rc = m->alloc(&m->part, sizeof(float) * (size_t)kSplits * H * H))) return rc;
     if ((rc = m->alloc(&m->bpart, sizeof(float) * (size_t)kSplits * (NOUT * H + NOUT + H)))) return rc;
     if ((rc = m->alloc(&m->loss_part, sizeof(double) * (B / 256)))) return rc;
+    build_ws_maps(m);
     return E2D_OK;
 }
 
 void adam(e2d_mlp *m, cudaStream_t s, Tensor &t, const float *part, int nparts, size_t pstride, const float *lr,
           float *grad_out) {
     const auto &c = m->cfg;
-    k_adam_dev<<<(t.count() + 255) / 256, 256, 0, s>>>(t.count(), part, nparts, pstride, t.w32, t.wbf, t.m, t.v,
-                                                        lr, (float)c.beta1, (float)c.beta2, (float)c.eps, m->bc_dev,
-                                                        grad_out);
+    k_adam_dev<<<(t.count() + 255) / 256, 256, 0, s>>>(t.count(), part, nparts, pstride, t.w32, t.wbf, t.wbfT,
+                                                        t.rows, t.cols, t.m, t.v, lr, (float)c.beta1, (float)c.beta2,
+                                                        (float)c.eps, m->bc_dev, grad_out);
 }
 
 template <bool TA, bool TB, int EPI> void gemm(e2d_mlp *m, GemmArgs g, dim3 grid, cudaStream_t s) {
@@ -213,6 +299,12 @@ int check_flag(e2d_mlp *m) {
 void forward(e2d_mlp *m, cudaStream_t s, bool with_loss) {
     const int B = m->B;
     for (int l = 0; l < m->nhidden; l++) {
+        if (l > 0 && m->use_ws) {
+            ws::Args a{};
+            a.M = B; a.bias = m->b[l].w32; a.out = m->Hh[l]; a.zout = m->Z[l];
+            gemm_ws<EPI_BIAS_GELU>(m, m->mapHf[l], m->mapW[l], a, s);
+            continue;
+        }
         GemmArgs g{};
         g.M = B; g.N = H; g.K = l == 0 ? NIN : H;
         g.A = l == 0 ? m->xb : m->Hh[l - 1];
@@ -262,7 +354,11 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
         k_colsum<<<dim3(H / 32, kSplits), 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart);
         // gradient at the previous pre-activation (before this layer's weights
         // change): dz W_l, W_l read MN-major ([out][in] = [K][N])
-        if (l > 0) {
+        if (l > 0 && m->use_ws) {
+            ws::Args a{};
+            a.M = B; a.zin = m->Z[l - 1]; a.out = m->dz[cur ^ 1];
+            gemm_ws<EPI_GELU_BWD>(m, m->mapDz[cur], m->mapWT[l], a, s);
+        } else if (l > 0) {
             GemmArgs gd{};
             gd.M = B; gd.N = H; gd.K = H;
             gd.A = m->dz[cur]; gd.lda = H;
@@ -355,10 +451,13 @@ int e2d_mlp_create(const e2d_mlp_config *cfg, e2d_mlp **out) {
             if ((rc = m->alloc(&t->m, sizeof(float) * n))) return rc;
             if ((rc = m->alloc(&t->v, sizeof(float) * n))) return rc;
             if (!last && t == &W && (rc = m->alloc(&t->wbf, sizeof(bf16) * n))) return rc;
+            if (!last && l > 0 && t == &W && (rc = m->alloc(&t->wbfT, sizeof(bf16) * n))) return rc;
         }
         CK(cudaMemcpy(W.w32, hw.data(), sizeof(float) * hw.size(), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(b.w32, hb.data(), sizeof(float) * hb.size(), cudaMemcpyHostToDevice));
-        if (W.wbf) k_to_bf16<<<(W.count() + 255) / 256, 256, 0, m->stream>>>(W.count(), W.w32, W.wbf);
+        if (W.wbf)
+            k_to_bf16<<<(W.count() + 255) / 256, 256, 0, m->stream>>>(W.count(), W.w32, W.wbf, W.wbfT, W.rows,
+                                                                       W.cols);
         m->W.push_back(W);
         m->b.push_back(b);
     }
@@ -406,7 +505,9 @@ int e2d_mlp_set_params(e2d_mlp *m, const float *in) {
     for (size_t l = 0; l < m->W.size(); l++)
         for (Tensor *t : {&m->W[l], &m->b[l]}) {
             CK(cudaMemcpy(t->w32, in + off, sizeof(float) * t->count(), cudaMemcpyHostToDevice));
-            if (t->wbf) k_to_bf16<<<(t->count() + 255) / 256, 256, 0, m->stream>>>(t->count(), t->w32, t->wbf);
+            if (t->wbf)
+                k_to_bf16<<<(t->count() + 255) / 256, 256, 0, m->stream>>>(t->count(), t->w32, t->wbf, t->wbfT,
+                                                                            t->rows, t->cols);
             off += t->count();
         }
     CK(cudaStreamSynchronize(m->stream));

@@ -15,11 +15,34 @@ typedef __nv_bfloat16 bf16;
 
 constexpr int BM = 128, BN = 128;  // CTA tile of every GEMM
 
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+// Phi(x) and phi(x), the standard normal distribution and density, for GELU
+// (x Phi(x)) and its derivative (Phi(x) + x phi(x)).  Phi comes from
+// erf(|x| / sqrt 2) by Abramowitz and Stegun's rational approximation 7.1.26
+// (Handbook of Mathematical Functions, 1964: erf(u) = 1 - t (a1 + t (a2 + t (a3
+// + t (a4 + t a5)))) exp(-u^2), t = 1 / (1 + p u), absolute error <= 1.5e-7),
+// whose exp(-u^2) = exp(-x^2 / 2) is also phi's; a dozen instructions instead
+// of an erf and an exp, well below the bf16 rounding of every activation.
+__device__ __forceinline__ void normal_parts(float x, float &Phi, float &phi) {
+    const float u = fabsf(x) * 0.70710678118654752f;
+    const float t = __fdividef(1.0f, fmaf(0.3275911f, u, 1.0f));
+    const float P = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f),
+                                     -0.284496736f), 0.254829592f);
+    const float e = __expf(-0.5f * x * x);
+    const float q = 0.5f * P * e;  // 0.5 (1 - erf(|x| / sqrt 2))
+    Phi = x >= 0.0f ? 1.0f - q : q;
+    phi = e * 0.39894228040143268f;
+}
+
+__device__ __forceinline__ float gelu(float x) {
+    float Phi, phi;
+    normal_parts(x, Phi, phi);
+    return x * Phi;
+}
 
 __device__ __forceinline__ float gelu_grad(float x) {
-    // d/dx [x Phi(x)] = Phi(x) + x phi(x)
-    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+    float Phi, phi;
+    normal_parts(x, Phi, phi);
+    return fmaf(x, phi, Phi);
 }
 
 // Epilogue modes of the GEMM.

@@ -1,0 +1,258 @@
+// mlp_tma.cuh -- the 256 x 256 hidden-layer GEMMs of the warm-start MLP (the
+// forward pass with bias + GELU, and the data gradient with GELU') as one
+// persistent, warp-specialised kernel per layer.  No reference counterpart.
+//
+//   C[B x 256] = A[B x 256] . Wt^T,  A and Wt both K-major (row-major, the
+//   reduction index contiguous): Wt = W (forward) or W^T (data gradient).
+//
+// One CTA per SM walks 128-row tiles of the batch:
+//   warp 0  (one thread) loads the 256 x 256 weights once and streams each
+//           tile's A in four 128 x 64 slices by TMA (cp.async.bulk.tensor,
+//           128-byte swizzle) into a four-slot ring;
+//   warp 1  (one thread) issues tcgen05.mma (kind::f16, M = 128, N = 256,
+//           K = 16; BF16 operands from shared memory, FP32 accumulate) into
+//           one of two 256-column accumulators in tensor memory; each slice's
+//           MMAs release its slot (tcgen05.commit), a finished tile releases
+//           its accumulator to the epilogue;
+//   warps 2-17 drain the other accumulator with tcgen05.ld (each warp one
+//           32-lane quarter of the rows and a quarter of the columns), apply
+//           the epilogue and store bf16 rows, while the next tile's MMAs run.
+// Every wait is bounded: a timed-out thread sets *flag and leaves its loop;
+// the producer then waits (bounded) for the copies it issued, the MMA thread
+// for the MMAs it issued, and the tensor memory is freed on every path.
+#pragma once
+
+#include <cuda.h>
+
+#include "mlp_kernels.cuh"
+
+namespace e2d {
+namespace mlp {
+namespace ws {
+
+constexpr int KD = 256, ND = 256, BM = 128;  // reduction, output width, rows per tile
+constexpr int KC = 64;                       // K columns per A slice: one 128-byte swizzle row of bf16
+constexpr int NSLICE = KD / KC;
+constexpr int NSLOT = 4;                     // A slices in flight
+constexpr int SLICE_BYTES = BM * KC * 2;     // 16 KB
+constexpr int WSLICE_BYTES = ND * KC * 2;    // 32 KB
+constexpr int W_BYTES = ND * KD * 2;         // 128 KB
+constexpr int SMEM = W_BYTES + NSLOT * SLICE_BYTES + 1024;  // + slack to align the base to 1024 bytes
+constexpr int NEPI = 16;                     // epilogue warps: 4 per 32-lane quarter of tensor memory
+constexpr int THREADS = 32 * (2 + NEPI);
+constexpr uint32_t TMEM_COLS = 512;          // two 256-column FP32 accumulators
+constexpr int WAIT_LIMIT = 1 << 22;          // try_wait calls before giving up
+
+// instruction descriptor: FP32 D, BF16 A and B, both K-major, N = 256, M = 128
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(ND >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+// Shared-memory matrix descriptor of a K-major operand in the 128-byte swizzle
+// layout TMA writes: rows of 128 bytes (64 bf16 of K), 8-row groups 1024 bytes
+// apart (SBO), version 1, layout type 2 (128-byte swizzle).  A K = 16 step
+// inside the 64-column slice advances the start address by 32 bytes.
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool wait(uint32_t bar, uint32_t parity) {
+    for (int it = 0; it < WAIT_LIMIT; it++) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" :: "r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" :: "r"(bar) : "memory");
+}
+
+// 2D tiled TMA load of box (x, y) of the tensor map into shared memory,
+// completing on bar.  x is a multiple of 64 elements (128 bytes).
+__device__ __forceinline__ void tma_load(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n"
+                 :: "r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" :: "r"(bar)
+                 : "memory");
+}
+
+struct Args {
+    int M;                // rows (batch), a multiple of 128
+    const float *bias;    // EPI_BIAS_GELU: [256]
+    const bf16 *zin;      // EPI_GELU_BWD: [M][256]
+    bf16 *out;            // [M][256]
+    bf16 *zout;           // EPI_BIAS_GELU: [M][256] pre-activations
+    int *flag;            // set to 1 when a wait gave up
+};
+
+template <int EPI>
+__global__ void __launch_bounds__(THREADS, 1)
+    k_gemm_ws(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapW, Args g) {
+    extern __shared__ unsigned char ws_raw[];
+    __shared__ __align__(8) uint64_t full[NSLOT], empty[NSLOT], tfull[2], tempty[2], wfull, mdone;
+    __shared__ uint32_t tmem_sh;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // 1024-byte aligned base: the swizzle pattern is taken from address bits
+    const uint32_t base = (smem_u32(ws_raw) + 1023u) & ~1023u;
+    const uint32_t Wsm = base, Asm = base + W_BYTES;
+    const int ntiles = g.M / BM;
+    if (tid == 0) {
+        for (int s = 0; s < NSLOT; s++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&empty[s])));
+        }
+        for (int a = 0; a < 2; a++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&tfull[a])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" :: "r"(smem_u32(&tempty[a])), "n"(NEPI));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&wfull)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&mdone)));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n"
+                     :: "r"(smem_u32(&tmem_sh)), "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem = tmem_sh;
+
+    if (warp == 0 && lane == 0) {
+        // ---- producer ----
+        bool ok = true;
+        expect_tx(smem_u32(&wfull), W_BYTES);
+        for (int s = 0; s < NSLICE; s++) tma_load(Wsm + s * WSLICE_BYTES, &mapW, s * KC, 0, smem_u32(&wfull));
+        int q = 0;
+        for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+            for (int s = 0; s < NSLICE; s++, q++) {
+                const int slot = q % NSLOT;
+                if (!wait(smem_u32(&empty[slot]), ((q / NSLOT) & 1) ^ 1)) { ok = false; break; }
+                expect_tx(smem_u32(&full[slot]), SLICE_BYTES);
+                tma_load(Asm + slot * SLICE_BYTES, &mapA, s * KC, t * BM, smem_u32(&full[slot]));
+            }
+        }
+        if (!ok) atomicExch(g.flag, 1);
+        // every copy issued lands before the CTA can leave: the weights and the
+        // last load of each slot
+        wait(smem_u32(&wfull), 0);
+        for (int k = q - NSLOT > 0 ? q - NSLOT : 0; k < q; k++) wait(smem_u32(&full[k % NSLOT]), (k / NSLOT) & 1);
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer ----
+        bool ok = wait(smem_u32(&wfull), 0);
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+        int q = 0, li = 0;
+        for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, li++) {
+            const int acc = li & 1;
+            if (!wait(smem_u32(&tempty[acc]), ((li >> 1) & 1) ^ 1)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            const uint32_t dt = tmem + (uint32_t)(acc * ND);
+            for (int s = 0; s < NSLICE && ok; s++, q++) {
+                const int slot = q % NSLOT;
+                if (!wait(smem_u32(&full[slot]), (q / NSLOT) & 1)) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;\n");
+#pragma unroll
+                for (int kk = 0; kk < KC / 16; kk++) {
+                    const uint64_t ad = desc_sw128(Asm + slot * SLICE_BYTES + kk * 32);
+                    const uint64_t bd = desc_sw128(Wsm + s * WSLICE_BYTES + kk * 32);
+                    const uint32_t accumulate = (s > 0 || kk > 0) ? 1u : 0u;
+                    asm volatile("{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                                 :: "r"(dt), "l"(ad), "l"(bd), "r"(IDESC), "r"(accumulate));
+                }
+                commit(smem_u32(&empty[slot]));
+            }
+            if (ok) commit(smem_u32(&tfull[acc]));
+        }
+        if (!ok) atomicExch(g.flag, 1);
+        // every MMA issued completes before the tensor memory is freed
+        commit(smem_u32(&mdone));
+        wait(smem_u32(&mdone), 0);
+    } else if (warp >= 2) {
+        // ---- epilogue ----
+        const int quarter = warp & 3, group = (warp - 2) >> 2;  // rows 32 quarter.., columns 64 group..
+        int li = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, li++) {
+            const int acc = li & 1;
+            // one lane waits and the warp follows its answer, so that the warp
+            // stays converged for the collective tensor-memory loads
+            int okw = lane == 0 ? (int)wait(smem_u32(&tfull[acc]), (li >> 1) & 1) : 0;
+            okw = __shfl_sync(0xffffffffu, okw, 0);
+            if (!okw) {
+                if (lane == 0) atomicExch(g.flag, 1);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            const int m = t * BM + quarter * 32 + lane;
+#pragma unroll 1
+            for (int ch = 0; ch < 4; ch++) {
+                const int n0 = group * 64 + ch * 16;
+                uint32_t v[16];
+                const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * ND + n0);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];\n"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (m >= g.M) continue;
+                __align__(16) __nv_bfloat162 o2[8];
+                if (EPI == EPI_BIAS_GELU) {
+                    __align__(16) __nv_bfloat162 z2[8];
+                    const float4 *b4 = (const float4 *)(g.bias + n0);
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const float4 bb = b4[j];
+                        const float z0 = __uint_as_float(v[4 * j]) + bb.x, z1 = __uint_as_float(v[4 * j + 1]) + bb.y;
+                        const float z2a = __uint_as_float(v[4 * j + 2]) + bb.z, z3 = __uint_as_float(v[4 * j + 3]) + bb.w;
+                        z2[2 * j] = __floats2bfloat162_rn(z0, z1);
+                        z2[2 * j + 1] = __floats2bfloat162_rn(z2a, z3);
+                        o2[2 * j] = __floats2bfloat162_rn(gelu(z0), gelu(z1));
+                        o2[2 * j + 1] = __floats2bfloat162_rn(gelu(z2a), gelu(z3));
+                    }
+                    uint4 *zo = (uint4 *)(g.zout + (size_t)m * ND + n0);
+                    zo[0] = ((const uint4 *)z2)[0];
+                    zo[1] = ((const uint4 *)z2)[1];
+                } else {
+                    const uint4 *zi = (const uint4 *)(g.zin + (size_t)m * ND + n0);
+                    __align__(16) uint4 zz[2] = {zi[0], zi[1]};
+                    const __nv_bfloat162 *z2 = (const __nv_bfloat162 *)zz;
+#pragma unroll
+                    for (int j = 0; j < 8; j++)
+                        o2[j] = __floats2bfloat162_rn(__uint_as_float(v[2 * j]) * gelu_grad(__bfloat162float(z2[j].x)),
+                                                      __uint_as_float(v[2 * j + 1]) * gelu_grad(__bfloat162float(z2[j].y)));
+                }
+                uint4 *oo = (uint4 *)(g.out + (size_t)m * ND + n0);
+                oo[0] = ((const uint4 *)o2)[0];
+                oo[1] = ((const uint4 *)o2)[1];
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n");
+            __syncwarp();
+            if (lane == 0) arrive(smem_u32(&tempty[acc]));
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(tmem), "r"(TMEM_COLS));
+}
+
+}  // namespace ws
+}  // namespace mlp
+}  // namespace e2d

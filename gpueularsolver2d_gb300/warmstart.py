@@ -114,7 +114,10 @@ def generate(mesh, conds, settings: SolverSettings, iters: int, chunk: int = 128
         params = [settings.params(m, a, maxstep=iters) for m, a in part]
         b = e2d.Batch([mesh] * len(part), params)
         t0 = time.perf_counter()
-        b.step(iters)
+        try:
+            b.step(iters)
+        except E2DError as exc:  # the other cases ran all their iterations; the diverged ones are left out later
+            log(f"generate: {exc}")
         dt = time.perf_counter() - t0
         for c in range(len(part)):
             states.append(b.state(c))

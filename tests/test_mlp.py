@@ -91,3 +91,32 @@ def test_adam_step_size_is_scheduled_on_device(lib):
     assert np.all(d <= lr * (1 + 1e-3) + 1e-6)
     moved = d[d > 0]
     assert np.median(np.abs(moved - lr)) < 1e-6, np.median(moved)
+
+
+def test_warp_specialised_gemms_match_per_tile_gemms(lib):
+    """The hidden-layer GEMMs of the persistent TMA / tcgen05 kernel (weights
+    resident in shared memory, two accumulators in tensor memory) against the
+    per-tile kernel (E2D_MLP_WS=0) on the same network and batch: forward
+    outputs and every gradient agree to the accumulation order (bf16 storage
+    of activations and gradients)."""
+    import os
+    B, L = 4096, 4
+    rng = np.random.default_rng(9)
+    x = np.zeros((B, 32), np.float32)
+    x[:, :22] = rng.normal(size=(B, 22)).astype(np.float32)
+    t = rng.normal(size=(B, 4)).astype(np.float32) * 0.3
+    out = {}
+    for mode in ("1", "0"):
+        os.environ["E2D_MLP_WS"] = mode
+        try:
+            net = e2d.MLP(nhidden=L, batch=B, seed=4)
+            loss, g = net.gradient(x, t)
+            out[mode] = (net.forward(x), loss, g)
+            net.close()
+        finally:
+            os.environ.pop("E2D_MLP_WS", None)
+    (y1, l1, g1), (y0, l0, g0) = out["1"], out["0"]
+    assert np.max(np.abs(y1 - y0)) <= 1e-2 * np.max(np.abs(y0)) + 1e-6
+    assert abs(l1 - l0) <= 1e-3 * abs(l0)
+    cos = float(g1 @ g0 / (np.linalg.norm(g1) * np.linalg.norm(g0)))
+    assert cos > 0.9999 and np.linalg.norm(g1 - g0) < 2e-2 * np.linalg.norm(g0), cos
