@@ -7,6 +7,7 @@
 // accumulates in FP32.  The output layer (H -> 4) runs on the CUDA cores.
 // One training step (batch gather, forward, MSE loss, backward, Adam) is one
 // CUDA graph; the step counter lives in device memory so the graph is static.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -148,8 +149,8 @@ struct e2d_mlp {
     // l >= 1: forward A = Hh[l-1], W_l; data gradient A = dz[0] / dz[1], W_l^T
     bool use_ws = false;
     int nsm = 0;
-    std::vector<CUtensorMap> mapHf, mapW, mapWT;
-    CUtensorMap mapDz[2];
+    std::vector<CUtensorMap> mapHf, mapW, mapWT, mapHw;
+    CUtensorMap mapDz[2], mapDzw[2];  // dz[0] / dz[1] with 128-row boxes (data gradient), 64-row boxes (weights)
     std::vector<double> loss_host;
 
     ~e2d_mlp() {
@@ -214,17 +215,23 @@ void build_ws_maps(e2d_mlp *m) {
     m->mapHf.assign(m->nhidden, CUtensorMap{});
     m->mapW.assign(m->nhidden, CUtensorMap{});
     m->mapWT.assign(m->nhidden, CUtensorMap{});
-    bool ok = true;
+    m->mapHw.assign(m->nhidden, CUtensorMap{});
+    bool ok = m->B % ws::WROWS == 0;
     for (int l = 1; l < m->nhidden && ok; l++) {
         ok = ok && map_2d(&m->mapHf[l], m->Hh[l - 1], m->B, H, ws::BM);
         ok = ok && map_2d(&m->mapW[l], m->W[l].wbf, H, H, ws::ND);
         ok = ok && map_2d(&m->mapWT[l], m->W[l].wbfT, H, H, ws::ND);
+        ok = ok && map_2d(&m->mapHw[l], m->Hh[l - 1], m->B, H, ws::WCH);
     }
-    for (int k = 0; k < 2 && ok; k++) ok = map_2d(&m->mapDz[k], m->dz[k], m->B, H, ws::BM);
+    for (int k = 0; k < 2 && ok; k++) {
+        ok = ok && map_2d(&m->mapDz[k], m->dz[k], m->B, H, ws::BM);
+        ok = ok && map_2d(&m->mapDzw[k], m->dz[k], m->B, H, ws::WCH);
+    }
     if (ok && cudaFuncSetAttribute(ws::k_gemm_ws<EPI_BIAS_GELU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    ws::SMEM) == cudaSuccess &&
         cudaFuncSetAttribute(ws::k_gemm_ws<EPI_GELU_BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, ws::SMEM) ==
-            cudaSuccess)
+            cudaSuccess &&
+        cudaFuncSetAttribute(ws::k_wgrad_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, ws::WSMEM) == cudaSuccess)
         m->use_ws = true;
     cudaGetLastError();
 }
@@ -262,7 +269,10 @@ int ensure_batch(e2d_mlp *m, int B) {
     }
     for (int k = 0; k < 2; k++)
         if ((rc = m->alloc(&m->dz[k], sizeof(bf16) * (size_t)B * H))) return rc;
-    if ((rc = m->alloc(&m->part, sizeof(float) * (size_t)kSplits * H * H))) return rc;
+    // weight-gradient partials: kSplits of the per-tile kernel, or one per
+    // ws::WROWS rows of the batch for the warp-specialised one
+    const int nparts = std::max(kSplits, B / ws::WROWS);
+    if ((rc = m->alloc(&m->part, sizeof(float) * (size_t)nparts * H * H))) return rc;
     if ((rc = m->alloc(&m->bpart, sizeof(float) * (size_t)kSplits * (NOUT * H + NOUT + H)))) return rc;
     if ((rc = m->alloc(&m->loss_part, sizeof(double) * (B / 256)))) return rc;
     build_ws_maps(m);
@@ -345,12 +355,19 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
         // dW_l = dz^T hin (split over the batch; both operands are read
         // MN-major, the batch index being their slow one), db_l = column sums
         // of dz
-        GemmArgs gw{};
-        gw.M = H; gw.N = kin; gw.K = B;
-        gw.A = m->dz[cur]; gw.lda = H;
-        gw.B = l == 0 ? m->xb : m->Hh[l - 1]; gw.ldb = kin;
-        gw.part = m->part;
-        gemm<true, true, EPI_PARTIAL>(m, gw, dim3((kin + BN - 1) / BN, H / BM, kSplits), s);
+        int wparts = kSplits;
+        if (l > 0 && m->use_ws) {
+            wparts = B / ws::WROWS;
+            ws::k_wgrad_ws<<<wparts, ws::WTHREADS, ws::WSMEM, s>>>(m->mapDzw[cur], m->mapHw[l], B, m->part,
+                                                                   m->flag_dev);
+        } else {
+            GemmArgs gw{};
+            gw.M = H; gw.N = kin; gw.K = B;
+            gw.A = m->dz[cur]; gw.lda = H;
+            gw.B = l == 0 ? m->xb : m->Hh[l - 1]; gw.ldb = kin;
+            gw.part = m->part;
+            gemm<true, true, EPI_PARTIAL>(m, gw, dim3((kin + BN - 1) / BN, H / BM, kSplits), s);
+        }
         k_colsum<<<dim3(H / 32, kSplits), 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart);
         // gradient at the previous pre-activation (before this layer's weights
         // change): dz W_l, W_l read MN-major ([out][in] = [K][N])
@@ -369,7 +386,7 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
         float *gb = gslot(m->b[l]);
         float *gW = gslot(m->W[l]);
         adam(m, s, m->b[l], m->bpart, kSplits, H, lr, gb);
-        adam(m, s, m->W[l], m->part, kSplits, (size_t)H * kin, lr, gW);
+        adam(m, s, m->W[l], m->part, wparts, (size_t)H * kin, lr, gW);
         cur ^= 1;
     }
 }

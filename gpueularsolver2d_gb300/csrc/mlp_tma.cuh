@@ -253,6 +253,141 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(tmem), "r"(TMEM_COLS));
 }
 
+// ---------------------------------------------------------------------------
+// Weight gradient of a 256 x 256 hidden layer, split over the batch:
+//   part[split][m][n] = sum over the split's rows b of dZ[b][m] H[b][n]
+// (the batch, the reduction index, is the slow index of both operands, so
+// both are MN-major).  CTA `split` takes WROWS consecutive rows in 64-row
+// chunks: warp 0 loads each chunk of dZ and of H as four 64 x 64 boxes apiece
+// (TMA, 128-byte swizzle) into a three-stage ring, warp 1 accumulates the two
+// 128-row halves of the 256 x 256 product in tensor memory (all 512
+// columns), and eight warps write the FP32 partial.
+constexpr int WROWS = 1024;                     // batch rows per split
+constexpr int WCH = 64;                         // rows per chunk
+constexpr int WBOX = 64 * WCH * 2;              // one 64 (MN) x 64 (K) box: 8 KB
+constexpr int WSTAGE = 8 * WBOX;                // dZ and H boxes of one chunk: 64 KB
+constexpr int WNST = 3;
+constexpr int WSMEM = WNST * WSTAGE + 1024;
+constexpr int WEPI = 8;
+constexpr int WTHREADS = 32 * (2 + WEPI);
+// FP32 D, BF16 A and B, both MN-major (bits 15 / 16), N = 256, M = 128
+constexpr uint32_t IDESC_MN = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
+                              ((uint32_t)(ND >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+
+// MN-major operand in the 128-byte swizzle layout: 64-element (128-byte) rows
+// along MN, one per K index; 8-row K groups 1024 bytes apart (SBO), the next
+// 64 MN elements one box (8 KB) further (LBO); a K = 16 step advances the
+// start by two K groups (2048 bytes).
+__device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(WBOX >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__global__ void __launch_bounds__(WTHREADS, 1)
+    k_wgrad_ws(const __grid_constant__ CUtensorMap mapDz, const __grid_constant__ CUtensorMap mapH, int M,
+               float *__restrict__ part, int *flag) {
+    extern __shared__ unsigned char ws_raw[];
+    __shared__ __align__(8) uint64_t full[WNST], empty[WNST], tfull, mdone;
+    __shared__ uint32_t tmem_sh;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t base = (smem_u32(ws_raw) + 1023u) & ~1023u;
+    const int r0 = blockIdx.x * WROWS, nch = WROWS / WCH;
+    if (tid == 0) {
+        for (int s = 0; s < WNST; s++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&empty[s])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&tfull)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&mdone)));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n"
+                     :: "r"(smem_u32(&tmem_sh)), "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem = tmem_sh;
+    if (warp == 0 && lane == 0) {
+        // ---- producer: boxes 0..3 dZ columns 64j.., boxes 4..7 H columns 64j.. ----
+        bool ok = true;
+        int c = 0;
+        for (; c < nch && r0 + c * WCH < M; c++) {
+            const int st = c % WNST;
+            if (!wait(smem_u32(&empty[st]), ((c / WNST) & 1) ^ 1)) { ok = false; break; }
+            expect_tx(smem_u32(&full[st]), WSTAGE);
+            const uint32_t dst = base + st * WSTAGE;
+            for (int j = 0; j < 4; j++) {
+                tma_load(dst + j * WBOX, &mapDz, 64 * j, r0 + c * WCH, smem_u32(&full[st]));
+                tma_load(dst + (4 + j) * WBOX, &mapH, 64 * j, r0 + c * WCH, smem_u32(&full[st]));
+            }
+        }
+        if (!ok) atomicExch(flag, 1);
+        for (int k = c - WNST > 0 ? c - WNST : 0; k < c; k++) wait(smem_u32(&full[k % WNST]), (k / WNST) & 1);
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer: D_h (columns 256 h..) += dZ[:, 128 h..]^T H ----
+        bool ok = true;
+        for (int c = 0; c < nch && r0 + c * WCH < M && ok; c++) {
+            const int st = c % WNST;
+            if (!wait(smem_u32(&full[st]), (c / WNST) & 1)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            const uint32_t src = base + st * WSTAGE;
+#pragma unroll
+            for (int kk = 0; kk < WCH / 16; kk++)
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const uint64_t ad = desc_sw128_mn(src + (2 * h) * WBOX + kk * 2048);
+                    const uint64_t bd = desc_sw128_mn(src + 4 * WBOX + kk * 2048);
+                    const uint32_t accumulate = (c > 0 || kk > 0) ? 1u : 0u;
+                    asm volatile("{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                                 :: "r"(tmem + (uint32_t)(h * ND)), "l"(ad), "l"(bd), "r"(IDESC_MN), "r"(accumulate));
+                }
+            commit(smem_u32(&empty[st]));
+        }
+        if (ok) commit(smem_u32(&tfull));
+        else atomicExch(flag, 1);
+        commit(smem_u32(&mdone));
+        wait(smem_u32(&mdone), 0);
+    } else if (warp >= 2) {
+        // ---- epilogue: warp -> (32-lane quarter, half of the rows' M-half) ----
+        const int quarter = warp & 3, h = (warp - 2) >> 2;
+        int okw = lane == 0 ? (int)wait(smem_u32(&tfull), 0) : 0;
+        okw = __shfl_sync(0xffffffffu, okw, 0);
+        if (okw) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            const int m = h * BM + quarter * 32 + lane;
+            float *dst = part + ((size_t)blockIdx.x * ND + m) * ND;
+#pragma unroll 1
+            for (int ch = 0; ch < ND / 16; ch++) {
+                uint32_t v[16];
+                const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(h * ND + ch * 16);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];\n"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                float4 *o = (float4 *)(dst + ch * 16);
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    o[j] = make_float4(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1]),
+                                       __uint_as_float(v[4 * j + 2]), __uint_as_float(v[4 * j + 3]));
+            }
+        } else if (lane == 0) {
+            atomicExch(flag, 1);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(tmem), "r"(TMEM_COLS));
+}
+
 }  // namespace ws
 }  // namespace mlp
 }  // namespace e2d
