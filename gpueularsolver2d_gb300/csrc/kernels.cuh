@@ -853,7 +853,9 @@ __device__ __forceinline__ void block_partial(float drho, int bad, double *slot,
     }
 }
 
-template <typename T>
+// GDT: the global time-step option (its FP64 slot is converted per thread, an
+// FP64-pipe instruction the local-step variant does without).
+template <typename T, bool GDT>
 __global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, int smooth,
                                                 const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
                                                 const T *__restrict__ dt, const V4<T> *W0, V4<T> *Wout,
@@ -864,7 +866,9 @@ __global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, i
     T drho = T(0.0);
     int bad = 0;
     if (i < m.n)
-        update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, ctl, st, dt, i), W0, Wout, part != nullptr, drho, bad);
+        update_cell(m, f, rk, smooth, i, src, res,
+                    GDT ? (T)__longlong_as_double((long long)ctl->dtmin[st]) : dt[i], W0, Wout, part != nullptr,
+                    drho, bad);
     if (!part) return;
     block_partial(drho, bad, part + blockIdx.x, &ctl->nbad);
 }
@@ -1030,8 +1034,12 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
             launch_chained(k_smooth<T>, G, B, s, p.m, p.f.irs_eps, src, p.res, dst, p.ctl);
             src = dst;
         }
-        launch_chained(k_update<T>, G, B, s, p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
-                       p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
+        if (p.f.global_dt)
+            launch_chained(k_update<T, true>, G, B, s, p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
+                           p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
+        else
+            launch_chained(k_update<T, false>, G, B, s, p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
+                           p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
     }
     enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, sizeof(T) == 4, s);
 }
@@ -1065,8 +1073,12 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
             src = dst;
         }
         mark(3);
-        k_update<T><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
-                                    p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
+        if (p.f.global_dt)
+            k_update<T, true><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
+                                              p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
+        else
+            k_update<T, false><<<G, B, 0, s>>>(p.m, p.f, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
+                                               p.W[0], Wout, last ? p.part : nullptr, p.ctl, st);
         done();
     }
     mark(4); enqueue_resid(p.part, G, p.ctl, p.hist, p.hist_cap, sizeof(T) == 4, s); done();

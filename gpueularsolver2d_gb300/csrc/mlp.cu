@@ -60,8 +60,15 @@ __global__ void __launch_bounds__(256) k_adam_dev(int count, const float *__rest
                                                   float *__restrict__ grad_out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
-    float g = 0.f;
-    for (int p = 0; p < nparts; p++) g += part[(size_t)p * pstride + i];
+    // sum of the split partials: eight independent loads in flight per
+    // round, the eight running sums added in a fixed tree (deterministic)
+    float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int p = 0;
+    for (; p + 8 <= nparts; p += 8)
+#pragma unroll
+        for (int j = 0; j < 8; j++) a[j] += part[(size_t)(p + j) * pstride + i];
+    for (; p < nparts; p++) a[0] += part[(size_t)p * pstride + i];
+    const float g = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
     if (grad_out) grad_out[i] = g;
     if (!lr_dev) return;
     const float lr = *lr_dev;
@@ -273,7 +280,7 @@ int ensure_batch(e2d_mlp *m, int B) {
     // ws::WROWS rows of the batch for the warp-specialised one
     const int nparts = std::max(kSplits, B / ws::WROWS);
     if ((rc = m->alloc(&m->part, sizeof(float) * (size_t)nparts * H * H))) return rc;
-    if ((rc = m->alloc(&m->bpart, sizeof(float) * (size_t)kSplits * (NOUT * H + NOUT + H)))) return rc;
+    if ((rc = m->alloc(&m->bpart, sizeof(float) * (size_t)nparts * (NOUT * H + NOUT + H)))) return rc;
     if ((rc = m->alloc(&m->loss_part, sizeof(double) * (B / 256)))) return rc;
     build_ws_maps(m);
     return E2D_OK;
@@ -359,7 +366,7 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
         if (l > 0 && m->use_ws) {
             wparts = B / ws::WROWS;
             ws::k_wgrad_ws<<<wparts, ws::WTHREADS, ws::WSMEM, s>>>(m->mapDzw[cur], m->mapHw[l], B, m->part,
-                                                                   m->flag_dev);
+                                                                   m->bpart, m->flag_dev);
         } else {
             GemmArgs gw{};
             gw.M = H; gw.N = kin; gw.K = B;
@@ -368,7 +375,9 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
             gw.part = m->part;
             gemm<true, true, EPI_PARTIAL>(m, gw, dim3((kin + BN - 1) / BN, H / BM, kSplits), s);
         }
-        k_colsum<<<dim3(H / 32, kSplits), 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart);
+        // (the warp-specialised weight-gradient kernel also writes the bias
+        // gradient's partials, one per split)
+        if (!(l > 0 && m->use_ws)) k_colsum<<<dim3(H / 32, kSplits), 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart);
         // gradient at the previous pre-activation (before this layer's weights
         // change): dz W_l, W_l read MN-major ([out][in] = [K][N])
         if (l > 0 && m->use_ws) {
@@ -385,7 +394,7 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
         }
         float *gb = gslot(m->b[l]);
         float *gW = gslot(m->W[l]);
-        adam(m, s, m->b[l], m->bpart, kSplits, H, lr, gb);
+        adam(m, s, m->b[l], m->bpart, wparts, H, lr, gb);
         adam(m, s, m->W[l], m->part, wparts, (size_t)H * kin, lr, gW);
         cur ^= 1;
     }

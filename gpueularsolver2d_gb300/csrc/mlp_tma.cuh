@@ -188,6 +188,15 @@ __global__ void __launch_bounds__(THREADS, 1)
         int li = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, li++) {
             const int acc = li & 1;
+            const int m = t * BM + quarter * 32 + lane;
+            // the data gradient's pre-activations of this thread's 64 columns,
+            // requested before the accumulator is ready (they do not depend on it)
+            __align__(16) uint4 zpre[8];
+            if (EPI == EPI_GELU_BWD && m < g.M) {
+                const uint4 *zi = (const uint4 *)(g.zin + (size_t)m * ND + group * 64);
+#pragma unroll
+                for (int j = 0; j < 8; j++) zpre[j] = zi[j];
+            }
             // one lane waits and the warp follows its answer, so that the warp
             // stays converged for the collective tensor-memory loads
             int okw = lane == 0 ? (int)wait(smem_u32(&tfull[acc]), (li >> 1) & 1) : 0;
@@ -197,8 +206,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n");
-            const int m = t * BM + quarter * 32 + lane;
-#pragma unroll 1
+#pragma unroll
             for (int ch = 0; ch < 4; ch++) {
                 const int n0 = group * 64 + ch * 16;
                 uint32_t v[16];
@@ -230,9 +238,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     zo[0] = ((const uint4 *)z2)[0];
                     zo[1] = ((const uint4 *)z2)[1];
                 } else {
-                    const uint4 *zi = (const uint4 *)(g.zin + (size_t)m * ND + n0);
-                    __align__(16) uint4 zz[2] = {zi[0], zi[1]};
-                    const __nv_bfloat162 *z2 = (const __nv_bfloat162 *)zz;
+                    const __nv_bfloat162 *z2 = (const __nv_bfloat162 *)&zpre[2 * ch];
 #pragma unroll
                     for (int j = 0; j < 8; j++)
                         o2[j] = __floats2bfloat162_rn(__uint_as_float(v[2 * j]) * gelu_grad(__bfloat162float(z2[j].x)),
@@ -261,7 +267,11 @@ __global__ void __launch_bounds__(THREADS, 1)
 // chunks: warp 0 loads each chunk of dZ and of H as four 64 x 64 boxes apiece
 // (TMA, 128-byte swizzle) into a three-stage ring, warp 1 accumulates the two
 // 128-row halves of the 256 x 256 product in tensor memory (all 512
-// columns), and eight warps write the FP32 partial.
+// columns), and eight warps write the FP32 partial.  While the MMAs run, the
+// same eight warps sum each column of dZ over the split's rows from the
+// staged boxes (thread m: column m), the bias gradient's partial
+// bpart[split][m]; a stage is released when its MMAs and these reads are
+// done.
 constexpr int WROWS = 1024;                     // batch rows per split
 constexpr int WCH = 64;                         // rows per chunk
 constexpr int WBOX = 64 * WCH * 2;              // one 64 (MN) x 64 (K) box: 8 KB
@@ -285,7 +295,7 @@ __device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t addr) {
 
 __global__ void __launch_bounds__(WTHREADS, 1)
     k_wgrad_ws(const __grid_constant__ CUtensorMap mapDz, const __grid_constant__ CUtensorMap mapH, int M,
-               float *__restrict__ part, int *flag) {
+               float *__restrict__ part, float *__restrict__ bpart, int *flag) {
     extern __shared__ unsigned char ws_raw[];
     __shared__ __align__(8) uint64_t full[WNST], empty[WNST], tfull, mdone;
     __shared__ uint32_t tmem_sh;
@@ -295,7 +305,8 @@ __global__ void __launch_bounds__(WTHREADS, 1)
     if (tid == 0) {
         for (int s = 0; s < WNST; s++) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&full[s])));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&empty[s])));
+            // released by the MMAs' commit and by each column-sum warp
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" :: "r"(smem_u32(&empty[s])), "n"(1 + WEPI));
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&tfull)));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&mdone)));
@@ -352,9 +363,28 @@ __global__ void __launch_bounds__(WTHREADS, 1)
         commit(smem_u32(&mdone));
         wait(smem_u32(&mdone), 0);
     } else if (warp >= 2) {
+        // ---- column sums of dZ while the MMAs run (thread e: column e) ----
+        const int e = tid - 64;
+        const int bj = e >> 6, chunk = (e & 63) >> 3, elem = e & 7;
+        float bsum = 0.0f;
+        int okw = 1;
+        for (int c = 0; c < nch && r0 + c * WCH < M; c++) {
+            const int st = c % WNST;
+            okw = lane == 0 ? (int)wait(smem_u32(&full[st]), (c / WNST) & 1) : 0;
+            okw = __shfl_sync(0xffffffffu, okw, 0);
+            if (!okw) break;
+            // box bj of dZ: row k at 128 k bytes, its 16-byte chunks swizzled by k % 8
+            const unsigned char *box = ws_raw + (base - smem_u32(ws_raw)) + st * WSTAGE + bj * WBOX;
+#pragma unroll 8
+            for (int k = 0; k < WCH; k++)
+                bsum += __bfloat162float(*(const bf16 *)(box + k * 128 + ((chunk ^ (k & 7)) << 4) + elem * 2));
+            __syncwarp();
+            if (lane == 0) arrive(smem_u32(&empty[st]));
+        }
+        if (okw) bpart[(size_t)blockIdx.x * ND + e] = bsum;
         // ---- epilogue: warp -> (32-lane quarter, half of the rows' M-half) ----
         const int quarter = warp & 3, h = (warp - 2) >> 2;
-        int okw = lane == 0 ? (int)wait(smem_u32(&tfull), 0) : 0;
+        if (okw) okw = lane == 0 ? (int)wait(smem_u32(&tfull), 0) : 0;
         okw = __shfl_sync(0xffffffffu, okw, 0);
         if (okw) {
             asm volatile("tcgen05.fence::after_thread_sync;\n");
