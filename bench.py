@@ -497,6 +497,8 @@ def mlp_record(layers: int, steps: int, warmup: int) -> dict:
     import torch
     import gpueularsolver2d_gb300 as e2d
     L, B = layers, 65536
+    # the warp-specialised hidden-layer kernels or an error, never the per-tile fallback
+    os.environ.setdefault("E2D_MLP_WS", "1")
     net = e2d.MLP(nhidden=L, batch=B, seed=3)
     rng = np.random.default_rng(0)
     n = 32768 * 64
@@ -519,7 +521,10 @@ def mlp_record(layers: int, steps: int, warmup: int) -> dict:
             "config": {"workload": f"MLP 32 -> {L} x 256 GELU -> 4, batch {B}, Adam"},
             "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
                          "peak_source": f"{kind} bf16_tflops (MEASURED_PEAKS.json)", "traffic": None},
-            "gpu_launches": (6 * L + 6) * steps}
+            # per step: step counter, gather, L forward GEMMs, the output layer,
+            # L weight gradients, L - 1 data gradients, one bias column sum
+            # (first layer), L + 1 Adam launches
+            "gpu_launches": (4 * L + 4) * steps}
 
 
 def run_mlp(args):

@@ -47,39 +47,60 @@ __global__ void k_step_update(int *step, float beta1, float beta2, float *bc) {
     bc[1] = 1.f - powf(beta2, (float)s);
 }
 
-// wbf (may be null): the bf16 copy used by the GEMMs, wbfT (may be null) its
-// transpose ([cols][rows], the data-gradient GEMM's K-major operand); lr
-// (device, read at run time so that the host can schedule it) null: gradient
-// only.
-__global__ void __launch_bounds__(256) k_adam_dev(int count, const float *__restrict__ part, int nparts,
-                                                  size_t pstride, float *__restrict__ w32, bf16 *__restrict__ wbf,
-                                                  bf16 *__restrict__ wbfT, int rows, int cols,
-                                                  float *__restrict__ m, float *__restrict__ v,
-                                                  const float *__restrict__ lr_dev,
-                                                  float beta1, float beta2, float eps, const float *__restrict__ bc,
-                                                  float *__restrict__ grad_out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
-    // sum of the split partials: eight independent loads in flight per
-    // round, the eight running sums added in a fixed tree (deterministic)
-    float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    int p = 0;
-    for (; p + 8 <= nparts; p += 8)
+// One parameter tensor's Adam step: its gradient is the sum of nparts
+// partials part[p * pstride + i]; wbf (may be null) is the bf16 copy used by
+// the GEMMs, wbfT (may be null) its transpose ([cols][rows], the data-gradient
+// GEMM's K-major operand); grad_out (may be null) receives the gradient.
+struct AdamSeg {
+    const float *part;
+    size_t pstride;
+    int nparts, count, rows, cols;
+    float *w32, *m, *v;
+    bf16 *wbf, *wbfT;
+    float *grad_out;
+};
+
+// Adam on two tensors (a layer's weights and bias) in one launch: blocks
+// [0, nb0) take seg0, the rest seg1, 32 parameters per 256-thread block.
+// Warp j sums partials j, j + 8, ... of the block's parameters (lane =
+// parameter, 128-byte loads, four in flight), the eight warp sums are added
+// in a fixed tree (deterministic), and warp 0 applies the step.  lr (device,
+// read at run time so that the host can schedule it) null: gradient only.
+__global__ void __launch_bounds__(256) k_adam_seg(AdamSeg seg0, AdamSeg seg1, int nb0,
+                                                  const float *__restrict__ lr_dev, float beta1, float beta2,
+                                                  float eps, const float *__restrict__ bc) {
+    __shared__ float red[8][32];
+    const bool first = (int)blockIdx.x < nb0;
+    const AdamSeg &S = first ? seg0 : seg1;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const int i = ((int)blockIdx.x - (first ? 0 : nb0)) * 32 + lane;
+    float a[4] = {0.f, 0.f, 0.f, 0.f};
+    if (i < S.count) {
+        const float *pp = S.part + i;
+        int p = wp;
+        for (; p + 24 < S.nparts; p += 32)
 #pragma unroll
-        for (int j = 0; j < 8; j++) a[j] += part[(size_t)(p + j) * pstride + i];
-    for (; p < nparts; p++) a[0] += part[(size_t)p * pstride + i];
-    const float g = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
-    if (grad_out) grad_out[i] = g;
+            for (int j = 0; j < 4; j++) a[j] += pp[(size_t)(p + 8 * j) * S.pstride];
+        if (p < S.nparts) a[0] += pp[(size_t)p * S.pstride];
+        if (p + 8 < S.nparts) a[1] += pp[(size_t)(p + 8) * S.pstride];
+        if (p + 16 < S.nparts) a[2] += pp[(size_t)(p + 16) * S.pstride];
+    }
+    red[wp][lane] = (a[0] + a[1]) + (a[2] + a[3]);
+    __syncthreads();
+    if (wp != 0 || i >= S.count) return;
+    const float g = ((red[0][lane] + red[1][lane]) + (red[2][lane] + red[3][lane])) +
+                    ((red[4][lane] + red[5][lane]) + (red[6][lane] + red[7][lane]));
+    if (S.grad_out) S.grad_out[i] = g;
     if (!lr_dev) return;
     const float lr = *lr_dev;
-    const float mi = beta1 * m[i] + (1.f - beta1) * g;
-    const float vi = beta2 * v[i] + (1.f - beta2) * g * g;
-    m[i] = mi;
-    v[i] = vi;
-    const float w = w32[i] - lr * (mi / bc[0]) / (sqrtf(vi / bc[1]) + eps);
-    w32[i] = w;
-    if (wbf) wbf[i] = __float2bfloat16_rn(w);
-    if (wbfT) wbfT[(size_t)(i % cols) * rows + i / cols] = __float2bfloat16_rn(w);
+    const float mi = beta1 * S.m[i] + (1.f - beta1) * g;
+    const float vi = beta2 * S.v[i] + (1.f - beta2) * g * g;
+    S.m[i] = mi;
+    S.v[i] = vi;
+    const float w = S.w32[i] - lr * (mi / bc[0]) / (sqrtf(vi / bc[1]) + eps);
+    S.w32[i] = w;
+    if (S.wbf) S.wbf[i] = __float2bfloat16_rn(w);
+    if (S.wbfT) S.wbfT[(size_t)(i % S.cols) * S.rows + i / S.cols] = __float2bfloat16_rn(w);
 }
 
 // bf16 copy of a [rows][cols] matrix, and (bT non-null) of its transpose
@@ -135,7 +156,7 @@ struct e2d_mlp {
     int B = 0;
     bf16 *xb = nullptr;  // [B][NIN]
     float *tb = nullptr, *y = nullptr, *dy = nullptr;
-    std::vector<bf16 *> Z, Hh;  // [nhidden] of [B][H]
+    std::vector<bf16 *> Gd, Hh;  // [nhidden] of [B][H]: gelu'(z) and gelu(z) of each hidden layer
     bf16 *dz[2] = {nullptr, nullptr};  // [B][H]
     float *part = nullptr;      // weight-gradient partials (largest tensor x kSplits)
     float *bpart = nullptr;     // bias-gradient partials
@@ -157,7 +178,9 @@ struct e2d_mlp {
     bool use_ws = false;
     int nsm = 0;
     std::vector<CUtensorMap> mapHf, mapW, mapWT, mapHw;
-    CUtensorMap mapDz[2], mapDzw[2];  // dz[0] / dz[1] with 128-row boxes (data gradient), 64-row boxes (weights)
+    std::vector<CUtensorMap> mapHo, mapGo;  // Hh[l], Gd[l] in 32 x 32 epilogue slabs
+    // dz[0] / dz[1] with 128-row boxes (data gradient), 64-row boxes (weights), 32 x 32 slabs
+    CUtensorMap mapDz[2], mapDzw[2], mapDzo[2];
     std::vector<double> loss_host;
 
     ~e2d_mlp() {
@@ -194,36 +217,48 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 // 2D map of a row-major [rows][cols] bf16 matrix, box 64 columns x box_rows,
 // 128-byte swizzle (the layout the ws kernel's descriptors describe)
-bool map_2d(CUtensorMap *map, const bf16 *ptr, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+// Row-major [rows][cols] bf16 tensor, boxes of box_rows x 64 columns with the
+// 128-byte swizzle (MMA operands) or, slab = true, 32 x 32 with the 64-byte
+// swizzle (the epilogue slabs of ws::k_gemm_ws).
+bool map_2d(CUtensorMap *map, const bf16 *ptr, uint64_t rows, uint64_t cols, uint32_t box_rows, bool slab = false) {
     auto enc = tensor_map_encoder();
     if (!enc) return false;
     const cuuint64_t dims[2] = {cols, rows};
     const cuuint64_t strides[1] = {cols * sizeof(bf16)};
-    const cuuint32_t box[2] = {(cuuint32_t)ws::KC, box_rows};
+    const cuuint32_t box[2] = {slab ? 32u : (cuuint32_t)ws::KC, slab ? 32u : box_rows};
     const cuuint32_t estr[2] = {1, 1};
     return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)ptr, dims, strides, box, estr,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+               CU_TENSOR_MAP_INTERLEAVE_NONE, slab ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 // Tensor maps of the warp-specialised GEMMs once the batch buffers exist;
 // use_ws stays false (the per-tile kernel runs every layer) when the driver
-// entry point or a map is not available, or E2D_MLP_WS=0.
-void build_ws_maps(e2d_mlp *m) {
+// entry point, a map or the shared-memory size is not available, or
+// E2D_MLP_WS=0.  With E2D_MLP_WS=1 that is an error instead.
+int build_ws_maps(e2d_mlp *m) {
     m->use_ws = false;
     const char *env = std::getenv("E2D_MLP_WS");
-    if ((env && env[0] == '0') || m->nhidden < 2) return;
+    const bool required = env && env[0] == '1';
+    if ((env && env[0] == '0') || m->nhidden < 2) return E2D_OK;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&m->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
         cudaGetLastError();
-        return;
+        if (required) { set_error("E2D_MLP_WS=1: no device attributes"); return E2D_ERR_CUDA; }
+        return E2D_OK;
     }
     m->mapHf.assign(m->nhidden, CUtensorMap{});
     m->mapW.assign(m->nhidden, CUtensorMap{});
     m->mapWT.assign(m->nhidden, CUtensorMap{});
     m->mapHw.assign(m->nhidden, CUtensorMap{});
+    m->mapHo.assign(m->nhidden, CUtensorMap{});
+    m->mapGo.assign(m->nhidden, CUtensorMap{});
     bool ok = m->B % ws::WROWS == 0;
+    for (int l = 0; l < m->nhidden && ok; l++) {
+        ok = ok && map_2d(&m->mapHo[l], m->Hh[l], m->B, H, 32, true);
+        ok = ok && map_2d(&m->mapGo[l], m->Gd[l], m->B, H, 32, true);
+    }
     for (int l = 1; l < m->nhidden && ok; l++) {
         ok = ok && map_2d(&m->mapHf[l], m->Hh[l - 1], m->B, H, ws::BM);
         ok = ok && map_2d(&m->mapW[l], m->W[l].wbf, H, H, ws::ND);
@@ -233,6 +268,7 @@ void build_ws_maps(e2d_mlp *m) {
     for (int k = 0; k < 2 && ok; k++) {
         ok = ok && map_2d(&m->mapDz[k], m->dz[k], m->B, H, ws::BM);
         ok = ok && map_2d(&m->mapDzw[k], m->dz[k], m->B, H, ws::WCH);
+        ok = ok && map_2d(&m->mapDzo[k], m->dz[k], m->B, H, 32, true);
     }
     if (ok && cudaFuncSetAttribute(ws::k_gemm_ws<EPI_BIAS_GELU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    ws::SMEM) == cudaSuccess &&
@@ -241,12 +277,19 @@ void build_ws_maps(e2d_mlp *m) {
         cudaFuncSetAttribute(ws::k_wgrad_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, ws::WSMEM) == cudaSuccess)
         m->use_ws = true;
     cudaGetLastError();
+    if (required && !m->use_ws) {
+        set_error("E2D_MLP_WS=1: the warp-specialised GEMMs cannot run here (tensor maps or shared memory)");
+        return E2D_ERR_CUDA;
+    }
+    return E2D_OK;
 }
 
-template <int EPI> void gemm_ws(e2d_mlp *m, const CUtensorMap &a, const CUtensorMap &w, ws::Args g, cudaStream_t s) {
+template <int EPI>
+void gemm_ws(e2d_mlp *m, const CUtensorMap &a, const CUtensorMap &w, const CUtensorMap &out, const CUtensorMap &aux,
+             ws::Args g, cudaStream_t s) {
     g.flag = m->flag_dev;
     const int ntiles = g.M / ws::BM, grid = ntiles < m->nsm ? ntiles : m->nsm;
-    ws::k_gemm_ws<EPI><<<grid, ws::THREADS, ws::SMEM, s>>>(a, w, g);
+    ws::k_gemm_ws<EPI><<<grid, ws::THREADS, ws::SMEM, s>>>(a, w, out, aux, g);
 }
 
 size_t param_count(const e2d_mlp *m) {
@@ -268,10 +311,10 @@ int ensure_batch(e2d_mlp *m, int B) {
     if ((rc = m->alloc(&m->tb, sizeof(float) * (size_t)B * NOUT))) return rc;
     if ((rc = m->alloc(&m->y, sizeof(float) * (size_t)B * NOUT))) return rc;
     if ((rc = m->alloc(&m->dy, sizeof(float) * (size_t)B * NOUT))) return rc;
-    m->Z.resize(m->nhidden);
+    m->Gd.resize(m->nhidden);
     m->Hh.resize(m->nhidden);
     for (int l = 0; l < m->nhidden; l++) {
-        if ((rc = m->alloc(&m->Z[l], sizeof(bf16) * (size_t)B * H))) return rc;
+        if ((rc = m->alloc(&m->Gd[l], sizeof(bf16) * (size_t)B * H))) return rc;
         if ((rc = m->alloc(&m->Hh[l], sizeof(bf16) * (size_t)B * H))) return rc;
     }
     for (int k = 0; k < 2; k++)
@@ -280,18 +323,27 @@ int ensure_batch(e2d_mlp *m, int B) {
     // ws::WROWS rows of the batch for the warp-specialised one
     const int nparts = std::max(kSplits, B / ws::WROWS);
     if ((rc = m->alloc(&m->part, sizeof(float) * (size_t)nparts * H * H))) return rc;
-    if ((rc = m->alloc(&m->bpart, sizeof(float) * (size_t)nparts * (NOUT * H + NOUT + H)))) return rc;
+    // bias / output-layer partials: the same, or one per 256 rows for the output layer
+    if ((rc = m->alloc(&m->bpart, sizeof(float) * (size_t)std::max(nparts, B / 256) * (NOUT * H + NOUT + H))))
+        return rc;
     if ((rc = m->alloc(&m->loss_part, sizeof(double) * (B / 256)))) return rc;
-    build_ws_maps(m);
-    return E2D_OK;
+    return build_ws_maps(m);
 }
 
-void adam(e2d_mlp *m, cudaStream_t s, Tensor &t, const float *part, int nparts, size_t pstride, const float *lr,
-          float *grad_out) {
+AdamSeg adam_seg(const Tensor &t, const float *part, int nparts, size_t pstride, float *grad_out) {
+    AdamSeg g{};
+    g.part = part; g.pstride = pstride; g.nparts = nparts; g.count = t.count();
+    g.rows = t.rows; g.cols = t.cols;
+    g.w32 = t.w32; g.m = t.m; g.v = t.v; g.wbf = t.wbf; g.wbfT = t.wbfT;
+    g.grad_out = grad_out;
+    return g;
+}
+
+// Adam on a weight tensor and its bias in one launch.
+void adam2(e2d_mlp *m, cudaStream_t s, const AdamSeg &w, const AdamSeg &b, const float *lr) {
     const auto &c = m->cfg;
-    k_adam_dev<<<(t.count() + 255) / 256, 256, 0, s>>>(t.count(), part, nparts, pstride, t.w32, t.wbf, t.wbfT,
-                                                        t.rows, t.cols, t.m, t.v, lr, (float)c.beta1, (float)c.beta2,
-                                                        (float)c.eps, m->bc_dev, grad_out);
+    const int nb0 = (w.count + 31) / 32, nb1 = (b.count + 31) / 32;
+    k_adam_seg<<<nb0 + nb1, 256, 0, s>>>(w, b, nb0, lr, (float)c.beta1, (float)c.beta2, (float)c.eps, m->bc_dev);
 }
 
 template <bool TA, bool TB, int EPI> void gemm(e2d_mlp *m, GemmArgs g, dim3 grid, cudaStream_t s) {
@@ -312,14 +364,15 @@ int check_flag(e2d_mlp *m) {
     return E2D_OK;
 }
 
-// Forward on the batch in xb (rows B); with targets, the loss partials and dy.
+// Forward on the batch in xb (rows B) through the hidden layers; without
+// targets (inference) also the output layer into y.
 void forward(e2d_mlp *m, cudaStream_t s, bool with_loss) {
     const int B = m->B;
     for (int l = 0; l < m->nhidden; l++) {
         if (l > 0 && m->use_ws) {
             ws::Args a{};
-            a.M = B; a.bias = m->b[l].w32; a.out = m->Hh[l]; a.zout = m->Z[l];
-            gemm_ws<EPI_BIAS_GELU>(m, m->mapHf[l], m->mapW[l], a, s);
+            a.M = B; a.bias = m->b[l].w32;
+            gemm_ws<EPI_BIAS_GELU>(m, m->mapHf[l], m->mapW[l], m->mapHo[l], m->mapGo[l], a, s);
             continue;
         }
         GemmArgs g{};
@@ -327,13 +380,15 @@ void forward(e2d_mlp *m, cudaStream_t s, bool with_loss) {
         g.A = l == 0 ? m->xb : m->Hh[l - 1];
         g.lda = g.K;
         g.B = m->W[l].wbf; g.ldb = g.K;
-        g.bias = m->b[l].w32; g.out = m->Hh[l]; g.zout = m->Z[l]; g.ldc = H;
+        g.bias = m->b[l].w32; g.out = m->Hh[l]; g.zout = m->Gd[l]; g.ldc = H;
         gemm<false, false, EPI_BIAS_GELU>(m, g, dim3(H / BN, (B + BM - 1) / BM, 1), s);
     }
+    // with targets the output layer runs at the start of the backward pass
+    // (k_out_train), fused with its gradient
+    if (with_loss) return;
     const Tensor &Wo = m->W[m->nhidden], &bo = m->b[m->nhidden];
-    k_out_fwd_loss<H, NOUT><<<(B + 255) / 256, 256, 0, s>>>(B, m->Hh[m->nhidden - 1], Wo.w32, bo.w32,
-                                                            with_loss ? m->tb : nullptr, m->y, m->dy,
-                                                            with_loss ? m->loss_part : nullptr);
+    k_out_fwd_loss<H, NOUT><<<(B + 255) / 256, 256, 0, s>>>(B, m->Hh[m->nhidden - 1], Wo.w32, bo.w32, nullptr,
+                                                            m->y, m->dy, nullptr);
 }
 
 // Backward + Adam with the step size at lr (null: gradient only, written to
@@ -347,15 +402,18 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
         goff -= t.count();
         return m->grad + goff;
     };
-    // output layer: weight / bias partials, then the gradient at the last pre-activation
+    // output layer, forward and backward in one pass (loss, its weight / bias
+    // partials, and the gradient at the last pre-activation: the output
+    // layer's data gradient times the stored gelu'(z))
     Tensor &Wo = m->W[L], &bo = m->b[L];
-    k_out_bwd_weight<H, NOUT><<<dim3(H / 32, kSplits), 256, 0, s>>>(B, rows, m->dy, m->Hh[L - 1], m->bpart);
-    k_out_bwd_data<H, NOUT><<<(B * (H / 2) + 255) / 256, 256, 0, s>>>(B, m->dy, Wo.w32, m->Z[L - 1], m->dz[0]);
+    const int oparts = B / 256;
+    k_out_train<H, NOUT><<<oparts, 256, 0, s>>>(B, m->Hh[L - 1], Wo.w32, bo.w32, m->tb, m->Gd[L - 1], m->y, m->dy,
+                                                m->dz[0], m->bpart, m->loss_part);
     const size_t ostride = NOUT * H + NOUT;
     float *gbo = gslot(bo);
     float *gWo = gslot(Wo);
-    adam(m, s, bo, m->bpart + NOUT * H, kSplits, ostride, lr, gbo);
-    adam(m, s, Wo, m->bpart, kSplits, ostride, lr, gWo);
+    adam2(m, s, adam_seg(Wo, m->bpart, oparts, ostride, gWo), adam_seg(bo, m->bpart + NOUT * H, oparts, ostride, gbo),
+          lr);
     int cur = 0;
     for (int l = L - 1; l >= 0; l--) {
         const int kin = l == 0 ? NIN : H;
@@ -382,20 +440,20 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
         // change): dz W_l, W_l read MN-major ([out][in] = [K][N])
         if (l > 0 && m->use_ws) {
             ws::Args a{};
-            a.M = B; a.zin = m->Z[l - 1]; a.out = m->dz[cur ^ 1];
-            gemm_ws<EPI_GELU_BWD>(m, m->mapDz[cur], m->mapWT[l], a, s);
+            a.M = B;
+            gemm_ws<EPI_GELU_BWD>(m, m->mapDz[cur], m->mapWT[l], m->mapDzo[cur ^ 1], m->mapGo[l - 1], a, s);
         } else if (l > 0) {
             GemmArgs gd{};
             gd.M = B; gd.N = H; gd.K = H;
             gd.A = m->dz[cur]; gd.lda = H;
             gd.B = m->W[l].wbf; gd.ldb = H;
-            gd.zin = m->Z[l - 1]; gd.out = m->dz[cur ^ 1]; gd.ldc = H;
+            gd.zin = m->Gd[l - 1]; gd.out = m->dz[cur ^ 1]; gd.ldc = H;
             gemm<false, true, EPI_GELU_BWD>(m, gd, dim3(H / BN, (B + BM - 1) / BM, 1), s);
         }
         float *gb = gslot(m->b[l]);
         float *gW = gslot(m->W[l]);
-        adam(m, s, m->b[l], m->bpart, wparts, H, lr, gb);
-        adam(m, s, m->W[l], m->part, wparts, (size_t)H * kin, lr, gW);
+        adam2(m, s, adam_seg(m->W[l], m->part, wparts, (size_t)H * kin, gW), adam_seg(m->b[l], m->bpart, wparts, H, gb),
+              lr);
         cur ^= 1;
     }
 }

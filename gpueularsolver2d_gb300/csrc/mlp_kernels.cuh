@@ -15,40 +15,38 @@ typedef __nv_bfloat16 bf16;
 
 constexpr int BM = 128, BN = 128;  // CTA tile of every GEMM
 
-// Phi(x) and phi(x), the standard normal distribution and density, for GELU
-// (x Phi(x)) and its derivative (Phi(x) + x phi(x)).  Phi comes from
-// erf(|x| / sqrt 2) by Abramowitz and Stegun's rational approximation 7.1.26
-// (Handbook of Mathematical Functions, 1964: erf(u) = 1 - t (a1 + t (a2 + t (a3
-// + t (a4 + t a5)))) exp(-u^2), t = 1 / (1 + p u), absolute error <= 1.5e-7),
-// whose exp(-u^2) = exp(-x^2 / 2) is also phi's; a dozen instructions instead
-// of an erf and an exp, well below the bf16 rounding of every activation.
-__device__ __forceinline__ void normal_parts(float x, float &Phi, float &phi) {
-    const float u = fabsf(x) * 0.70710678118654752f;
-    const float t = __fdividef(1.0f, fmaf(0.3275911f, u, 1.0f));
-    const float P = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f),
-                                     -0.284496736f), 0.254829592f);
-    const float e = __expf(-0.5f * x * x);
-    const float q = 0.5f * P * e;  // 0.5 (1 - erf(|x| / sqrt 2))
-    Phi = x >= 0.0f ? 1.0f - q : q;
-    phi = e * 0.39894228040143268f;
+// GELU in its tanh form (Hendrycks and Gimpel, "Gaussian Error Linear Units",
+// 2016): gelu(x) = x (1 + tanh(u)) / 2 with u = sqrt(2 / pi) (x + 0.044715 x^3),
+// and its derivative gelu'(x) = (1 + t) / 2 + x (1 - t^2) u'(x) / 2, t = tanh(u).
+// One tanh.approx.f32 (the special-function unit's hyperbolic tangent, relative
+// error about 2^-11) serves both; the forward epilogue stores gelu'(z) beside
+// gelu(z), so the backward pass multiplies instead of re-evaluating.
+__device__ __forceinline__ float tanh_approx(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+constexpr float kGeluC0 = 0.7978845608028654f;  // sqrt(2 / pi)
+constexpr float kGeluC1 = 0.044715f;
+
+__device__ __forceinline__ void gelu_and_grad(float x, float &h, float &g) {
+    const float x2 = x * x;
+    const float t = tanh_approx(kGeluC0 * x * fmaf(kGeluC1, x2, 1.0f));
+    const float hx = 0.5f * x;
+    h = fmaf(hx, t, hx);
+    g = fmaf(hx * fmaf(-t, t, 1.0f), kGeluC0 * fmaf(3.0f * kGeluC1, x2, 1.0f), fmaf(0.5f, t, 0.5f));
 }
 
 __device__ __forceinline__ float gelu(float x) {
-    float Phi, phi;
-    normal_parts(x, Phi, phi);
-    return x * Phi;
-}
-
-__device__ __forceinline__ float gelu_grad(float x) {
-    float Phi, phi;
-    normal_parts(x, Phi, phi);
-    return fmaf(x, phi, Phi);
+    const float hx = 0.5f * x;
+    return fmaf(hx, tanh_approx(kGeluC0 * x * fmaf(kGeluC1, x * x, 1.0f)), hx);
 }
 
 // Epilogue modes of the GEMM.
 enum Epi : int {
-    EPI_BIAS_GELU = 0,  // z = acc + bias[n]; out = gelu(z), zout = z (bf16)
-    EPI_GELU_BWD = 1,   // out = acc * gelu'(zin[m,n]) (bf16)
+    EPI_BIAS_GELU = 0,  // z = acc + bias[n]; out = gelu(z), zout = gelu'(z) (bf16)
+    EPI_GELU_BWD = 1,   // out = acc * zin[m,n] (bf16), zin the forward pass's gelu'(z)
     EPI_PARTIAL = 2,    // part[split][m][n] = acc (fp32): split-K partial of a weight gradient
 };
 
@@ -63,9 +61,9 @@ struct GemmArgs {
     const bf16 *B;         // TB ? [K][ldb] : [N][ldb]
     int ldb;
     const float *bias;     // EPI_BIAS_GELU
-    const bf16 *zin;       // EPI_GELU_BWD: [M][ldc]
+    const bf16 *zin;       // EPI_GELU_BWD: [M][ldc] gelu'(z) of the layer
     bf16 *out;             // EPI_BIAS_GELU / EPI_GELU_BWD: [M][ldc]
-    bf16 *zout;            // EPI_BIAS_GELU: [M][ldc]
+    bf16 *zout;            // EPI_BIAS_GELU: [M][ldc] gelu'(z)
     float *part;           // EPI_PARTIAL: [splits][M][N]
     int ldc;
     int *flag;             // set to 1 if a wait timed out
@@ -257,8 +255,11 @@ __global__ void __launch_bounds__(256, GemmOcc<EPI>::value) k_gemm_tc(GemmArgs g
                 for (int j = 0; j < 8; j++) {
                     const float z0 = __uint_as_float(v[2 * j]) + g.bias[n + 2 * j];
                     const float z1 = __uint_as_float(v[2 * j + 1]) + g.bias[n + 2 * j + 1];
-                    z2[j] = __floats2bfloat162_rn(z0, z1);
-                    o2[j] = __floats2bfloat162_rn(gelu(z0), gelu(z1));
+                    float h0, g0, h1, g1;
+                    gelu_and_grad(z0, h0, g0);
+                    gelu_and_grad(z1, h1, g1);
+                    z2[j] = __floats2bfloat162_rn(g0, g1);
+                    o2[j] = __floats2bfloat162_rn(h0, h1);
                 }
                 uint4 *zo = (uint4 *)(g.zout + (size_t)m * g.ldc + n);
                 zo[0] = ((const uint4 *)z2)[0]; zo[1] = ((const uint4 *)z2)[1];
@@ -268,8 +269,8 @@ __global__ void __launch_bounds__(256, GemmOcc<EPI>::value) k_gemm_tc(GemmArgs g
                 const __nv_bfloat162 *z2 = (const __nv_bfloat162 *)zz;
 #pragma unroll
                 for (int j = 0; j < 8; j++)
-                    o2[j] = __floats2bfloat162_rn(__uint_as_float(v[2 * j]) * gelu_grad(__bfloat162float(z2[j].x)),
-                                                  __uint_as_float(v[2 * j + 1]) * gelu_grad(__bfloat162float(z2[j].y)));
+                    o2[j] = __floats2bfloat162_rn(__uint_as_float(v[2 * j]) * __bfloat162float(z2[j].x),
+                                                  __uint_as_float(v[2 * j + 1]) * __bfloat162float(z2[j].y));
             }
             uint4 *oo = (uint4 *)(g.out + (size_t)m * g.ldc + n);
             oo[0] = ((const uint4 *)o2)[0]; oo[1] = ((const uint4 *)o2)[1];
@@ -329,10 +330,11 @@ __global__ void __launch_bounds__(256) k_out_fwd_loss(int B, const bf16 *__restr
     }
 }
 
-// Output layer backward: dz[b][k] = (sum_o dy[b][o] W[o][k]) * gelu'(z[b][k]) (bf16).
+// Output layer backward: dz[b][k] = (sum_o dy[b][o] W[o][k]) * gd[b][k] (bf16),
+// gd = gelu'(z) of the last hidden layer as its forward epilogue stored it.
 template <int H, int NOUT>
 __global__ void __launch_bounds__(256) k_out_bwd_data(int B, const float *__restrict__ dy, const float *__restrict__ W,
-                                                      const bf16 *__restrict__ z, bf16 *__restrict__ dz) {
+                                                      const bf16 *__restrict__ gd, bf16 *__restrict__ dz) {
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;  // one (b, pair of k)
     if (idx >= (size_t)B * (H / 2)) return;
     const int b = (int)(idx / (H / 2)), k = (int)(idx % (H / 2)) * 2;
@@ -343,10 +345,120 @@ __global__ void __launch_bounds__(256) k_out_bwd_data(int B, const float *__rest
         s0 += d * W[o * H + k];
         s1 += d * W[o * H + k + 1];
     }
-    const __nv_bfloat162 zz = *(const __nv_bfloat162 *)(z + (size_t)b * H + k);
-    const __nv_bfloat162 d =
-        __floats2bfloat162_rn(s0 * gelu_grad(__bfloat162float(zz.x)), s1 * gelu_grad(__bfloat162float(zz.y)));
+    const __nv_bfloat162 gg = *(const __nv_bfloat162 *)(gd + (size_t)b * H + k);
+    const __nv_bfloat162 d = __floats2bfloat162_rn(s0 * __bfloat162float(gg.x), s1 * __bfloat162float(gg.y));
     *(__nv_bfloat162 *)(dz + (size_t)b * H + k) = d;
+}
+
+// Output layer of a training step, forward and backward in one pass over the
+// last hidden layer (256 -> NOUT on the CUDA cores), one warp per row: lane l
+// holds h[b][8l .. 8l + 7] (one 16-byte load), the NOUT dot products are
+// butterfly-reduced over the warp, then y, the squared-error loss, dY = 2 (y - t)
+// / (B NOUT), the gradient dz[b][k] = (sum_o dY[b][o] W[o][k]) gd[b][k] (bf16,
+// gd = gelu'(z) stored by the forward epilogue) and the lane's share of
+// dW = dY^T h, db = sum dY.  Block c (256 rows, 8 warps of 32 rows) writes
+// part[c][o * H + k] and part[c][NOUT * H + o] (its warps added in a fixed
+// order) and loss_part[c]: deterministic.
+template <int H, int NOUT>
+__global__ void __launch_bounds__(256, 2) k_out_train(int B, const bf16 *__restrict__ h, const float *__restrict__ W,
+                                                   const float *__restrict__ bias, const float *__restrict__ t,
+                                                   const bf16 *__restrict__ gd, float *__restrict__ y,
+                                                   float *__restrict__ dy, bf16 *__restrict__ dz,
+                                                   float *__restrict__ part, double *__restrict__ loss_part) {
+    static_assert(H == 256, "one 16-byte load per lane covers a row");
+    __shared__ float red[8][NOUT * H + NOUT];
+    __shared__ __align__(16) float Ws[NOUT * H];
+    __shared__ double lred[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, k0 = lane * 8;
+    for (int e = threadIdx.x; e < NOUT * H; e += blockDim.x) Ws[e] = W[e];
+    __syncthreads();
+    float acc[NOUT][8], dacc[NOUT];
+#pragma unroll
+    for (int o = 0; o < NOUT; o++) {
+        dacc[o] = 0.f;
+#pragma unroll
+        for (int q = 0; q < 8; q++) acc[o][q] = 0.f;
+    }
+    double l = 0.0;
+    const int r0 = blockIdx.x * 256 + warp * 32;  // B is a multiple of 256
+    constexpr int RB = 2;                          // rows whose loads are in flight together
+    for (int rb = 0; rb < 32; rb += RB) {
+        uint4 hvs[RB], gvs[RB];
+#pragma unroll
+        for (int j = 0; j < RB; j++) {
+            hvs[j] = *(const uint4 *)(h + (size_t)(r0 + rb + j) * H + k0);
+            gvs[j] = *(const uint4 *)(gd + (size_t)(r0 + rb + j) * H + k0);
+        }
+#pragma unroll
+    for (int j = 0; j < RB; j++) {
+        const int b = r0 + rb + j;
+        const uint4 hv = hvs[j], gv = gvs[j];
+        const __nv_bfloat162 *h2 = (const __nv_bfloat162 *)&hv;
+        float x[8];
+#pragma unroll
+        for (int q = 0; q < 4; q++) { x[2 * q] = __low2float(h2[q]); x[2 * q + 1] = __high2float(h2[q]); }
+        float p[NOUT];
+#pragma unroll
+        for (int o = 0; o < NOUT; o++) {
+            const float4 wa = *(const float4 *)&Ws[o * H + k0], wb = *(const float4 *)&Ws[o * H + k0 + 4];
+            p[o] = fmaf(x[0], wa.x, fmaf(x[1], wa.y, fmaf(x[2], wa.z, fmaf(x[3], wa.w,
+                   fmaf(x[4], wb.x, fmaf(x[5], wb.y, fmaf(x[6], wb.z, x[7] * wb.w)))))));
+        }
+#pragma unroll
+        for (int o = 0; o < NOUT; o++)
+#pragma unroll
+            for (int sh = 16; sh > 0; sh >>= 1) p[o] += __shfl_xor_sync(0xffffffffu, p[o], sh);
+        float d[NOUT];
+#pragma unroll
+        for (int o = 0; o < NOUT; o++) {
+            const float yo = p[o] + bias[o];
+            const float e = yo - t[(size_t)b * NOUT + o];
+            if (lane == 0) {
+                y[(size_t)b * NOUT + o] = yo;
+                l += (double)e * e;
+            }
+            d[o] = 2.0f * e / (float)(B * NOUT);
+            if (lane == o) dy[(size_t)b * NOUT + o] = d[o];
+            dacc[o] += d[o];
+#pragma unroll
+            for (int q = 0; q < 8; q++) acc[o][q] = fmaf(d[o], x[q], acc[o][q]);
+        }
+        const __nv_bfloat162 *g2 = (const __nv_bfloat162 *)&gv;
+        __align__(16) __nv_bfloat162 o2[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+            for (int o = 0; o < NOUT; o++) {
+                const float2 wo = *(const float2 *)&Ws[o * H + k0 + 2 * q];
+                s0 = fmaf(d[o], wo.x, s0);
+                s1 = fmaf(d[o], wo.y, s1);
+            }
+            o2[q] = __floats2bfloat162_rn(s0 * __low2float(g2[q]), s1 * __high2float(g2[q]));
+        }
+        *(uint4 *)(dz + (size_t)b * H + k0) = *(const uint4 *)o2;
+    }
+    }
+#pragma unroll
+    for (int o = 0; o < NOUT; o++) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) red[warp][o * H + k0 + q] = acc[o][q];
+        if (lane == 0) red[warp][NOUT * H + o] = dacc[o];
+    }
+    if (lane == 0) lred[warp] = l;
+    __syncthreads();
+    float *pc = part + (size_t)blockIdx.x * (NOUT * H + NOUT);
+    for (int e = threadIdx.x; e < NOUT * H + NOUT; e += blockDim.x) {
+        float s = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; k++) s += red[k][e];
+        pc[e] = s;
+    }
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < 8; k++) s += lred[k];
+        loss_part[blockIdx.x] = s;
+    }
 }
 
 // Split partials of the output layer's weight gradient: part[split][o][k] =

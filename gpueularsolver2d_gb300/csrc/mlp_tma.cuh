@@ -16,7 +16,10 @@
 //           its accumulator to the epilogue;
 //   warps 2-17 drain the other accumulator with tcgen05.ld (each warp one
 //           32-lane quarter of the rows and a quarter of the columns), apply
-//           the epilogue and store bf16 rows, while the next tile's MMAs run.
+//           the epilogue into a 32 x 32 bf16 slab of its own in shared memory
+//           (64-byte swizzle) and store the slab by TMA, while the next
+//           tile's MMAs run; the data gradient's gelu'(z) factors come into
+//           the same slabs by TMA before the accumulator is ready.
 // Every wait is bounded: a timed-out thread sets *flag and leaves its loop;
 // the producer then waits (bounded) for the copies it issued, the MMA thread
 // for the MMAs it issued, and the tensor memory is freed on every path.
@@ -33,12 +36,15 @@ namespace ws {
 constexpr int KD = 256, ND = 256, BM = 128;  // reduction, output width, rows per tile
 constexpr int KC = 64;                       // K columns per A slice: one 128-byte swizzle row of bf16
 constexpr int NSLICE = KD / KC;
-constexpr int NSLOT = 4;                     // A slices in flight
+constexpr int NSLOT = 2;                     // A slices in flight
 constexpr int SLICE_BYTES = BM * KC * 2;     // 16 KB
 constexpr int WSLICE_BYTES = ND * KC * 2;    // 32 KB
 constexpr int W_BYTES = ND * KD * 2;         // 128 KB
-constexpr int SMEM = W_BYTES + NSLOT * SLICE_BYTES + 1024;  // + slack to align the base to 1024 bytes
 constexpr int NEPI = 16;                     // epilogue warps: 4 per 32-lane quarter of tensor memory
+constexpr int SLAB = 32 * 32 * 2;            // one epilogue slab: 32 rows x 32 columns of bf16
+constexpr int SLABS_BYTES = NEPI * 2 * SLAB; // two slabs per epilogue warp
+// weights, A ring, slabs, the bias (1 KB), and slack to align the base to 1024 bytes
+constexpr int SMEM = W_BYTES + NSLOT * SLICE_BYTES + SLABS_BYTES + ND * 4 + 1024;
 constexpr int THREADS = 32 * (2 + NEPI);
 constexpr uint32_t TMEM_COLS = 512;          // two 256-column FP32 accumulators
 constexpr int WAIT_LIMIT = 1 << 22;          // try_wait calls before giving up
@@ -84,32 +90,51 @@ __device__ __forceinline__ void tma_load(uint32_t dst, const CUtensorMap *map, i
                  :: "r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar) : "memory");
 }
 
+// 2D tiled TMA store of a shared-memory box to (x, y) of the tensor map, in
+// the calling thread's bulk group.
+__device__ __forceinline__ void tma_store(const CUtensorMap *map, uint32_t src, int x, int y) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];\n"
+                 :: "l"((uint64_t)map), "r"(x), "r"(y), "r"(src) : "memory");
+}
+
+// Byte offset of 16-byte unit u (0..3) of row r in a slab of 64-byte rows
+// with the 64-byte swizzle (unit index XOR bits 1-2 of the row), the layout
+// of a TMA box of 32 bf16 columns under CU_TENSOR_MAP_SWIZZLE_64B.  A
+// quarter-warp (8 consecutive rows, same u) covers all 32 banks.
+__device__ __forceinline__ uint32_t slab_off(int r, int u) { return (uint32_t)(r * 64 + ((u ^ ((r >> 1) & 3)) << 4)); }
+
 __device__ __forceinline__ void commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" :: "r"(bar)
                  : "memory");
 }
 
+// The row-major [M][256] bf16 outputs (and the data gradient's gelu'(z)
+// input) are reached through tensor maps with 32 x 32 boxes and the 64-byte
+// swizzle: mapOut = gelu(z) (forward) or the data gradient, mapAux = gelu'(z)
+// (written by the forward, read by the data gradient).
 struct Args {
     int M;                // rows (batch), a multiple of 128
     const float *bias;    // EPI_BIAS_GELU: [256]
-    const bf16 *zin;      // EPI_GELU_BWD: [M][256]
-    bf16 *out;            // [M][256]
-    bf16 *zout;           // EPI_BIAS_GELU: [M][256] pre-activations
     int *flag;            // set to 1 when a wait gave up
 };
 
 template <int EPI>
 __global__ void __launch_bounds__(THREADS, 1)
-    k_gemm_ws(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapW, Args g) {
+    k_gemm_ws(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapW,
+              const __grid_constant__ CUtensorMap mapOut, const __grid_constant__ CUtensorMap mapAux, Args g) {
     extern __shared__ unsigned char ws_raw[];
-    __shared__ __align__(8) uint64_t full[NSLOT], empty[NSLOT], tfull[2], tempty[2], wfull, mdone;
+    __shared__ __align__(8) uint64_t full[NSLOT], empty[NSLOT], tfull[2], tempty[2], wfull, mdone, aux[NEPI];
     __shared__ uint32_t tmem_sh;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     // 1024-byte aligned base: the swizzle pattern is taken from address bits
     const uint32_t base = (smem_u32(ws_raw) + 1023u) & ~1023u;
-    const uint32_t Wsm = base, Asm = base + W_BYTES;
+    const uint32_t Wsm = base, Asm = base + W_BYTES, Ssm = Asm + NSLOT * SLICE_BYTES;
+    float *bias_s = (float *)(ws_raw + (Ssm + SLABS_BYTES - smem_u32(ws_raw)));
     const int ntiles = g.M / BM;
+    if (EPI == EPI_BIAS_GELU)
+        for (int k = tid; k < ND; k += blockDim.x) bias_s[k] = g.bias[k];
     if (tid == 0) {
+        for (int e = 0; e < NEPI; e++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&aux[e])));
         for (int s = 0; s < NSLOT; s++) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&full[s])));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&empty[s])));
@@ -184,74 +209,134 @@ __global__ void __launch_bounds__(THREADS, 1)
         wait(smem_u32(&mdone), 0);
     } else if (warp >= 2) {
         // ---- epilogue ----
-        const int quarter = warp & 3, group = (warp - 2) >> 2;  // rows 32 quarter.., columns 64 group..
+        // warp: rows 32 quarter .. of the tile (its tensor-memory lane
+        // quarter), columns 64 group .. in two 32-column halves, each through
+        // one of the warp's two slabs
+        const int quarter = warp & 3, ew = warp - 2, group = ew >> 2;
+        const uint32_t slab0 = Ssm + (uint32_t)(ew * 2 * SLAB);
+        const uint32_t abar = smem_u32(&aux[ew]);
+        bool ok = true;
         int li = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, li++) {
             const int acc = li & 1;
-            const int m = t * BM + quarter * 32 + lane;
-            // the data gradient's pre-activations of this thread's 64 columns,
-            // requested before the accumulator is ready (they do not depend on it)
-            __align__(16) uint4 zpre[8];
-            if (EPI == EPI_GELU_BWD && m < g.M) {
-                const uint4 *zi = (const uint4 *)(g.zin + (size_t)m * ND + group * 64);
-#pragma unroll
-                for (int j = 0; j < 8; j++) zpre[j] = zi[j];
+            const int row0 = t * BM + quarter * 32, col0 = group * 64;
+            if (EPI == EPI_GELU_BWD && lane == 0) {
+                // the previous tile's stores have read the slabs; then this
+                // tile's gelu'(z) factors into them (they do not depend on
+                // the accumulator)
+                asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+                expect_tx(abar, 2 * SLAB);
+                tma_load(slab0, &mapAux, col0, row0, abar);
+                tma_load(slab0 + SLAB, &mapAux, col0 + 32, row0, abar);
             }
             // one lane waits and the warp follows its answer, so that the warp
             // stays converged for the collective tensor-memory loads
             int okw = lane == 0 ? (int)wait(smem_u32(&tfull[acc]), (li >> 1) & 1) : 0;
             okw = __shfl_sync(0xffffffffu, okw, 0);
+            if (EPI == EPI_GELU_BWD) {
+                // every lane observes the copy's completion before reading the slabs
+                okw = __all_sync(0xffffffffu, okw && wait(abar, li & 1));
+            }
             if (!okw) {
-                if (lane == 0) atomicExch(g.flag, 1);
+                ok = false;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n");
 #pragma unroll
-            for (int ch = 0; ch < 4; ch++) {
-                const int n0 = group * 64 + ch * 16;
-                uint32_t v[16];
-                const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * ND + n0);
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                    "[%16];\n"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                      "=r"(v[15])
-                    : "r"(taddr));
-                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                if (m >= g.M) continue;
-                __align__(16) __nv_bfloat162 o2[8];
+            for (int half = 0; half < 2; half++) {
+                const uint32_t sl = slab0 + (uint32_t)(half * SLAB);
                 if (EPI == EPI_BIAS_GELU) {
-                    __align__(16) __nv_bfloat162 z2[8];
-                    const float4 *b4 = (const float4 *)(g.bias + n0);
-#pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        const float4 bb = b4[j];
-                        const float z0 = __uint_as_float(v[4 * j]) + bb.x, z1 = __uint_as_float(v[4 * j + 1]) + bb.y;
-                        const float z2a = __uint_as_float(v[4 * j + 2]) + bb.z, z3 = __uint_as_float(v[4 * j + 3]) + bb.w;
-                        z2[2 * j] = __floats2bfloat162_rn(z0, z1);
-                        z2[2 * j + 1] = __floats2bfloat162_rn(z2a, z3);
-                        o2[2 * j] = __floats2bfloat162_rn(gelu(z0), gelu(z1));
-                        o2[2 * j + 1] = __floats2bfloat162_rn(gelu(z2a), gelu(z3));
-                    }
-                    uint4 *zo = (uint4 *)(g.zout + (size_t)m * ND + n0);
-                    zo[0] = ((const uint4 *)z2)[0];
-                    zo[1] = ((const uint4 *)z2)[1];
-                } else {
-                    const __nv_bfloat162 *z2 = (const __nv_bfloat162 *)&zpre[2 * ch];
-#pragma unroll
-                    for (int j = 0; j < 8; j++)
-                        o2[j] = __floats2bfloat162_rn(__uint_as_float(v[2 * j]) * gelu_grad(__bfloat162float(z2[j].x)),
-                                                      __uint_as_float(v[2 * j + 1]) * gelu_grad(__bfloat162float(z2[j].y)));
+                    // the slabs are free once the stores issued from them have read them
+                    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+                    __syncwarp();
                 }
-                uint4 *oo = (uint4 *)(g.out + (size_t)m * ND + n0);
-                oo[0] = ((const uint4 *)o2)[0];
-                oo[1] = ((const uint4 *)o2)[1];
+#pragma unroll
+                for (int c = 0; c < 2; c++) {
+                    const int n0 = col0 + half * 32 + c * 16;
+                    uint32_t v[16];
+                    const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * ND + n0);
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                        "[%16];\n"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                          "=r"(v[14]), "=r"(v[15])
+                        : "r"(taddr));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                    const uint32_t o0 = slab_off(lane, 2 * c), o1 = slab_off(lane, 2 * c + 1);
+                    __align__(16) __nv_bfloat162 o2[8];
+                    if (EPI == EPI_BIAS_GELU) {
+                        // forward: gelu(z) into slab 0's half, gelu'(z) into slab 1's (one half at a time)
+                        __align__(16) __nv_bfloat162 z2[8];
+#pragma unroll
+                        for (int j = 0; j < 8; j++) {
+                            const float2 bb = *(const float2 *)&bias_s[n0 + 2 * j];
+                            const float z0 = __uint_as_float(v[2 * j]) + bb.x;
+                            const float z1 = __uint_as_float(v[2 * j + 1]) + bb.y;
+                            float h0, g0, h1, g1;
+                            gelu_and_grad(z0, h0, g0);
+                            gelu_and_grad(z1, h1, g1);
+                            o2[j] = __floats2bfloat162_rn(h0, h1);
+                            z2[j] = __floats2bfloat162_rn(g0, g1);
+                        }
+                        const uint4 *pz = (const uint4 *)z2;
+                        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" :: "r"(slab0 + SLAB + o0),
+                                     "r"(pz[0].x), "r"(pz[0].y), "r"(pz[0].z), "r"(pz[0].w) : "memory");
+                        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" :: "r"(slab0 + SLAB + o1),
+                                     "r"(pz[1].x), "r"(pz[1].y), "r"(pz[1].z), "r"(pz[1].w) : "memory");
+                        const uint4 *po = (const uint4 *)o2;
+                        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" :: "r"(slab0 + o0),
+                                     "r"(po[0].x), "r"(po[0].y), "r"(po[0].z), "r"(po[0].w) : "memory");
+                        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" :: "r"(slab0 + o1),
+                                     "r"(po[1].x), "r"(po[1].y), "r"(po[1].z), "r"(po[1].w) : "memory");
+                    } else {
+                        // data gradient: acc * gelu'(z), written over the factors it used
+                        __align__(16) uint4 zz[2];
+                        asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];\n"
+                                     : "=r"(zz[0].x), "=r"(zz[0].y), "=r"(zz[0].z), "=r"(zz[0].w) : "r"(sl + o0) : "memory");
+                        asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];\n"
+                                     : "=r"(zz[1].x), "=r"(zz[1].y), "=r"(zz[1].z), "=r"(zz[1].w) : "r"(sl + o1) : "memory");
+                        const __nv_bfloat162 *z2 = (const __nv_bfloat162 *)zz;
+#pragma unroll
+                        for (int j = 0; j < 8; j++)
+                            o2[j] = __floats2bfloat162_rn(__uint_as_float(v[2 * j]) * __low2float(z2[j]),
+                                                          __uint_as_float(v[2 * j + 1]) * __high2float(z2[j]));
+                        const uint4 *po = (const uint4 *)o2;
+                        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" :: "r"(sl + o0),
+                                     "r"(po[0].x), "r"(po[0].y), "r"(po[0].z), "r"(po[0].w) : "memory");
+                        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" :: "r"(sl + o1),
+                                     "r"(po[1].x), "r"(po[1].y), "r"(po[1].z), "r"(po[1].w) : "memory");
+                    }
+                }
+                if (half == 1) {
+                    // the accumulator has been read: the MMAs of a later tile may overwrite it
+                    asm volatile("tcgen05.fence::before_thread_sync;\n");
+                    __syncwarp();
+                    if (lane == 0) arrive(smem_u32(&tempty[acc]));
+                }
+                // the slab writes become visible to the async proxy, then one
+                // lane stores the boxes
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                __syncwarp();
+                if (lane == 0) {
+                    if (EPI == EPI_BIAS_GELU) {
+                        tma_store(&mapOut, slab0, col0 + half * 32, row0);
+                        tma_store(&mapAux, slab0 + SLAB, col0 + half * 32, row0);
+                    } else {
+                        tma_store(&mapOut, sl, col0 + half * 32, row0);
+                    }
+                    asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+                }
             }
-            asm volatile("tcgen05.fence::before_thread_sync;\n");
-            __syncwarp();
-            if (lane == 0) arrive(smem_u32(&tempty[acc]));
         }
+        if (!ok && lane == 0) {
+            atomicExch(g.flag, 1);
+            // a gelu'(z) copy may still be in flight: let it land (bounded)
+            if (EPI == EPI_GELU_BWD) wait(abar, li & 1);
+        }
+        // the stores have completed before the CTA leaves
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
+        __syncwarp();
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();

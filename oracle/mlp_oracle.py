@@ -2,7 +2,7 @@
 ONLY: the checker of the GPU training kernels; no reference counterpart).
 
 Same network as gpueularsolver2d_gb300/csrc/mlp.cu: 32 inputs -> nhidden x 256
-(GELU, erf form) -> 4 outputs, MSE loss over the batch and the 4 outputs.
+(GELU, tanh form) -> 4 outputs, MSE loss over the batch and the 4 outputs.
 Parameters in the order W0, b0, ..., W_out, b_out with W[out][in].  The GPU
 rounds weights, inputs, activations and their gradients to BF16 and
 accumulates in FP32; this restatement works in FP64 on the BF16-rounded
@@ -36,12 +36,17 @@ def unpack(p: np.ndarray, nhidden: int):
     return Ws, bs
 
 
-def _erf(x):
-    try:
-        from scipy.special import erf
-        return erf(x)
-    except ImportError:  # pragma: no cover
-        return np.vectorize(math.erf)(x)
+C0, C1 = math.sqrt(2.0 / math.pi), 0.044715
+
+
+def gelu(z):
+    """GELU, tanh form: z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))) / 2."""
+    return 0.5 * z * (1.0 + np.tanh(C0 * (z + C1 * z ** 3)))
+
+
+def gelu_grad(z):
+    t = np.tanh(C0 * (z + C1 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * C0 * (1.0 + 3.0 * C1 * z * z)
 
 
 def loss_and_grad(p: np.ndarray, x: np.ndarray, t: np.ndarray, nhidden: int):
@@ -52,7 +57,7 @@ def loss_and_grad(p: np.ndarray, x: np.ndarray, t: np.ndarray, nhidden: int):
     zs, hs = [], [h]
     for l in range(nhidden):
         z = h @ Wq[l].T + bs[l]
-        h = 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+        h = gelu(z)
         zs.append(z)
         hs.append(h)
     y = h @ Wq[nhidden].T + bs[nhidden]
@@ -66,7 +71,7 @@ def loss_and_grad(p: np.ndarray, x: np.ndarray, t: np.ndarray, nhidden: int):
     dh = dy @ Wq[nhidden]
     for l in range(nhidden - 1, -1, -1):
         z = zs[l]
-        dz = dh * (0.5 * (1.0 + _erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2 * math.pi))
+        dz = dh * gelu_grad(z)
         grads_W[l] = dz.T @ hs[l]
         grads_b[l] = dz.sum(axis=0)
         dh = dz @ Wq[l]
