@@ -61,46 +61,69 @@ struct AdamSeg {
 };
 
 // Adam on two tensors (a layer's weights and bias) in one launch: blocks
-// [0, nb0) take seg0, the rest seg1, 32 parameters per 256-thread block.
-// Warp j sums partials j, j + 8, ... of the block's parameters (lane =
-// parameter, 128-byte loads, four in flight), the eight warp sums are added
-// in a fixed tree (deterministic), and warp 0 applies the step.  lr (device,
-// read at run time so that the host can schedule it) null: gradient only.
+// [0, nb0) take seg0, the rest seg1, 128 parameters per 256-thread block
+// (every count, stride and partial offset a multiple of 4).  Lane l of warp j
+// sums parameters 4l .. 4l + 3 of the block over partials j, j + 8, ...
+// (16-byte loads, eight in flight), the eight warp sums are added in a fixed
+// tree (deterministic), and warp 0 applies the step.  lr (device, read at run
+// time so that the host can schedule it) null: gradient only.
 __global__ void __launch_bounds__(256) k_adam_seg(AdamSeg seg0, AdamSeg seg1, int nb0,
                                                   const float *__restrict__ lr_dev, float beta1, float beta2,
                                                   float eps, const float *__restrict__ bc) {
-    __shared__ float red[8][32];
+    __shared__ float4 red[8][32];
     const bool first = (int)blockIdx.x < nb0;
     const AdamSeg &S = first ? seg0 : seg1;
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    const int i = ((int)blockIdx.x - (first ? 0 : nb0)) * 32 + lane;
-    float a[4] = {0.f, 0.f, 0.f, 0.f};
+    const int i = (((int)blockIdx.x - (first ? 0 : nb0)) * 32 + lane) * 4;
+    float4 a[2] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
     if (i < S.count) {
         const float *pp = S.part + i;
-        int p = wp;
-        for (; p + 24 < S.nparts; p += 32)
+        for (int p0 = wp; p0 < S.nparts; p0 += 64) {
+            float4 v[8];
 #pragma unroll
-            for (int j = 0; j < 4; j++) a[j] += pp[(size_t)(p + 8 * j) * S.pstride];
-        if (p < S.nparts) a[0] += pp[(size_t)p * S.pstride];
-        if (p + 8 < S.nparts) a[1] += pp[(size_t)(p + 8) * S.pstride];
-        if (p + 16 < S.nparts) a[2] += pp[(size_t)(p + 16) * S.pstride];
+            for (int j = 0; j < 8; j++)
+                v[j] = p0 + 8 * j < S.nparts ? *(const float4 *)(pp + (size_t)(p0 + 8 * j) * S.pstride)
+                                             : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                float4 &t = a[j & 1];
+                t.x += v[j].x; t.y += v[j].y; t.z += v[j].z; t.w += v[j].w;
+            }
+        }
     }
-    red[wp][lane] = (a[0] + a[1]) + (a[2] + a[3]);
+    red[wp][lane] = make_float4(a[0].x + a[1].x, a[0].y + a[1].y, a[0].z + a[1].z, a[0].w + a[1].w);
     __syncthreads();
     if (wp != 0 || i >= S.count) return;
-    const float g = ((red[0][lane] + red[1][lane]) + (red[2][lane] + red[3][lane])) +
-                    ((red[4][lane] + red[5][lane]) + (red[6][lane] + red[7][lane]));
-    if (S.grad_out) S.grad_out[i] = g;
+    float g[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        float r[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) r[k] = ((const float *)&red[k][lane])[q];
+        g[q] = ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7]));
+    }
+    if (S.grad_out) *(float4 *)(S.grad_out + i) = make_float4(g[0], g[1], g[2], g[3]);
     if (!lr_dev) return;
     const float lr = *lr_dev;
-    const float mi = beta1 * S.m[i] + (1.f - beta1) * g;
-    const float vi = beta2 * S.v[i] + (1.f - beta2) * g * g;
-    S.m[i] = mi;
-    S.v[i] = vi;
-    const float w = S.w32[i] - lr * (mi / bc[0]) / (sqrtf(vi / bc[1]) + eps);
-    S.w32[i] = w;
-    if (S.wbf) S.wbf[i] = __float2bfloat16_rn(w);
-    if (S.wbfT) S.wbfT[(size_t)(i % S.cols) * S.rows + i / S.cols] = __float2bfloat16_rn(w);
+    const float4 m4 = *(const float4 *)(S.m + i), v4 = *(const float4 *)(S.v + i), w4 = *(const float4 *)(S.w32 + i);
+    float mo[4], vo[4], wo[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        mo[q] = beta1 * ((const float *)&m4)[q] + (1.f - beta1) * g[q];
+        vo[q] = beta2 * ((const float *)&v4)[q] + (1.f - beta2) * g[q] * g[q];
+        wo[q] = ((const float *)&w4)[q] - lr * (mo[q] / bc[0]) / (sqrtf(vo[q] / bc[1]) + eps);
+    }
+    *(float4 *)(S.m + i) = make_float4(mo[0], mo[1], mo[2], mo[3]);
+    *(float4 *)(S.v + i) = make_float4(vo[0], vo[1], vo[2], vo[3]);
+    *(float4 *)(S.w32 + i) = make_float4(wo[0], wo[1], wo[2], wo[3]);
+    if (S.wbf) {
+        __align__(8) __nv_bfloat162 h2[2] = {__floats2bfloat162_rn(wo[0], wo[1]), __floats2bfloat162_rn(wo[2], wo[3])};
+        *(uint2 *)(S.wbf + i) = *(const uint2 *)h2;
+    }
+    if (S.wbfT)
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            S.wbfT[(size_t)((i + q) % S.cols) * S.rows + (i + q) / S.cols] = __float2bfloat16_rn(wo[q]);
 }
 
 // bf16 copy of a [rows][cols] matrix, and (bT non-null) of its transpose
@@ -181,6 +204,8 @@ struct e2d_mlp {
     std::vector<CUtensorMap> mapHo, mapGo;  // Hh[l], Gd[l] in 32 x 32 epilogue slabs
     // dz[0] / dz[1] with 128-row boxes (data gradient), 64-row boxes (weights), 32 x 32 slabs
     CUtensorMap mapDz[2], mapDzw[2], mapDzo[2];
+    CUtensorMap mapPart;  // weight-gradient partials of the 256 x 256 layers
+    int wrows = ws::WROWS;  // batch rows per weight-gradient split
     std::vector<double> loss_host;
 
     ~e2d_mlp() {
@@ -232,6 +257,20 @@ bool map_2d(CUtensorMap *map, const bf16 *ptr, uint64_t rows, uint64_t cols, uin
                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The weight-gradient partials, FP32 [rows][256], as boxes of 32 x 32 with the
+// 128-byte swizzle (the staging layout of ws::k_wgrad_ws's epilogue).
+bool map_part(CUtensorMap *map, const float *ptr, uint64_t rows) {
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)H, rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)H * sizeof(float)};
+    const cuuint32_t box[2] = {32, 32};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)ptr, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // Tensor maps of the warp-specialised GEMMs once the batch buffers exist;
 // use_ws stays false (the per-tile kernel runs every layer) when the driver
 // entry point, a map or the shared-memory size is not available, or
@@ -254,7 +293,7 @@ int build_ws_maps(e2d_mlp *m) {
     m->mapHw.assign(m->nhidden, CUtensorMap{});
     m->mapHo.assign(m->nhidden, CUtensorMap{});
     m->mapGo.assign(m->nhidden, CUtensorMap{});
-    bool ok = m->B % ws::WROWS == 0;
+    bool ok = m->wrows >= ws::WCH && m->wrows % ws::WCH == 0 && m->B % m->wrows == 0;
     for (int l = 0; l < m->nhidden && ok; l++) {
         ok = ok && map_2d(&m->mapHo[l], m->Hh[l], m->B, H, 32, true);
         ok = ok && map_2d(&m->mapGo[l], m->Gd[l], m->B, H, 32, true);
@@ -270,6 +309,7 @@ int build_ws_maps(e2d_mlp *m) {
         ok = ok && map_2d(&m->mapDzw[k], m->dz[k], m->B, H, ws::WCH);
         ok = ok && map_2d(&m->mapDzo[k], m->dz[k], m->B, H, 32, true);
     }
+    ok = ok && map_part(&m->mapPart, m->part, (uint64_t)(m->B / m->wrows) * H);
     if (ok && cudaFuncSetAttribute(ws::k_gemm_ws<EPI_BIAS_GELU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    ws::SMEM) == cudaSuccess &&
         cudaFuncSetAttribute(ws::k_gemm_ws<EPI_GELU_BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, ws::SMEM) ==
@@ -320,8 +360,10 @@ int ensure_batch(e2d_mlp *m, int B) {
     for (int k = 0; k < 2; k++)
         if ((rc = m->alloc(&m->dz[k], sizeof(bf16) * (size_t)B * H))) return rc;
     // weight-gradient partials: kSplits of the per-tile kernel, or one per
-    // ws::WROWS rows of the batch for the warp-specialised one
-    const int nparts = std::max(kSplits, B / ws::WROWS);
+    // wrows rows of the batch for the warp-specialised one (512 rows: 128
+    // CTAs at batch 65536, 20.7 us per layer against 26.9 us for 1024 rows,
+    // with Adam summing twice the partials)
+    const int nparts = std::max(kSplits, B / m->wrows);
     if ((rc = m->alloc(&m->part, sizeof(float) * (size_t)nparts * H * H))) return rc;
     // bias / output-layer partials: the same, or one per 256 rows for the output layer
     if ((rc = m->alloc(&m->bpart, sizeof(float) * (size_t)std::max(nparts, B / 256) * (NOUT * H + NOUT + H))))
@@ -342,7 +384,7 @@ AdamSeg adam_seg(const Tensor &t, const float *part, int nparts, size_t pstride,
 // Adam on a weight tensor and its bias in one launch.
 void adam2(e2d_mlp *m, cudaStream_t s, const AdamSeg &w, const AdamSeg &b, const float *lr) {
     const auto &c = m->cfg;
-    const int nb0 = (w.count + 31) / 32, nb1 = (b.count + 31) / 32;
+    const int nb0 = (w.count + 127) / 128, nb1 = (b.count + 127) / 128;
     k_adam_seg<<<nb0 + nb1, 256, 0, s>>>(w, b, nb0, lr, (float)c.beta1, (float)c.beta2, (float)c.eps, m->bc_dev);
 }
 
@@ -422,9 +464,9 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
         // of dz
         int wparts = kSplits;
         if (l > 0 && m->use_ws) {
-            wparts = B / ws::WROWS;
-            ws::k_wgrad_ws<<<wparts, ws::WTHREADS, ws::WSMEM, s>>>(m->mapDzw[cur], m->mapHw[l], B, m->part,
-                                                                   m->bpart, m->flag_dev);
+            wparts = B / m->wrows;
+            ws::k_wgrad_ws<<<wparts, ws::WTHREADS, ws::WSMEM, s>>>(m->mapDzw[cur], m->mapHw[l], m->mapPart, B,
+                                                                   m->wrows, m->bpart, m->flag_dev);
         } else {
             GemmArgs gw{};
             gw.M = H; gw.N = kin; gw.K = B;

@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 // staged boxes (thread m: column m), the bias gradient's partial
 // bpart[split][m]; a stage is released when its MMAs and these reads are
 // done.
-constexpr int WROWS = 1024;                     // batch rows per split
+constexpr int WROWS = 512;                      // batch rows per split (a multiple of WCH)
 constexpr int WCH = 64;                         // rows per chunk
 constexpr int WBOX = 64 * WCH * 2;              // one 64 (MN) x 64 (K) box: 8 KB
 constexpr int WSTAGE = 8 * WBOX;                // dZ and H boxes of one chunk: 64 KB
@@ -378,15 +378,19 @@ __device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t addr) {
            ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 
+// The partials are written through mapPart: FP32 [splits * 256][256], boxes
+// of 32 x 32 with the 128-byte swizzle.  After the last MMA the ring is free
+// and each epilogue warp stages its 32 rows there, 128 columns at a time
+// (four boxes), for TMA stores.
 __global__ void __launch_bounds__(WTHREADS, 1)
-    k_wgrad_ws(const __grid_constant__ CUtensorMap mapDz, const __grid_constant__ CUtensorMap mapH, int M,
-               float *__restrict__ part, float *__restrict__ bpart, int *flag) {
+    k_wgrad_ws(const __grid_constant__ CUtensorMap mapDz, const __grid_constant__ CUtensorMap mapH,
+               const __grid_constant__ CUtensorMap mapPart, int M, int rows, float *__restrict__ bpart, int *flag) {
     extern __shared__ unsigned char ws_raw[];
     __shared__ __align__(8) uint64_t full[WNST], empty[WNST], tfull, mdone;
     __shared__ uint32_t tmem_sh;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t base = (smem_u32(ws_raw) + 1023u) & ~1023u;
-    const int r0 = blockIdx.x * WROWS, nch = WROWS / WCH;
+    const int r0 = blockIdx.x * rows, nch = rows / WCH;
     if (tid == 0) {
         for (int s = 0; s < WNST; s++) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&full[s])));
@@ -467,32 +471,58 @@ __global__ void __launch_bounds__(WTHREADS, 1)
             if (lane == 0) arrive(smem_u32(&empty[st]));
         }
         if (okw) bpart[(size_t)blockIdx.x * ND + e] = bsum;
+        // the ring is reused for staging below: every column-sum warp has
+        // finished reading it (named barrier 1 over the WEPI epilogue warps)
+        asm volatile("bar.sync 1, %0;\n" :: "n"(WEPI * 32) : "memory");
         // ---- epilogue: warp -> (32-lane quarter, half of the rows' M-half) ----
         const int quarter = warp & 3, h = (warp - 2) >> 2;
         if (okw) okw = lane == 0 ? (int)wait(smem_u32(&tfull), 0) : 0;
         okw = __shfl_sync(0xffffffffu, okw, 0);
         if (okw) {
             asm volatile("tcgen05.fence::after_thread_sync;\n");
-            const int m = h * BM + quarter * 32 + lane;
-            float *dst = part + ((size_t)blockIdx.x * ND + m) * ND;
+            // the ring is free: every stage has been consumed by the MMAs and
+            // the column sums; 16 KB of it per warp
+            const uint32_t stg = base + (uint32_t)((warp - 2) * 4 * 4096);
+            const int prow = blockIdx.x * ND + h * BM + quarter * 32;
 #pragma unroll 1
-            for (int ch = 0; ch < ND / 16; ch++) {
-                uint32_t v[16];
-                const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(h * ND + ch * 16);
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                    "[%16];\n"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                      "=r"(v[15])
-                    : "r"(taddr));
-                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                float4 *o = (float4 *)(dst + ch * 16);
+            for (int pass = 0; pass < 2; pass++) {
+                if (pass == 1) {
+                    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+                    __syncwarp();
+                }
+#pragma unroll 1
+                for (int ch = 0; ch < 8; ch++) {
+                    uint32_t v[16];
+                    const uint32_t taddr =
+                        tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(h * ND + pass * 128 + ch * 16);
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                        "[%16];\n"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                          "=r"(v[14]), "=r"(v[15])
+                        : "r"(taddr));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                    // box ch / 2 (32 columns), 16-byte units 4 (ch % 2) .. of row lane,
+                    // swizzled by lane % 8 (conflict-free per quarter-warp)
+                    const uint32_t bx = stg + (uint32_t)((ch >> 1) * 4096 + lane * 128);
 #pragma unroll
-                for (int j = 0; j < 4; j++)
-                    o[j] = make_float4(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1]),
-                                       __uint_as_float(v[4 * j + 2]), __uint_as_float(v[4 * j + 3]));
+                    for (int j = 0; j < 4; j++) {
+                        const int u = (ch & 1) * 4 + j;
+                        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n"
+                                     :: "r"(bx + (uint32_t)((u ^ (lane & 7)) << 4)), "r"(v[4 * j]), "r"(v[4 * j + 1]),
+                                        "r"(v[4 * j + 2]), "r"(v[4 * j + 3]) : "memory");
+                    }
+                }
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                __syncwarp();
+                if (lane == 0) {
+                    for (int j = 0; j < 4; j++) tma_store(&mapPart, stg + j * 4096, pass * 128 + j * 32, prow);
+                    asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+                }
             }
+            if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
+            __syncwarp();
         } else if (lane == 0) {
             atomicExch(flag, 1);
         }
