@@ -72,6 +72,29 @@ template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return fmax(
 template <typename T> __device__ __forceinline__ T madd(T a, T b, T c) { return a * b + c; }
 template <> __device__ __forceinline__ float madd<float>(float a, float b, float c) { return fmaf(a, b, c); }
 
+// Divisions and square roots of the stencil's hot paths: IEEE in FP64 (bit
+// parity with the oracle); in FP32 the special-function unit's approximate
+// reciprocal, reciprocal square root and square root (rcp / rsqrt /
+// sqrt.approx.f32, a few ulp), one instruction each where the IEEE forms take
+// a refinement sequence: the FP32 gather passes are issue bound.
+__device__ __forceinline__ float frcp(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float frsqrt(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float fsqrt(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+template <typename T> __device__ __forceinline__ T fdiv(T a, T b) { return a / b; }
+template <> __device__ __forceinline__ float fdiv<float>(float a, float b) { return a * frcp(b); }
+
 template <typename T> __device__ __forceinline__ T comp(const V4<T> &v, int k) {
     return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
 }
@@ -173,12 +196,12 @@ __device__ __forceinline__ T spectral_radius(const V4<T> &a, const V4<T> &b, T v
 template <>
 __device__ __forceinline__ float spectral_radius<float>(const V4<float> &a, const V4<float> &b, float vectorx,
                                                        float vectory, float g) {
-    const float rou = (a.x + b.x) * 0.5f, ir = 1.0f / rou;
+    const float rou = (a.x + b.x) * 0.5f, ir = frcp(rou);
     const float u = (a.y + b.y) * (0.5f * ir), v = (a.z + b.z) * (0.5f * ir);
     const float EE = fmaf((a.w + b.w) * 0.5f, ir, -0.5f * fmaf(u, u, v * v));
     const float VC = fmaf(u, vectory, v * vectorx);
     const float p = rou * EE * (g - 1.0f);
-    const float CS = sqrtf(g * p * ir * fmaf(vectorx, vectorx, vectory * vectory));
+    const float CS = fsqrt(g * p * ir * fmaf(vectorx, vectorx, vectory * vectory));
     return fabsf(VC) + CS;
 }
 
@@ -256,27 +279,32 @@ template <>
 __device__ __forceinline__ V4<float> roe<float>(const V4<float> &LW, const V4<float> &RW, float nx, float ny,
                                                float g, float epsilon) {
     const float gm1 = g - 1.0f;
-    const float il = 1.0f / LW.x, ir = 1.0f / RW.x;
+    // one reciprocal square root per density gives both its square root and
+    // its reciprocal
+    const float rl = frsqrt(LW.x), rr = frsqrt(RW.x);
+    const float il = rl * rl, ir = rr * rr;
     const float U0 = LW.y * il, V0 = LW.z * il, U1 = RW.y * ir, V1 = RW.z * ir;
     const float P0 = gm1 * fmaf(-0.5f * LW.x, fmaf(U0, U0, V0 * V0), LW.w);
     const float P1 = gm1 * fmaf(-0.5f * RW.x, fmaf(U1, U1, V1 * V1), RW.w);
     const float H0 = (LW.w + P0) * il, H1 = (RW.w + P1) * ir;
     const float M0 = fmaf(U0, nx, V0 * ny), M1 = fmaf(U1, nx, V1 * ny);
     const float DVC = M1 - M0;
-    const float sl = sqrtf(LW.x), sr = sqrtf(RW.x);
-    const float ROUB = sl * sr, is = 1.0f / (sl + sr);
+    const float sl = LW.x * rl, sr = RW.x * rr;
+    const float ROUB = sl * sr, is = frcp(sl + sr);
     const float UB = fmaf(U0, sl, U1 * sr) * is;
     const float VB = fmaf(V0, sl, V1 * sr) * is;
     const float HB = fmaf(H0, sl, H1 * sr) * is;
     const float QB = fmaf(UB, UB, VB * VB);
-    const float AB = sqrtf(gm1 * fmaf(-0.5f, QB, HB));
+    // c^2 of the Roe average: AB = sqrt(c^2) and 1 / AB^2 from one rsqrt
+    const float c2 = gm1 * fmaf(-0.5f, QB, HB), rc = frsqrt(c2);
+    const float AB = c2 * rc;
     const float VC = fmaf(UB, nx, VB * ny);
     const float e2 = epsilon * epsilon, ie = 0.5f / epsilon;
     const float l0 = VC - AB, l2 = VC + AB;
     const float AD0 = fabsf(l0) < epsilon ? fmaf(l0, l0, e2) * ie : fabsf(l0);
     const float AD1 = fabsf(VC) < epsilon ? fmaf(VC, VC, e2) * ie : fabsf(VC);
     const float AD2 = fabsf(l2) < epsilon ? fmaf(l2, l2, e2) * ie : fabsf(l2);
-    const float dP = P1 - P0, ia2 = 1.0f / (AB * AB), rad = ROUB * AB * DVC, h2 = 0.5f * ia2;
+    const float dP = P1 - P0, ia2 = rc * rc, rad = ROUB * AB * DVC, h2 = 0.5f * ia2;
     const float F00 = AD0 * (dP - rad) * h2;
     const float F20 = AD2 * (dP + rad) * h2;
     const float F10 = AD1 * fmaf(-dP, ia2, RW.x - LW.x);
@@ -357,10 +385,10 @@ __device__ __forceinline__ T face_limiter(const int kind, const Flow<T> &f, cons
         const T e2 = f.venk_k3 * A * tsqrt(A);
         const T d1 = delt2 > T(0) ? umax - u : umin - u;
         return delt2 == T(0) ? T(1.0)
-                             : (d1 * d1 + e2 + T(2) * delt2 * d1) / (d1 * d1 + T(2) * delt2 * delt2 + d1 * delt2 + e2);
+                             : fdiv(d1 * d1 + e2 + T(2) * delt2 * d1, d1 * d1 + T(2) * delt2 * delt2 + d1 * delt2 + e2);
     }
     const T bound = delt2 > T(0) ? umax : umin;
-    return delt2 == T(0) ? T(1.0) : tmin((bound - u) / delt2, T(1.0));
+    return delt2 == T(0) ? T(1.0) : tmin(fdiv(bound - u, delt2), T(1.0));
 }
 
 // Returns the cell's local time step (also stored in dt[i]).  OPT compiles in
@@ -404,7 +432,7 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
         Tsum += spectral_radius(U, nbv[k], S[k].y, S[k].x, f.gamma);
     }
     const T A = cell_area(m, S, i);
-    const T rA = T(1.0) / A;
+    const T rA = fdiv(T(1.0), A);
     T gx[4], gy[4], umax[4], umin[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
@@ -466,7 +494,7 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
         }
         FS[k * n + i] = o;
     }
-    const T dti = tmin(A * f.cfl / Tsum, f.dt_cap);
+    const T dti = tmin(fdiv(A * f.cfl, Tsum), f.dt_cap);
     dt[i] = dti;
     return dti;
 }
@@ -553,6 +581,21 @@ __device__ __forceinline__ void flux_cell(const MeshDev<T> &m, const Flow<T> &f,
     res[i] = r;
 }
 
+// Length vn of the face vector S and the unit normal S / vn: IEEE in FP64; in
+// FP32 from one reciprocal square root of |S|^2 (the other cell of the face,
+// with S negated, gets the exact negative).
+template <typename T> __device__ __forceinline__ void unit_normal(const V2<T> S, T &nx, T &ny, T &vn) {
+    vn = tsqrt(S.y * S.y + S.x * S.x);
+    nx = S.x / vn;
+    ny = S.y / vn;
+}
+template <> __device__ __forceinline__ void unit_normal<float>(const V2<float> S, float &nx, float &ny, float &vn) {
+    const float q = fmaf(S.y, S.y, S.x * S.x), r = frsqrt(q);
+    vn = q * r;
+    nx = S.x * r;
+    ny = S.y * r;
+}
+
 // Inputs of the Roe flux of one face in the edge's orientation: left state a,
 // right state b (the ghost across a boundary face), unit normal (nx, ny) of
 // the edge and the face length vn; *right tells whether the cell is the
@@ -561,9 +604,7 @@ template <typename T>
 __device__ __forceinline__ void face_inputs(const Flow<T> &f, const int code, const V2<T> S, const V4<T> own,
                                             const V4<T> oth, V4<T> &a, V4<T> &b, T &nx, T &ny, T &vn,
                                             bool &right) {
-    vn = tsqrt(S.y * S.y + S.x * S.x);
-    nx = S.x / vn;
-    ny = S.y / vn;
+    unit_normal(S, nx, ny, vn);
     // the left state first: both cells of a face run the same instructions on
     // the same inputs (their normals are exact negatives), so they get the
     // same bits
@@ -726,10 +767,10 @@ __device__ __forceinline__ void smooth_cell(const MeshDev<T> &m, const T eps, co
     const V4<T> r0 = res[i];
     const T den = T(1.0) + (eps) * T(tp.w);
     V4<T> o;
-    o.x = madd(d.x, eps, r0.x) / den;
-    o.y = madd(d.y, eps, r0.y) / den;
-    o.z = madd(d.z, eps, r0.z) / den;
-    o.w = madd(d.w, eps, r0.w) / den;
+    o.x = fdiv(madd(d.x, eps, r0.x), den);
+    o.y = fdiv(madd(d.y, eps, r0.y), den);
+    o.z = fdiv(madd(d.z, eps, r0.z), den);
+    o.w = fdiv(madd(d.w, eps, r0.w), den);
     dst[i] = o;
 }
 
@@ -761,8 +802,8 @@ __device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &
             const V4<T> d = nb_sum(tp, src);
             const T eps = f.irs_eps;
             const T den = T(1.0) + (eps) * T(tp.w);
-            T s0 = madd(d.x, eps, r.x) / den, s1 = madd(d.y, eps, r.y) / den;
-            T s2 = madd(d.z, eps, r.z) / den, s3 = madd(d.w, eps, r.w) / den;
+            T s0 = fdiv(madd(d.x, eps, r.x), den), s1 = fdiv(madd(d.y, eps, r.y), den);
+            T s2 = fdiv(madd(d.z, eps, r.z), den), s3 = fdiv(madd(d.w, eps, r.w), den);
             if (tabs(r.x) > tabs(s0)) r.x = s0;
             if (tabs(r.y) > tabs(s1)) r.y = s1;
             if (tabs(r.z) > tabs(s2)) r.z = s2;
@@ -773,10 +814,10 @@ __device__ __forceinline__ void update_cell(const MeshDev<T> &m, const Flow<T> &
         const T A = m.area[i];
         const V4<T> w0 = W0[i];
         V4<T> w;
-        w.x = w0.x - RK * r.x / A;
-        w.y = w0.y - RK * r.y / A;
-        w.z = w0.z - RK * r.z / A;
-        w.w = w0.w - RK * r.w / A;
+        w.x = w0.x - fdiv(RK * r.x, A);
+        w.y = w0.y - fdiv(RK * r.y, A);
+        w.z = w0.z - fdiv(RK * r.z, A);
+        w.w = w0.w - fdiv(RK * r.w, A);
         Wout[i] = w;
         if (want) {
             // rho - rho0 in the stencil's precision: exact in FP32 as long as the
