@@ -38,6 +38,22 @@ __device__ __forceinline__ void gelu_and_grad(float x, float &h, float &g) {
     g = fmaf(hx * fmaf(-t, t, 1.0f), kGeluC0 * fmaf(3.0f * kGeluC1, x2, 1.0f), fmaf(0.5f, t, 0.5f));
 }
 
+// The same for a pair of values with the packed FP32 arithmetic of this
+// architecture (two lanes of fused multiply-add per instruction).
+__device__ __forceinline__ void gelu_and_grad2(const float2 x, float2 &h, float2 &g) {
+    const float2 one = make_float2(1.0f, 1.0f), half = make_float2(0.5f, 0.5f);
+    const float2 x2 = __fmul2_rn(x, x);
+    const float2 u = __fmul2_rn(__fmul2_rn(make_float2(kGeluC0, kGeluC0), x),
+                                __ffma2_rn(make_float2(kGeluC1, kGeluC1), x2, one));
+    const float2 t = make_float2(tanh_approx(u.x), tanh_approx(u.y));
+    const float2 hx = __fmul2_rn(half, x);
+    h = __ffma2_rn(hx, t, hx);
+    const float2 sech2 = __ffma2_rn(make_float2(-t.x, -t.y), t, one);
+    const float2 du = __ffma2_rn(make_float2(3.0f * kGeluC1 * kGeluC0, 3.0f * kGeluC1 * kGeluC0), x2,
+                                 make_float2(kGeluC0, kGeluC0));
+    g = __ffma2_rn(__fmul2_rn(hx, sech2), du, __ffma2_rn(half, t, half));
+}
+
 __device__ __forceinline__ float gelu(float x) {
     const float hx = 0.5f * x;
     return fmaf(hx, tanh_approx(kGeluC0 * x * fmaf(kGeluC1, x * x, 1.0f)), hx);

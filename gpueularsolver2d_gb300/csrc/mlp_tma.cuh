@@ -271,13 +271,12 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
                         for (int j = 0; j < 8; j++) {
                             const float2 bb = *(const float2 *)&bias_s[n0 + 2 * j];
-                            const float z0 = __uint_as_float(v[2 * j]) + bb.x;
-                            const float z1 = __uint_as_float(v[2 * j + 1]) + bb.y;
-                            float h0, g0, h1, g1;
-                            gelu_and_grad(z0, h0, g0);
-                            gelu_and_grad(z1, h1, g1);
-                            o2[j] = __floats2bfloat162_rn(h0, h1);
-                            z2[j] = __floats2bfloat162_rn(g0, g1);
+                            const float2 z = __fadd2_rn(make_float2(__uint_as_float(v[2 * j]),
+                                                                    __uint_as_float(v[2 * j + 1])), bb);
+                            float2 hh, gg;
+                            gelu_and_grad2(z, hh, gg);
+                            o2[j] = __floats2bfloat162_rn(hh.x, hh.y);
+                            z2[j] = __floats2bfloat162_rn(gg.x, gg.y);
                         }
                         const uint4 *pz = (const uint4 *)z2;
                         asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" :: "r"(slab0 + SLAB + o0),
@@ -298,9 +297,12 @@ __global__ void __launch_bounds__(THREADS, 1)
                                      : "=r"(zz[1].x), "=r"(zz[1].y), "=r"(zz[1].z), "=r"(zz[1].w) : "r"(sl + o1) : "memory");
                         const __nv_bfloat162 *z2 = (const __nv_bfloat162 *)zz;
 #pragma unroll
-                        for (int j = 0; j < 8; j++)
-                            o2[j] = __floats2bfloat162_rn(__uint_as_float(v[2 * j]) * __low2float(z2[j]),
-                                                          __uint_as_float(v[2 * j + 1]) * __high2float(z2[j]));
+                        for (int j = 0; j < 8; j++) {
+                            const float2 d = __fmul2_rn(make_float2(__uint_as_float(v[2 * j]),
+                                                                    __uint_as_float(v[2 * j + 1])),
+                                                        __bfloat1622float2(z2[j]));
+                            o2[j] = __floats2bfloat162_rn(d.x, d.y);
+                        }
                         const uint4 *po = (const uint4 *)o2;
                         asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" :: "r"(sl + o0),
                                      "r"(po[0].x), "r"(po[0].y), "r"(po[0].z), "r"(po[0].w) : "memory");
