@@ -522,9 +522,8 @@ def mlp_record(layers: int, steps: int, warmup: int) -> dict:
             "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
                          "peak_source": f"{kind} bf16_tflops (MEASURED_PEAKS.json)", "traffic": None},
             # per step: step counter, gather, L forward GEMMs, the output layer,
-            # L weight gradients, L - 1 data gradients, one bias column sum
-            # (first layer), L + 1 Adam launches
-            "gpu_launches": (4 * L + 4) * steps}
+            # L weight gradients, L - 1 data gradients, L + 1 Adam launches
+            "gpu_launches": (4 * L + 3) * steps}
 
 
 def run_mlp(args):

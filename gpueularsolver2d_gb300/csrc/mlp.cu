@@ -37,6 +37,10 @@ using namespace e2d::mlp;
 namespace {
 
 constexpr int NIN = E2D_MLP_INPUTS;  // padded input width
+// Row width of the batch's inputs and of the first layer's BF16 weights on
+// the device: the inputs padded with zeros to one 64-column (128-byte) slice,
+// the first layer's K on the tensor cores.
+constexpr int KX = 64;
 constexpr int NOUT = 4;
 constexpr int H = 256;
 constexpr int kSplits = 64;          // split-K over the batch for weight gradients
@@ -47,14 +51,16 @@ __global__ void k_step_update(int *step, float beta1, float beta2, float *bc) {
     bc[1] = 1.f - powf(beta2, (float)s);
 }
 
-// One parameter tensor's Adam step: its gradient is the sum of nparts
-// partials part[p * pstride + i]; wbf (may be null) is the bf16 copy used by
+// One parameter tensor's Adam step: the gradient of element i = (r, c) is the
+// sum of nparts partials part[p * pstride + r * pld + c]; wbf (may be null,
+// row pitch wld) is the bf16 copy used by
 // the GEMMs, wbfT (may be null) its transpose ([cols][rows], the data-gradient
 // GEMM's K-major operand); grad_out (may be null) receives the gradient.
 struct AdamSeg {
     const float *part;
     size_t pstride;
     int nparts, count, rows, cols;
+    int pld, wld;  // row pitch of a partial and of wbf (elements; cols unless padded)
     float *w32, *m, *v;
     bf16 *wbf, *wbfT;
     float *grad_out;
@@ -76,8 +82,9 @@ __global__ void __launch_bounds__(256) k_adam_seg(AdamSeg seg0, AdamSeg seg1, in
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
     const int i = (((int)blockIdx.x - (first ? 0 : nb0)) * 32 + lane) * 4;
     float4 a[2] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+    const int ri = i / S.cols, ci = i % S.cols;  // cols is 1 or a multiple of 4
     if (i < S.count) {
-        const float *pp = S.part + i;
+        const float *pp = S.part + (size_t)ri * S.pld + ci;
         for (int p0 = wp; p0 < S.nparts; p0 += 64) {
             float4 v[8];
 #pragma unroll
@@ -118,7 +125,7 @@ __global__ void __launch_bounds__(256) k_adam_seg(AdamSeg seg0, AdamSeg seg1, in
     *(float4 *)(S.w32 + i) = make_float4(wo[0], wo[1], wo[2], wo[3]);
     if (S.wbf) {
         __align__(8) __nv_bfloat162 h2[2] = {__floats2bfloat162_rn(wo[0], wo[1]), __floats2bfloat162_rn(wo[2], wo[3])};
-        *(uint2 *)(S.wbf + i) = *(const uint2 *)h2;
+        *(uint2 *)(S.wbf + (size_t)ri * S.wld + ci) = *(const uint2 *)h2;
     }
     if (S.wbfT)
 #pragma unroll
@@ -126,12 +133,12 @@ __global__ void __launch_bounds__(256) k_adam_seg(AdamSeg seg0, AdamSeg seg1, in
             S.wbfT[(size_t)((i + q) % S.cols) * S.rows + (i + q) / S.cols] = __float2bfloat16_rn(wo[q]);
 }
 
-// bf16 copy of a [rows][cols] matrix, and (bT non-null) of its transpose
+// bf16 copy (row pitch ld) of a [rows][cols] matrix, and (bT non-null) of its transpose
 __global__ void k_to_bf16(int n, const float *__restrict__ a, bf16 *__restrict__ b, bf16 *__restrict__ bT, int rows,
-                          int cols) {
+                          int cols, int ld) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    b[i] = __float2bfloat16_rn(a[i]);
+    b[(size_t)(i / cols) * ld + i % cols] = __float2bfloat16_rn(a[i]);
     if (bT) bT[(size_t)(i % cols) * rows + i / cols] = __float2bfloat16_rn(a[i]);
 }
 
@@ -164,9 +171,10 @@ __global__ void __launch_bounds__(256) k_wall_distance(int n, const double *__re
 struct Tensor {
     int rows, cols;
     float *w32 = nullptr, *m = nullptr, *v = nullptr;
-    bf16 *wbf = nullptr;   // hidden layers: [rows][cols]
+    bf16 *wbf = nullptr;   // hidden layers: [rows][wld()] (the first layer padded to KX columns)
     bf16 *wbfT = nullptr;  // hidden layers after the first: [cols][rows]
     int count() const { return rows * cols; }
+    int wld() const { return cols == NIN ? KX : cols; }
 };
 
 }  // namespace
@@ -177,7 +185,7 @@ struct e2d_mlp {
     std::vector<Tensor> W, b;  // hidden layers (W: H x in, b: H x 1) then the output layer
     // batch buffers
     int B = 0;
-    bf16 *xb = nullptr;  // [B][NIN]
+    bf16 *xb = nullptr;  // [B][KX], the inputs in the first NIN columns
     float *tb = nullptr, *y = nullptr, *dy = nullptr;
     std::vector<bf16 *> Gd, Hh;  // [nhidden] of [B][H]: gelu'(z) and gelu(z) of each hidden layer
     bf16 *dz[2] = {nullptr, nullptr};  // [B][H]
@@ -204,7 +212,8 @@ struct e2d_mlp {
     std::vector<CUtensorMap> mapHo, mapGo;  // Hh[l], Gd[l] in 32 x 32 epilogue slabs
     // dz[0] / dz[1] with 128-row boxes (data gradient), 64-row boxes (weights), 32 x 32 slabs
     CUtensorMap mapDz[2], mapDzw[2], mapDzo[2];
-    CUtensorMap mapPart;  // weight-gradient partials of the 256 x 256 layers
+    CUtensorMap mapPart, mapPart0;  // weight-gradient partials: 256 x 256 layers, the first layer (256 x KX)
+    CUtensorMap mapX, mapXw, mapW0;   // the first layer's inputs (128- and 64-row boxes) and BF16 weights
     int wrows = ws::WROWS;  // batch rows per weight-gradient split
     std::vector<double> loss_host;
 
@@ -257,13 +266,13 @@ bool map_2d(CUtensorMap *map, const bf16 *ptr, uint64_t rows, uint64_t cols, uin
                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// The weight-gradient partials, FP32 [rows][256], as boxes of 32 x 32 with the
+// The weight-gradient partials, FP32 [rows][cols], as boxes of 32 x 32 with the
 // 128-byte swizzle (the staging layout of ws::k_wgrad_ws's epilogue).
-bool map_part(CUtensorMap *map, const float *ptr, uint64_t rows) {
+bool map_part(CUtensorMap *map, const float *ptr, uint64_t rows, uint64_t cols) {
     auto enc = tensor_map_encoder();
     if (!enc) return false;
-    const cuuint64_t dims[2] = {(cuuint64_t)H, rows};
-    const cuuint64_t strides[1] = {(cuuint64_t)H * sizeof(float)};
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols * sizeof(float)};
     const cuuint32_t box[2] = {32, 32};
     const cuuint32_t estr[2] = {1, 1};
     return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)ptr, dims, strides, box, estr,
@@ -279,7 +288,7 @@ int build_ws_maps(e2d_mlp *m) {
     m->use_ws = false;
     const char *env = std::getenv("E2D_MLP_WS");
     const bool required = env && env[0] == '1';
-    if ((env && env[0] == '0') || m->nhidden < 2) return E2D_OK;
+    if (env && env[0] == '0') return E2D_OK;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&m->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
@@ -309,12 +318,18 @@ int build_ws_maps(e2d_mlp *m) {
         ok = ok && map_2d(&m->mapDzw[k], m->dz[k], m->B, H, ws::WCH);
         ok = ok && map_2d(&m->mapDzo[k], m->dz[k], m->B, H, 32, true);
     }
-    ok = ok && map_part(&m->mapPart, m->part, (uint64_t)(m->B / m->wrows) * H);
-    if (ok && cudaFuncSetAttribute(ws::k_gemm_ws<EPI_BIAS_GELU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   ws::SMEM) == cudaSuccess &&
-        cudaFuncSetAttribute(ws::k_gemm_ws<EPI_GELU_BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, ws::SMEM) ==
-            cudaSuccess &&
-        cudaFuncSetAttribute(ws::k_wgrad_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, ws::WSMEM) == cudaSuccess)
+    ok = ok && map_part(&m->mapPart, m->part, (uint64_t)(m->B / m->wrows) * H, H);
+    ok = ok && map_part(&m->mapPart0, m->part, (uint64_t)(m->B / m->wrows) * H, KX);
+    ok = ok && map_2d(&m->mapX, m->xb, m->B, KX, ws::BM);
+    ok = ok && map_2d(&m->mapXw, m->xb, m->B, KX, ws::WCH);
+    ok = ok && map_2d(&m->mapW0, m->W[0].wbf, H, KX, ws::ND);
+    const auto smem_ok = [](const void *f, int bytes) {
+        return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess;
+    };
+    if (ok && smem_ok((const void *)ws::k_gemm_ws<EPI_BIAS_GELU, 4>, ws::Gemm<4>::SMEM) &&
+        smem_ok((const void *)ws::k_gemm_ws<EPI_BIAS_GELU, 1>, ws::Gemm<1>::SMEM) &&
+        smem_ok((const void *)ws::k_gemm_ws<EPI_GELU_BWD, 4>, ws::Gemm<4>::SMEM) &&
+        smem_ok((const void *)ws::k_wgrad_ws<4>, ws::WSMEM) && smem_ok((const void *)ws::k_wgrad_ws<1>, ws::WSMEM))
         m->use_ws = true;
     cudaGetLastError();
     if (required && !m->use_ws) {
@@ -324,12 +339,12 @@ int build_ws_maps(e2d_mlp *m) {
     return E2D_OK;
 }
 
-template <int EPI>
+template <int EPI, int NK>
 void gemm_ws(e2d_mlp *m, const CUtensorMap &a, const CUtensorMap &w, const CUtensorMap &out, const CUtensorMap &aux,
              ws::Args g, cudaStream_t s) {
     g.flag = m->flag_dev;
     const int ntiles = g.M / ws::BM, grid = ntiles < m->nsm ? ntiles : m->nsm;
-    ws::k_gemm_ws<EPI><<<grid, ws::THREADS, ws::SMEM, s>>>(a, w, out, aux, g);
+    ws::k_gemm_ws<EPI, NK><<<grid, ws::THREADS, ws::Gemm<NK>::SMEM, s>>>(a, w, out, aux, g);
 }
 
 size_t param_count(const e2d_mlp *m) {
@@ -347,7 +362,7 @@ int ensure_batch(e2d_mlp *m, int B) {
     }
     m->B = B;
     int rc;
-    if ((rc = m->alloc(&m->xb, sizeof(bf16) * (size_t)B * NIN))) return rc;
+    if ((rc = m->alloc(&m->xb, sizeof(bf16) * (size_t)B * KX))) return rc;  // columns NIN.. stay zero
     if ((rc = m->alloc(&m->tb, sizeof(float) * (size_t)B * NOUT))) return rc;
     if ((rc = m->alloc(&m->y, sizeof(float) * (size_t)B * NOUT))) return rc;
     if ((rc = m->alloc(&m->dy, sizeof(float) * (size_t)B * NOUT))) return rc;
@@ -372,10 +387,11 @@ int ensure_batch(e2d_mlp *m, int B) {
     return build_ws_maps(m);
 }
 
-AdamSeg adam_seg(const Tensor &t, const float *part, int nparts, size_t pstride, float *grad_out) {
+AdamSeg adam_seg(const Tensor &t, const float *part, int nparts, size_t pstride, float *grad_out, int pld = 0) {
     AdamSeg g{};
     g.part = part; g.pstride = pstride; g.nparts = nparts; g.count = t.count();
     g.rows = t.rows; g.cols = t.cols;
+    g.pld = pld ? pld : t.cols; g.wld = t.wld();
     g.w32 = t.w32; g.m = t.m; g.v = t.v; g.wbf = t.wbf; g.wbfT = t.wbfT;
     g.grad_out = grad_out;
     return g;
@@ -411,17 +427,18 @@ int check_flag(e2d_mlp *m) {
 void forward(e2d_mlp *m, cudaStream_t s, bool with_loss) {
     const int B = m->B;
     for (int l = 0; l < m->nhidden; l++) {
-        if (l > 0 && m->use_ws) {
+        if (m->use_ws) {
             ws::Args a{};
             a.M = B; a.bias = m->b[l].w32;
-            gemm_ws<EPI_BIAS_GELU>(m, m->mapHf[l], m->mapW[l], m->mapHo[l], m->mapGo[l], a, s);
+            if (l == 0) gemm_ws<EPI_BIAS_GELU, 1>(m, m->mapX, m->mapW0, m->mapHo[0], m->mapGo[0], a, s);
+            else gemm_ws<EPI_BIAS_GELU, 4>(m, m->mapHf[l], m->mapW[l], m->mapHo[l], m->mapGo[l], a, s);
             continue;
         }
         GemmArgs g{};
         g.M = B; g.N = H; g.K = l == 0 ? NIN : H;
         g.A = l == 0 ? m->xb : m->Hh[l - 1];
-        g.lda = g.K;
-        g.B = m->W[l].wbf; g.ldb = g.K;
+        g.lda = l == 0 ? KX : H;
+        g.B = m->W[l].wbf; g.ldb = m->W[l].wld();
         g.bias = m->b[l].w32; g.out = m->Hh[l]; g.zout = m->Gd[l]; g.ldc = H;
         gemm<false, false, EPI_BIAS_GELU>(m, g, dim3(H / BN, (B + BM - 1) / BM, 1), s);
     }
@@ -462,28 +479,35 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
         // dW_l = dz^T hin (split over the batch; both operands are read
         // MN-major, the batch index being their slow one), db_l = column sums
         // of dz
-        int wparts = kSplits;
-        if (l > 0 && m->use_ws) {
+        int wparts = kSplits, pld = kin;
+        if (m->use_ws) {
+            // the first layer's partials are 256 x KX (its padding columns get zero)
             wparts = B / m->wrows;
-            ws::k_wgrad_ws<<<wparts, ws::WTHREADS, ws::WSMEM, s>>>(m->mapDzw[cur], m->mapHw[l], m->mapPart, B,
-                                                                   m->wrows, m->bpart, m->flag_dev);
+            if (l == 0) {
+                pld = KX;
+                ws::k_wgrad_ws<1><<<wparts, ws::WTHREADS, ws::WSMEM, s>>>(m->mapDzw[cur], m->mapXw, m->mapPart0, B,
+                                                                          m->wrows, m->bpart, m->flag_dev);
+            } else {
+                ws::k_wgrad_ws<4><<<wparts, ws::WTHREADS, ws::WSMEM, s>>>(m->mapDzw[cur], m->mapHw[l], m->mapPart, B,
+                                                                          m->wrows, m->bpart, m->flag_dev);
+            }
         } else {
             GemmArgs gw{};
             gw.M = H; gw.N = kin; gw.K = B;
             gw.A = m->dz[cur]; gw.lda = H;
-            gw.B = l == 0 ? m->xb : m->Hh[l - 1]; gw.ldb = kin;
+            gw.B = l == 0 ? m->xb : m->Hh[l - 1]; gw.ldb = l == 0 ? KX : H;
             gw.part = m->part;
             gemm<true, true, EPI_PARTIAL>(m, gw, dim3((kin + BN - 1) / BN, H / BM, kSplits), s);
+            // (the warp-specialised weight-gradient kernel also writes the
+            // bias gradient's partials, one per split)
+            k_colsum<<<dim3(H / 32, kSplits), 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart);
         }
-        // (the warp-specialised weight-gradient kernel also writes the bias
-        // gradient's partials, one per split)
-        if (!(l > 0 && m->use_ws)) k_colsum<<<dim3(H / 32, kSplits), 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart);
         // gradient at the previous pre-activation (before this layer's weights
         // change): dz W_l, W_l read MN-major ([out][in] = [K][N])
         if (l > 0 && m->use_ws) {
             ws::Args a{};
             a.M = B;
-            gemm_ws<EPI_GELU_BWD>(m, m->mapDz[cur], m->mapWT[l], m->mapDzo[cur ^ 1], m->mapGo[l - 1], a, s);
+            gemm_ws<EPI_GELU_BWD, 4>(m, m->mapDz[cur], m->mapWT[l], m->mapDzo[cur ^ 1], m->mapGo[l - 1], a, s);
         } else if (l > 0) {
             GemmArgs gd{};
             gd.M = B; gd.N = H; gd.K = H;
@@ -494,8 +518,8 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
         }
         float *gb = gslot(m->b[l]);
         float *gW = gslot(m->W[l]);
-        adam2(m, s, adam_seg(m->W[l], m->part, wparts, (size_t)H * kin, gW), adam_seg(m->b[l], m->bpart, wparts, H, gb),
-              lr);
+        adam2(m, s, adam_seg(m->W[l], m->part, wparts, (size_t)H * pld, gW, pld),
+              adam_seg(m->b[l], m->bpart, wparts, H, gb), lr);
         cur ^= 1;
     }
 }
@@ -507,7 +531,7 @@ int build_train_graph(e2d_mlp *m) {
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     k_step_update<<<1, 1, 0, s>>>(m->step_dev, (float)m->cfg.beta1, (float)m->cfg.beta2, m->bc_dev);
     // the gather reads the step from device memory through its seed argument
-    k_gather<<<(m->B + 255) / 256, 256, 0, s>>>(m->B, NIN, NOUT, m->cfg.seed, m->step_dev, m->nsamples, m->X,
+    k_gather<<<(m->B + 255) / 256, 256, 0, s>>>(m->B, NIN, KX, NOUT, m->cfg.seed, m->step_dev, m->nsamples, m->X,
                                                   m->T, m->xb, m->tb);
     forward(m, s, true);
     backward(m, s, m->lr_dev, false);
@@ -576,14 +600,14 @@ int e2d_mlp_create(const e2d_mlp_config *cfg, e2d_mlp **out) {
             if ((rc = m->alloc(&t->w32, sizeof(float) * n))) return rc;
             if ((rc = m->alloc(&t->m, sizeof(float) * n))) return rc;
             if ((rc = m->alloc(&t->v, sizeof(float) * n))) return rc;
-            if (!last && t == &W && (rc = m->alloc(&t->wbf, sizeof(bf16) * n))) return rc;
+            if (!last && t == &W && (rc = m->alloc(&t->wbf, sizeof(bf16) * (size_t)t->rows * t->wld()))) return rc;
             if (!last && l > 0 && t == &W && (rc = m->alloc(&t->wbfT, sizeof(bf16) * n))) return rc;
         }
         CK(cudaMemcpy(W.w32, hw.data(), sizeof(float) * hw.size(), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(b.w32, hb.data(), sizeof(float) * hb.size(), cudaMemcpyHostToDevice));
         if (W.wbf)
             k_to_bf16<<<(W.count() + 255) / 256, 256, 0, m->stream>>>(W.count(), W.w32, W.wbf, W.wbfT, W.rows,
-                                                                       W.cols);
+                                                                       W.cols, W.wld());
         m->W.push_back(W);
         m->b.push_back(b);
     }
@@ -633,7 +657,7 @@ int e2d_mlp_set_params(e2d_mlp *m, const float *in) {
             CK(cudaMemcpy(t->w32, in + off, sizeof(float) * t->count(), cudaMemcpyHostToDevice));
             if (t->wbf)
                 k_to_bf16<<<(t->count() + 255) / 256, 256, 0, m->stream>>>(t->count(), t->w32, t->wbf, t->wbfT,
-                                                                            t->rows, t->cols);
+                                                                            t->rows, t->cols, t->wld());
             off += t->count();
         }
     CK(cudaStreamSynchronize(m->stream));
@@ -691,11 +715,12 @@ int e2d_mlp_forward(e2d_mlp *m, int64_t n, const float *x, float *y) {
     if (!m || !x || !y || n < 1) { set_error("bad argument"); return E2D_ERR_ARG; }
     int rc = ensure_batch(m, m->cfg.batch);
     if (rc) return rc;
-    std::vector<bf16> xb((size_t)m->B * NIN);
+    std::vector<bf16> xb((size_t)m->B * KX, __float2bfloat16_rn(0.f));
     for (int64_t r0 = 0; r0 < n; r0 += m->B) {
         const int64_t cnt = std::min<int64_t>(m->B, n - r0);
-        for (size_t i = 0; i < xb.size(); i++)
-            xb[i] = __float2bfloat16_rn(i < (size_t)cnt * NIN ? x[(size_t)r0 * NIN + i] : 0.f);
+        for (size_t r = 0; r < (size_t)m->B; r++)
+            for (int c = 0; c < NIN; c++)
+                xb[r * KX + c] = __float2bfloat16_rn(r < (size_t)cnt ? x[(size_t)(r0 + r) * NIN + c] : 0.f);
         CK(cudaMemcpyAsync(m->xb, xb.data(), sizeof(bf16) * xb.size(), cudaMemcpyHostToDevice, m->stream));
         forward(m, m->stream, false);
         CK(cudaGetLastError());
@@ -709,8 +734,9 @@ int e2d_mlp_gradient(e2d_mlp *m, const float *x, const float *t, double *loss, f
     if (!m || !x || !t || !grad) { set_error("bad argument"); return E2D_ERR_ARG; }
     int rc = ensure_batch(m, m->cfg.batch);
     if (rc) return rc;
-    std::vector<bf16> xb((size_t)m->B * NIN);
-    for (size_t i = 0; i < xb.size(); i++) xb[i] = __float2bfloat16_rn(x[i]);
+    std::vector<bf16> xb((size_t)m->B * KX, __float2bfloat16_rn(0.f));
+    for (size_t r = 0; r < (size_t)m->B; r++)
+        for (int c = 0; c < NIN; c++) xb[r * KX + c] = __float2bfloat16_rn(x[r * NIN + c]);
     CK(cudaMemcpy(m->xb, xb.data(), sizeof(bf16) * xb.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(m->tb, t, sizeof(float) * (size_t)m->B * NOUT, cudaMemcpyHostToDevice));
     forward(m, m->stream, true);

@@ -539,9 +539,10 @@ __global__ void __launch_bounds__(256) k_colsum(int B, int N, int rows_per_split
     }
 }
 
-// Random mini-batch gather: rows idx(step, j) of the training set, with the
-// step counter read from device memory (the training step is a static graph).
-__global__ void __launch_bounds__(256) k_gather(int B, int nin, int nout, unsigned long long seed,
+// Random mini-batch gather: rows idx(step, j) of the training set (nin
+// columns) into row j of xb (row pitch ldx), with the step counter read from
+// device memory (the training step is a static graph).
+__global__ void __launch_bounds__(256) k_gather(int B, int nin, int ldx, int nout, unsigned long long seed,
                                                 const int *__restrict__ stepp, long long nsamples,
                                                 const bf16 *__restrict__ X, const float *__restrict__ T,
                                                 bf16 *__restrict__ xb, float *__restrict__ tb) {
@@ -554,7 +555,7 @@ __global__ void __launch_bounds__(256) k_gather(int B, int nin, int nout, unsign
     z ^= z >> 31;
     const long long r = (long long)(z % (unsigned long long)nsamples);
     for (int k = 0; k < nin; k += 8)
-        *(uint4 *)(xb + (size_t)j * nin + k) = *(const uint4 *)(X + (size_t)r * nin + k);
+        *(uint4 *)(xb + (size_t)j * ldx + k) = *(const uint4 *)(X + (size_t)r * nin + k);
     for (int o = 0; o < nout; o++) tb[(size_t)j * nout + o] = T[(size_t)r * nout + o];
 }
 

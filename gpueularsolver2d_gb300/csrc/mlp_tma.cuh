@@ -33,18 +33,21 @@ namespace e2d {
 namespace mlp {
 namespace ws {
 
-constexpr int KD = 256, ND = 256, BM = 128;  // reduction, output width, rows per tile
+constexpr int ND = 256, BM = 128;            // output width, rows per tile
 constexpr int KC = 64;                       // K columns per A slice: one 128-byte swizzle row of bf16
-constexpr int NSLICE = KD / KC;
 constexpr int NSLOT = 2;                     // A slices in flight
 constexpr int SLICE_BYTES = BM * KC * 2;     // 16 KB
 constexpr int WSLICE_BYTES = ND * KC * 2;    // 32 KB
-constexpr int W_BYTES = ND * KD * 2;         // 128 KB
 constexpr int NEPI = 16;                     // epilogue warps: 4 per 32-lane quarter of tensor memory
 constexpr int SLAB = 32 * 32 * 2;            // one epilogue slab: 32 rows x 32 columns of bf16
 constexpr int SLABS_BYTES = NEPI * 2 * SLAB; // two slabs per epilogue warp
-// weights, A ring, slabs, the bias (1 KB), and slack to align the base to 1024 bytes
-constexpr int SMEM = W_BYTES + NSLOT * SLICE_BYTES + SLABS_BYTES + ND * 4 + 1024;
+// Shared memory of a layer with NK slices of K (K = 64 NK: 4 for the 256-wide
+// layers, 1 for the first layer's inputs padded to 64): weights, A ring,
+// slabs, the bias (1 KB), and slack to align the base to 1024 bytes.
+template <int NK> struct Gemm {
+    static constexpr int W_BYTES = NK * WSLICE_BYTES;
+    static constexpr int SMEM = W_BYTES + NSLOT * SLICE_BYTES + SLABS_BYTES + ND * 4 + 1024;
+};
 constexpr int THREADS = 32 * (2 + NEPI);
 constexpr uint32_t TMEM_COLS = 512;          // two 256-column FP32 accumulators
 constexpr int WAIT_LIMIT = 1 << 22;          // try_wait calls before giving up
@@ -118,7 +121,7 @@ struct Args {
     int *flag;            // set to 1 when a wait gave up
 };
 
-template <int EPI>
+template <int EPI, int NK>
 __global__ void __launch_bounds__(THREADS, 1)
     k_gemm_ws(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapW,
               const __grid_constant__ CUtensorMap mapOut, const __grid_constant__ CUtensorMap mapAux, Args g) {
@@ -128,6 +131,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     // 1024-byte aligned base: the swizzle pattern is taken from address bits
     const uint32_t base = (smem_u32(ws_raw) + 1023u) & ~1023u;
+    constexpr int W_BYTES = Gemm<NK>::W_BYTES, NSLICE = NK;
     const uint32_t Wsm = base, Asm = base + W_BYTES, Ssm = Asm + NSLOT * SLICE_BYTES;
     float *bias_s = (float *)(ws_raw + (Ssm + SLABS_BYTES - smem_u32(ws_raw)));
     const int ntiles = g.M / BM;
@@ -367,9 +371,6 @@ constexpr int WNST = 3;
 constexpr int WSMEM = WNST * WSTAGE + 1024;
 constexpr int WEPI = 8;
 constexpr int WTHREADS = 32 * (2 + WEPI);
-// FP32 D, BF16 A and B, both MN-major (bits 15 / 16), N = 256, M = 128
-constexpr uint32_t IDESC_MN = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
-                              ((uint32_t)(ND >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 
 // MN-major operand in the 128-byte swizzle layout: 64-element (128-byte) rows
 // along MN, one per K index; 8-row K groups 1024 bytes apart (SBO), the next
@@ -380,13 +381,22 @@ __device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t addr) {
            ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 
-// The partials are written through mapPart: FP32 [splits * 256][256], boxes
+// The partials are written through mapPart: FP32 [splits * 256][64 NH], boxes
 // of 32 x 32 with the 128-byte swizzle.  After the last MMA the ring is free
-// and each epilogue warp stages its 32 rows there, 128 columns at a time
-// (four boxes), for TMA stores.
+// and each epilogue warp stages its 32 rows there, up to 128 columns at a time
+// (four boxes), for TMA stores.  Instruction descriptor: FP32 D, BF16 A and B,
+// both MN-major (bits 15 / 16), N = 64 NH, M = 128.
+template <int NH>
 __global__ void __launch_bounds__(WTHREADS, 1)
     k_wgrad_ws(const __grid_constant__ CUtensorMap mapDz, const __grid_constant__ CUtensorMap mapH,
                const __grid_constant__ CUtensorMap mapPart, int M, int rows, float *__restrict__ bpart, int *flag) {
+    // N = 64 NH columns of H (4 boxes for a 256-wide layer, 1 for the first
+    // layer's inputs padded to 64); tensor memory: two M halves of N columns
+    constexpr int NCOL = 64 * NH, PASSES = NCOL >= 128 ? NCOL / 128 : 1, PCOLS = NCOL / PASSES;
+    constexpr uint32_t TCOLS = 2 * NCOL;
+    constexpr uint32_t IDESC_W = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
+                                 ((uint32_t)(NCOL >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+    constexpr uint32_t STAGE_TX = (4 + NH) * WBOX;
     extern __shared__ unsigned char ws_raw[];
     __shared__ __align__(8) uint64_t full[WNST], empty[WNST], tfull, mdone;
     __shared__ uint32_t tmem_sh;
@@ -405,7 +415,7 @@ __global__ void __launch_bounds__(WTHREADS, 1)
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n"
-                     :: "r"(smem_u32(&tmem_sh)), "r"(TMEM_COLS));
+                     :: "r"(smem_u32(&tmem_sh)), "r"(TCOLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n");
@@ -419,12 +429,11 @@ __global__ void __launch_bounds__(WTHREADS, 1)
         for (; c < nch && r0 + c * WCH < M; c++) {
             const int st = c % WNST;
             if (!wait(smem_u32(&empty[st]), ((c / WNST) & 1) ^ 1)) { ok = false; break; }
-            expect_tx(smem_u32(&full[st]), WSTAGE);
+            expect_tx(smem_u32(&full[st]), STAGE_TX);
             const uint32_t dst = base + st * WSTAGE;
-            for (int j = 0; j < 4; j++) {
-                tma_load(dst + j * WBOX, &mapDz, 64 * j, r0 + c * WCH, smem_u32(&full[st]));
+            for (int j = 0; j < 4; j++) tma_load(dst + j * WBOX, &mapDz, 64 * j, r0 + c * WCH, smem_u32(&full[st]));
+            for (int j = 0; j < NH; j++)
                 tma_load(dst + (4 + j) * WBOX, &mapH, 64 * j, r0 + c * WCH, smem_u32(&full[st]));
-            }
         }
         if (!ok) atomicExch(flag, 1);
         for (int k = c - WNST > 0 ? c - WNST : 0; k < c; k++) wait(smem_u32(&full[k % WNST]), (k / WNST) & 1);
@@ -445,7 +454,7 @@ __global__ void __launch_bounds__(WTHREADS, 1)
                     const uint32_t accumulate = (c > 0 || kk > 0) ? 1u : 0u;
                     asm volatile("{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
                                  " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-                                 :: "r"(tmem + (uint32_t)(h * ND)), "l"(ad), "l"(bd), "r"(IDESC_MN), "r"(accumulate));
+                                 :: "r"(tmem + (uint32_t)(h * NCOL)), "l"(ad), "l"(bd), "r"(IDESC_W), "r"(accumulate));
                 }
             commit(smem_u32(&empty[st]));
         }
@@ -487,16 +496,16 @@ __global__ void __launch_bounds__(WTHREADS, 1)
             const uint32_t stg = base + (uint32_t)((warp - 2) * 4 * 4096);
             const int prow = blockIdx.x * ND + h * BM + quarter * 32;
 #pragma unroll 1
-            for (int pass = 0; pass < 2; pass++) {
+            for (int pass = 0; pass < PASSES; pass++) {
                 if (pass == 1) {
                     if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
                     __syncwarp();
                 }
 #pragma unroll 1
-                for (int ch = 0; ch < 8; ch++) {
+                for (int ch = 0; ch < PCOLS / 16; ch++) {
                     uint32_t v[16];
                     const uint32_t taddr =
-                        tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(h * ND + pass * 128 + ch * 16);
+                        tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(h * NCOL + pass * PCOLS + ch * 16);
                     asm volatile(
                         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
                         "[%16];\n"
@@ -519,7 +528,8 @@ __global__ void __launch_bounds__(WTHREADS, 1)
                 asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
                 __syncwarp();
                 if (lane == 0) {
-                    for (int j = 0; j < 4; j++) tma_store(&mapPart, stg + j * 4096, pass * 128 + j * 32, prow);
+                    for (int j = 0; j < PCOLS / 32; j++)
+                        tma_store(&mapPart, stg + j * 4096, pass * PCOLS + j * 32, prow);
                     asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
                 }
             }
@@ -532,7 +542,7 @@ __global__ void __launch_bounds__(WTHREADS, 1)
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n");
-    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(tmem), "r"(TMEM_COLS));
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(tmem), "r"(TCOLS));
 }
 
 }  // namespace ws
