@@ -70,8 +70,10 @@ struct AdamSeg {
 // [0, nb0) take seg0, the rest seg1, 128 parameters per 256-thread block
 // (every count, stride and partial offset a multiple of 4).  Lane l of warp j
 // sums parameters 4l .. 4l + 3 of the block over partials j, j + 8, ...
-// (16-byte loads, eight in flight), the eight warp sums are added in a fixed
-// tree (deterministic), and warp 0 applies the step.  lr (device, read at run
+// (16-byte loads, sixteen in flight: one round for up to 128 partials; the
+// partials are still in L2, so the kernel is bound by the latency of its
+// rounds), the eight warp sums are added in a fixed tree (deterministic), and
+// warp 0 applies the step with its moments and weights requested up front.  lr (device, read at run
 // time so that the host can schedule it) null: gradient only.
 __global__ void __launch_bounds__(256) k_adam_seg(AdamSeg seg0, AdamSeg seg1, int nb0,
                                                   const float *__restrict__ lr_dev, float beta1, float beta2,
@@ -81,18 +83,31 @@ __global__ void __launch_bounds__(256) k_adam_seg(AdamSeg seg0, AdamSeg seg1, in
     const AdamSeg &S = first ? seg0 : seg1;
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
     const int i = (((int)blockIdx.x - (first ? 0 : nb0)) * 32 + lane) * 4;
-    float4 a[2] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
     const int ri = i / S.cols, ci = i % S.cols;  // cols is 1 or a multiple of 4
-    if (i < S.count) {
+    const bool live = i < S.count;
+    // the step's other operands are requested first: they do not depend on the sum
+    float4 m4 = make_float4(0.f, 0.f, 0.f, 0.f), v4 = m4, w4 = m4;
+    float lr = 0.f, bc0 = 1.f, bc1 = 1.f;
+    if (wp == 0 && live && lr_dev) {
+        m4 = *(const float4 *)(S.m + i);
+        v4 = *(const float4 *)(S.v + i);
+        w4 = *(const float4 *)(S.w32 + i);
+        lr = *lr_dev;
+        bc0 = bc[0];
+        bc1 = bc[1];
+    }
+    // partials wp, wp + 8, ..., sixteen 16-byte loads in flight per round
+    float4 a[2] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+    if (live) {
         const float *pp = S.part + (size_t)ri * S.pld + ci;
-        for (int p0 = wp; p0 < S.nparts; p0 += 64) {
-            float4 v[8];
+        for (int p0 = wp; p0 < S.nparts; p0 += 128) {
+            float4 v[16];
 #pragma unroll
-            for (int j = 0; j < 8; j++)
+            for (int j = 0; j < 16; j++)
                 v[j] = p0 + 8 * j < S.nparts ? *(const float4 *)(pp + (size_t)(p0 + 8 * j) * S.pstride)
                                              : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-            for (int j = 0; j < 8; j++) {
+            for (int j = 0; j < 16; j++) {
                 float4 &t = a[j & 1];
                 t.x += v[j].x; t.y += v[j].y; t.z += v[j].z; t.w += v[j].w;
             }
@@ -100,7 +115,7 @@ __global__ void __launch_bounds__(256) k_adam_seg(AdamSeg seg0, AdamSeg seg1, in
     }
     red[wp][lane] = make_float4(a[0].x + a[1].x, a[0].y + a[1].y, a[0].z + a[1].z, a[0].w + a[1].w);
     __syncthreads();
-    if (wp != 0 || i >= S.count) return;
+    if (wp != 0 || !live) return;
     float g[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
@@ -111,14 +126,12 @@ __global__ void __launch_bounds__(256) k_adam_seg(AdamSeg seg0, AdamSeg seg1, in
     }
     if (S.grad_out) *(float4 *)(S.grad_out + i) = make_float4(g[0], g[1], g[2], g[3]);
     if (!lr_dev) return;
-    const float lr = *lr_dev;
-    const float4 m4 = *(const float4 *)(S.m + i), v4 = *(const float4 *)(S.v + i), w4 = *(const float4 *)(S.w32 + i);
     float mo[4], vo[4], wo[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         mo[q] = beta1 * ((const float *)&m4)[q] + (1.f - beta1) * g[q];
         vo[q] = beta2 * ((const float *)&v4)[q] + (1.f - beta2) * g[q] * g[q];
-        wo[q] = ((const float *)&w4)[q] - lr * (mo[q] / bc[0]) / (sqrtf(vo[q] / bc[1]) + eps);
+        wo[q] = ((const float *)&w4)[q] - lr * (mo[q] / bc0) / (sqrtf(vo[q] / bc1) + eps);
     }
     *(float4 *)(S.m + i) = make_float4(mo[0], mo[1], mo[2], mo[3]);
     *(float4 *)(S.v + i) = make_float4(vo[0], vo[1], vo[2], vo[3]);
@@ -476,6 +489,22 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
     int cur = 0;
     for (int l = L - 1; l >= 0; l--) {
         const int kin = l == 0 ? NIN : H;
+        // gradient at the previous pre-activation, first (it reads W_l before
+        // this layer's Adam step changes it): dz W_l, W_l read MN-major
+        // ([out][in] = [K][N]); then the weight gradient, whose partials the
+        // Adam step reads straight after, while they are still in L2
+        if (l > 0 && m->use_ws) {
+            ws::Args a{};
+            a.M = B;
+            gemm_ws<EPI_GELU_BWD, 4>(m, m->mapDz[cur], m->mapWT[l], m->mapDzo[cur ^ 1], m->mapGo[l - 1], a, s);
+        } else if (l > 0) {
+            GemmArgs gd{};
+            gd.M = B; gd.N = H; gd.K = H;
+            gd.A = m->dz[cur]; gd.lda = H;
+            gd.B = m->W[l].wbf; gd.ldb = H;
+            gd.zin = m->Gd[l - 1]; gd.out = m->dz[cur ^ 1]; gd.ldc = H;
+            gemm<false, true, EPI_GELU_BWD>(m, gd, dim3(H / BN, (B + BM - 1) / BM, 1), s);
+        }
         // dW_l = dz^T hin (split over the batch; both operands are read
         // MN-major, the batch index being their slow one), db_l = column sums
         // of dz
@@ -501,20 +530,6 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
             // (the warp-specialised weight-gradient kernel also writes the
             // bias gradient's partials, one per split)
             k_colsum<<<dim3(H / 32, kSplits), 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart);
-        }
-        // gradient at the previous pre-activation (before this layer's weights
-        // change): dz W_l, W_l read MN-major ([out][in] = [K][N])
-        if (l > 0 && m->use_ws) {
-            ws::Args a{};
-            a.M = B;
-            gemm_ws<EPI_GELU_BWD, 4>(m, m->mapDz[cur], m->mapWT[l], m->mapDzo[cur ^ 1], m->mapGo[l - 1], a, s);
-        } else if (l > 0) {
-            GemmArgs gd{};
-            gd.M = B; gd.N = H; gd.K = H;
-            gd.A = m->dz[cur]; gd.lda = H;
-            gd.B = m->W[l].wbf; gd.ldb = H;
-            gd.zin = m->Gd[l - 1]; gd.out = m->dz[cur ^ 1]; gd.ldc = H;
-            gemm<false, true, EPI_GELU_BWD>(m, gd, dim3(H / BN, (B + BM - 1) / BM, 1), s);
         }
         float *gb = gslot(m->b[l]);
         float *gW = gslot(m->W[l]);
