@@ -50,6 +50,13 @@ template <> struct MinBlocks<float> {
     static constexpr int flux = E2D_MINB_FLUX > 0 ? E2D_MINB_FLUX : 1;
 };
 #define E2D_LB_FACES __launch_bounds__(256, MinBlocks<T>::faces)
+// The batched (persistent, tile-walking) FP32 kernels hold a few more live
+// values across their tile loop: one block fewer per SM, so that they do not
+// spill (at the single-case targets ptxas spilled 144 / 60 bytes per thread).
+template <typename T> struct BatchMinBlocks {
+    static constexpr int faces = MinBlocks<T>::faces > 2 ? MinBlocks<T>::faces - 1 : MinBlocks<T>::faces;
+    static constexpr int flux = MinBlocks<T>::flux > 2 ? MinBlocks<T>::flux - 1 : MinBlocks<T>::flux;
+};
 
 // Pass B variant.  FP64 evaluates each interior face inside a block's tile of
 // cells once (flux_tile): the FP64 Roe flux is arithmetic bound on this GPU,
@@ -917,36 +924,31 @@ __global__ void __launch_bounds__(256) k_update(MeshDev<T> m, Flow<T> f, T rk, i
 // ---------------------------------------------------------------------------
 // Batched cases: the same per-cell work as the kernels above, by persistent
 // CTAs that walk the tiles of all cases (tile = blockDim.x consecutive cells,
-// all of one case).  Cells of halted (converged) cases and padding cells are
-// skipped; each cell uses the flow constants of its own case.
-template <typename T>
-__device__ __forceinline__ bool batch_cell(const BatchDev<T> &b, const int n, const int i, int &c) {
-    if (i >= n) return false;
-    c = b.chunk_case[i / kChunk];
-    return i < b.case_end[c] && !b.ctl[c].halt;
-}
+// all of one case: cases are padded to kChunk cells and a block has at most
+// kChunk threads).  The tile's case, its halt flag and its flow constants are
+// looked up once per tile (uniform over the block); tiles of halted
+// (converged) cases and padding cells are skipped.
 
 template <typename T, bool OPT>
-__global__ void E2D_LB_FACES kb_faces(MeshDev<T> m, BatchDev<T> b, int ntiles, const V4<T> *__restrict__ W,
+__global__ void __launch_bounds__(256, BatchMinBlocks<T>::faces) kb_faces(MeshDev<T> m, BatchDev<T> b, int ntiles, const V4<T> *__restrict__ W,
                                       V4<T> *__restrict__ FS, T *__restrict__ dt, V4<T> *__restrict__ phi,
                                       const int st) {
     wait_prior_grid();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int i = t * blockDim.x + threadIdx.x;
-        const int tc = b.chunk_case[(t * blockDim.x) / kChunk];  // the tile's case
+        const int base = t * blockDim.x, i = base + threadIdx.x;
+        const int tc = b.chunk_case[base / kChunk];  // the tile's case
+        if (b.ctl[tc].halt) continue;                // uniform over the block
+        const Flow<T> f = b.flows[tc];
         double v = __longlong_as_double((long long)kDtNone);
-        int c;
-        if (batch_cell(b, m.n, i, c)) {
-            const Flow<T> f = b.flows[c];
-            v = (double)faces_cell<T, OPT>(m, f, i, W, FS, dt, phi, OPT && phi ? b.ctl[c].frozen : 0,
-                                           OPT && b.ctl[c].step < f.first_order);
-        }
-        if (OPT && b.flows[tc].global_dt) block_min_dt(v, &b.ctl[tc].dtmin[st]);  // uniform over the block
+        if (i < b.case_end[tc])
+            v = (double)faces_cell<T, OPT>(m, f, i, W, FS, dt, phi, OPT && phi ? b.ctl[tc].frozen : 0,
+                                           OPT && b.ctl[tc].step < f.first_order);
+        if (OPT && f.global_dt) block_min_dt(v, &b.ctl[tc].dtmin[st]);  // uniform over the block
     }
 }
 
 template <typename T>
-__global__ void E2D_LB_FLUX kb_flux(MeshDev<T> m, BatchDev<T> b, int ntiles, const V4<T> *__restrict__ FS,
+__global__ void __launch_bounds__(256, BatchMinBlocks<T>::flux) kb_flux(MeshDev<T> m, BatchDev<T> b, int ntiles, const V4<T> *__restrict__ FS,
                                     V4<T> *__restrict__ res) {
     wait_prior_grid();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -969,27 +971,30 @@ __global__ void __launch_bounds__(256) kb_smooth(MeshDev<T> m, BatchDev<T> b, in
                                                  V4<T> *__restrict__ dst) {
     wait_prior_grid();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int i = t * blockDim.x + threadIdx.x;
-        int c;
-        if (batch_cell(b, m.n, i, c)) smooth_cell(m, eps, i, src, res, dst);
+        const int base = t * blockDim.x, i = base + threadIdx.x;
+        const int tc = b.chunk_case[base / kChunk];
+        if (b.ctl[tc].halt) continue;
+        if (i < b.case_end[tc]) smooth_cell(m, eps, i, src, res, dst);
     }
 }
 
-template <typename T>
+// GDT: some case uses the global time-step option (read per case); without
+// it the FP32 build issues no FP64 conversion.
+template <typename T, bool GDT>
 __global__ void __launch_bounds__(256) kb_update(MeshDev<T> m, BatchDev<T> b, int ntiles, T rk, int smooth,
                                                  const V4<T> *__restrict__ src, const V4<T> *__restrict__ res,
                                                  const T *__restrict__ dt, const V4<T> *W0, V4<T> *Wout,
                                                  double *__restrict__ part, const int st) {
     wait_prior_grid();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int tc = b.chunk_case[(t * blockDim.x) / kChunk];  // the tile's case
-        if (b.ctl[tc].halt) continue;                             // uniform over the block
-        const int i = t * blockDim.x + threadIdx.x;
+        const int base = t * blockDim.x, i = base + threadIdx.x;
+        const int tc = b.chunk_case[base / kChunk];  // the tile's case
+        if (b.ctl[tc].halt) continue;                // uniform over the block
         T drho = T(0.0);
-        int bad = 0, c;
-        if (batch_cell(b, m.n, i, c)) {
-            const Flow<T> f = b.flows[c];
-            update_cell(m, f, rk, smooth, i, src, res, stage_dt(f, &b.ctl[c], st, dt, i), W0, Wout,
+        int bad = 0;
+        if (i < b.case_end[tc]) {
+            const Flow<T> f = b.flows[tc];
+            update_cell(m, f, rk, smooth, i, src, res, GDT ? stage_dt(f, &b.ctl[tc], st, dt, i) : dt[i], W0, Wout,
                         part != nullptr, drho, bad);
         }
         if (part) block_partial(drho, bad, part + t, &b.ctl[tc].nbad);
@@ -1013,8 +1018,12 @@ template <typename T> void enqueue_batch_iteration(const BPlan<T> &p, cudaStream
             launch_chained(kb_smooth<T>, G, B, s, p.m, p.b, NT, p.f.irs_eps, src, p.res, dst);
             src = dst;
         }
-        launch_chained(kb_update<T>, G, B, s, p.m, p.b, NT, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res, p.dt,
-                       p.W[0], Wout, last ? p.part : nullptr, st);
+        if (p.options)
+            launch_chained(kb_update<T, true>, G, B, s, p.m, p.b, NT, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res,
+                           p.dt, p.W[0], Wout, last ? p.part : nullptr, st);
+        else
+            launch_chained(kb_update<T, false>, G, B, s, p.m, p.b, NT, p.rk[st], p.sweeps > 0 ? 1 : 0, src, p.res,
+                           p.dt, p.W[0], Wout, last ? p.part : nullptr, st);
     }
     enqueue_batch_resid(p.part, p.case_tiles, p.ncase, p.b.ctl, p.hist, p.hist_cap, sizeof(T) == 4, s);
 }
