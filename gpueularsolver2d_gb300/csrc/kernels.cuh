@@ -403,11 +403,13 @@ __device__ __forceinline__ T face_limiter(const int kind, const Flow<T> &f, cons
 // faces, positivity fallback); without them the reference configuration runs
 // in fewer registers (no spills at the FP32 occupancy target) with the same
 // arithmetic.  first: this iteration uses first-order faces (option).
-template <typename T, bool OPT>
+// SRX: the sum of the three face spectral radii comes in as tsum_ext
+// (faces_tile evaluates each interior face's radius once per tile).
+template <typename T, bool OPT, bool SRX = false>
 __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, const int i,
                                         const V4<T> *__restrict__ W, V4<T> *__restrict__ FS,
                                         T *__restrict__ dt, V4<T> *__restrict__ phi, const int frozen,
-                                        const bool first = false) {
+                                        const bool first = false, const T tsum_ext = T(0)) {
     const int n = m.n;
     const int4 tp = m.topo[i];
     const int code[3] = {tp.x, tp.y, tp.z};
@@ -436,8 +438,9 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
             g0[q] = madd(T(0.5) * (u + c), S[k].x, g0[q]);
             g1[q] = madd(T(0.5) * (u + c), S[k].y, g1[q]);
         }
-        Tsum += spectral_radius(U, nbv[k], S[k].y, S[k].x, f.gamma);
+        if (!SRX) Tsum += spectral_radius(U, nbv[k], S[k].y, S[k].x, f.gamma);
     }
+    if (SRX) Tsum = tsum_ext;
     const T A = cell_area(m, S, i);
     const T rA = fdiv(T(1.0), A);
     T gx[4], gy[4], umax[4], umin[4];
@@ -505,6 +508,98 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
     dt[i] = dti;
     return dti;
 }
+
+// Pass A for one tile of cells [base, base + nvalid) with each interior
+// face's spectral radius evaluated once (the FP64 path, bound by the FP64
+// rate: the radius takes 4 divisions and a square root): the tile lists the
+// radii it must evaluate (boundary faces, faces to cells outside the tile,
+// and inside faces from their left cell only, as flux_tile does for the Roe
+// flux), spreads that list over its threads with the cell states in shared
+// memory, then every cell sums its three radii in face order and runs the
+// rest of faces_cell.  The radius is symmetric in its two states and in the
+// sign of the face vector, and the two cells of a face hold exactly negated
+// face vectors, so each cell gets the bits of its own evaluation.
+// blockDim.x <= 256.
+template <typename T>
+__device__ __forceinline__ void faces_tile(const MeshDev<T> &m, const Flow<T> &f, const int base, const int nvalid,
+                                           const V4<T> *__restrict__ W, V4<T> *__restrict__ FS,
+                                           T *__restrict__ dt) {
+    __shared__ V4<T> Us[256];
+    __shared__ int4 tps[256];
+    __shared__ T SRs[256 * 3];
+    __shared__ unsigned short items[256 * 3];
+    __shared__ int wtot[8];
+    const int n = m.n, t = threadIdx.x, i = base + t;
+    const bool live = t < nvalid;
+    const int4 tp = live ? m.topo[i] : make_int4(-3, -3, -3, 0);
+    tps[t] = tp;
+    if (live) Us[t] = W[i];
+    const int code[3] = {tp.x, tp.y, tp.z};
+    unsigned mask = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        if (!live) continue;
+        const int c = code[k];
+        if (c < 0) { mask |= 1u << k; continue; }
+        const bool inside = (unsigned)((c >> 3) - base) < (unsigned)nvalid;
+        if (!inside || !((c >> 2) & 1)) mask |= 1u << k;
+    }
+    // exclusive prefix sum of the per-cell counts over the block
+    const int cnt = __popc(mask), lane = t & 31, wid = t >> 5;
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) wtot[wid] = incl;
+    __syncthreads();
+    int off = incl - cnt, total = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+        if (w < wid) off += wtot[w];
+        total += wtot[w];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        if (mask & (1u << k)) items[off++] = (unsigned short)((t << 2) | k);
+    __syncthreads();
+    for (int j = t; j < total; j += blockDim.x) {
+        const int it = items[j], tt = it >> 2, k = it & 3;
+        const int4 q = tps[tt];
+        const int c = k == 0 ? q.x : k == 1 ? q.y : q.z;
+        const V4<T> Uo = Us[tt];
+        const V2<T> S = m.S[k * n + base + tt];
+        V4<T> nb;
+        if (c >= 0) {
+            const int nj = c >> 3;
+            nb = (unsigned)(nj - base) < (unsigned)nvalid ? Us[nj - base] : W[nj];
+        } else {
+            nb = ghost(c, Uo, S.x, S.y, f);
+        }
+        SRs[tt * 3 + k] = spectral_radius(Uo, nb, S.y, S.x, f.gamma);
+    }
+    __syncthreads();
+    if (!live) return;
+    T Tsum = T(0);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int c = code[k];
+        Tsum += (mask & (1u << k)) ? SRs[t * 3 + k] : SRs[((c >> 3) - base) * 3 + (c & 3)];
+    }
+    faces_cell<T, false, true>(m, f, i, W, FS, dt, nullptr, 0, false, Tsum);
+}
+
+// Pass A of the reference configuration in tiles (FP64, see faces_tile).
+template <typename T>
+__global__ void E2D_LB_FACES k_faces_tile(MeshDev<T> m, Flow<T> f, const V4<T> *__restrict__ W,
+                                          V4<T> *__restrict__ FS, T *__restrict__ dt, Ctl *__restrict__ ctl,
+                                          V4<T> *__restrict__ phi, const int st) {
+    wait_prior_grid();
+    if (ctl->halt) return;
+    const int base = blockIdx.x * blockDim.x;
+    faces_tile(m, f, base, min((int)blockDim.x, m.n - base), W, FS, dt);
+}
+template <typename T> struct FacesTiled { static constexpr bool value = sizeof(T) == 8; };
 
 // Global time-step option: the block's smallest step folded into *slot.
 // Every thread of the block must call it (v = +inf for no cell).  A time
@@ -1075,6 +1170,8 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
         if (opt) launch_chained(k_faces<T, true>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
+        else if (FacesTiled<T>::value)
+            launch_chained(k_faces_tile<T>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
         else launch_chained(k_faces<T, false>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
         if (FluxTiled<T>::value) launch_chained(k_flux_tile<T>, G, B, s, p.m, p.f, p.FS, p.res, p.ctl);
         else launch_chained(k_flux<T>, G, B, s, p.m, p.f, p.FS, p.res, p.ctl);
@@ -1110,6 +1207,7 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
         V4<T> *Wout = last ? p.W[0] : p.W[1];
         mark(0);
         if (opt) k_faces<T, true><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
+        else if (FacesTiled<T>::value) k_faces_tile<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
         else k_faces<T, false><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
         done();
         mark(1);
