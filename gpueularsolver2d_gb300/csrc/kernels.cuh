@@ -403,13 +403,30 @@ __device__ __forceinline__ T face_limiter(const int kind, const Flow<T> &f, cons
 // faces, positivity fallback); without them the reference configuration runs
 // in fewer registers (no spills at the FP32 occupancy target) with the same
 // arithmetic.  first: this iteration uses first-order faces (option).
+// |x| < |y| on the bit patterns (finite values order like their magnitudes'
+// bits; a NaN compares above every finite value)
+__device__ __forceinline__ bool abs_less(double x, double y) {
+    return (unsigned long long)(__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) <
+           (unsigned long long)(__double_as_longlong(y) & 0x7FFFFFFFFFFFFFFFLL);
+}
+
 // SRX: the sum of the three face spectral radii comes in as tsum_ext
 // (faces_tile evaluates each interior face's radius once per tile).
-template <typename T, bool OPT, bool SRX = false>
+// LDQ (FP64, reference configuration, called by every lane of the warp; live
+// false for padding lanes, which store nothing): the limiter divisions are
+// shared out over the warp.  min(1, (bound - u) / delt2) is 1 exactly when
+// |bound - u| >= |delt2| (the two have the same sign, and a correctly rounded
+// quotient of magnitude >= 1 is >= 1), so only the other slots divide: each
+// lane parks those (numerator, delt2) pairs in its row of qv (12 slots x 2),
+// the warp lists them in qi, every lane divides list entries lane, lane + 32,
+// ..., and reads its quotients back.  Same operands, same IEEE division: the
+// bits do not change; a warp divides about 2-3 times per lane instead of 12.
+template <typename T, bool OPT, bool SRX = false, bool LDQ = false>
 __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, const int i,
                                         const V4<T> *__restrict__ W, V4<T> *__restrict__ FS,
                                         T *__restrict__ dt, V4<T> *__restrict__ phi, const int frozen,
-                                        const bool first = false, const T tsum_ext = T(0)) {
+                                        const bool first = false, const T tsum_ext = T(0),
+                                        T *qv_warp = nullptr, unsigned short *qi = nullptr, const bool live = true) {
     const int n = m.n;
     const int4 tp = m.topo[i];
     const int code[3] = {tp.x, tp.y, tp.z};
@@ -471,6 +488,46 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
             }
         }
     }
+    unsigned need = 0;
+    T *qv = nullptr;
+    if constexpr (LDQ) {
+        const int lane = threadIdx.x & 31;
+        qv = qv_warp + lane * 24;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            if (code[k] < 0) continue;
+            const V2<T> r = face_offset(m, S, k, i);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int sl = 4 * k + q;
+                const T delt2 = madd(gx[q], r.x, gy[q] * r.y);
+                const T num = (delt2 > T(0) ? umax[q] : umin[q]) - comp(U, q);
+                if (live && delt2 != T(0) && abs_less(num, delt2)) {
+                    need |= 1u << sl;
+                    qv[2 * sl] = num;
+                    qv[2 * sl + 1] = delt2;
+                }
+            }
+        }
+        const int cnt = __popc(need);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        int off = incl - cnt;
+        for (unsigned mm = need; mm; mm &= mm - 1) qi[off++] = (unsigned short)((lane << 4) | (__ffs(mm) - 1));
+        __syncwarp();
+        for (int j = lane; j < total; j += 32) {
+            const int e = qi[j];
+            T *pv = qv_warp + (e >> 4) * 24 + 2 * (e & 15);
+            pv[0] = pv[0] / pv[1];
+        }
+        __syncwarp();
+        if (!live) return T(0);
+    }
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         V4<T> o = U;
@@ -485,6 +542,7 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
                 T u = comp(U, q);
                 if (reuse) fi = comp(pf, q);
                 else if (cellwise) fi = phic[q];
+                else if (LDQ) fi = (need >> (4 * k + q)) & 1 ? tmin(qv[2 * (4 * k + q)], T(1.0)) : T(1.0);
                 else fi = face_limiter(OPT ? f.limiter : 0, f, A, umax[q], umin[q], u, delt2);
                 ph[q] = fi;
                 d[q] = madd(delt2, fi, u);
@@ -519,16 +577,20 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
 // rest of faces_cell.  The radius is symmetric in its two states and in the
 // sign of the face vector, and the two cells of a face hold exactly negated
 // face vectors, so each cell gets the bits of its own evaluation.
-// blockDim.x <= 256.
+// The limiter divisions are shared out over each warp (faces_cell, LDQ).
+// blockDim.x <= kFacesTile.
+constexpr int kFacesTile = 128;
 template <typename T>
 __device__ __forceinline__ void faces_tile(const MeshDev<T> &m, const Flow<T> &f, const int base, const int nvalid,
                                            const V4<T> *__restrict__ W, V4<T> *__restrict__ FS,
                                            T *__restrict__ dt) {
-    __shared__ V4<T> Us[256];
-    __shared__ int4 tps[256];
-    __shared__ T SRs[256 * 3];
-    __shared__ unsigned short items[256 * 3];
-    __shared__ int wtot[8];
+    __shared__ V4<T> Us[kFacesTile];
+    __shared__ int4 tps[kFacesTile];
+    __shared__ T SRs[kFacesTile * 3];
+    __shared__ unsigned short items[kFacesTile * 3];
+    __shared__ int wtot[kFacesTile / 32];
+    __shared__ T qv[kFacesTile * 24];
+    __shared__ unsigned short qi[kFacesTile * 12];
     const int n = m.n, t = threadIdx.x, i = base + t;
     const bool live = t < nvalid;
     const int4 tp = live ? m.topo[i] : make_int4(-3, -3, -3, 0);
@@ -579,14 +641,20 @@ __device__ __forceinline__ void faces_tile(const MeshDev<T> &m, const Flow<T> &f
         SRs[tt * 3 + k] = spectral_radius(Uo, nb, S.y, S.x, f.gamma);
     }
     __syncthreads();
-    if (!live) return;
-    T Tsum = T(0);
+    T Tsum = T(1);
+    if (live) {
+        Tsum = T(0);
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const int c = code[k];
-        Tsum += (mask & (1u << k)) ? SRs[t * 3 + k] : SRs[((c >> 3) - base) * 3 + (c & 3)];
+        for (int k = 0; k < 3; k++) {
+            const int c = code[k];
+            Tsum += (mask & (1u << k)) ? SRs[t * 3 + k] : SRs[((c >> 3) - base) * 3 + (c & 3)];
+        }
     }
-    faces_cell<T, false, true>(m, f, i, W, FS, dt, nullptr, 0, false, Tsum);
+    // every lane of a warp takes part in the shared limiter divisions; a
+    // padding lane computes on the tile's first cell and stores nothing
+    const int w = t >> 5;
+    faces_cell<T, false, true, true>(m, f, live ? i : base, W, FS, dt, nullptr, 0, false, Tsum, qv + w * 32 * 24,
+                                     qi + w * 32 * 12, live);
 }
 
 // Pass A of the reference configuration in tiles (FP64, see faces_tile).
@@ -600,6 +668,7 @@ __global__ void E2D_LB_FACES k_faces_tile(MeshDev<T> m, Flow<T> f, const V4<T> *
     faces_tile(m, f, base, min((int)blockDim.x, m.n - base), W, FS, dt);
 }
 template <typename T> struct FacesTiled { static constexpr bool value = sizeof(T) == 8; };
+template <typename T> inline bool faces_tiled(int block) { return FacesTiled<T>::value && block <= kFacesTile; }
 
 // Global time-step option: the block's smallest step folded into *slot.
 // Every thread of the block must call it (v = +inf for no cell).  A time
@@ -1170,7 +1239,7 @@ template <typename T> void enqueue_iteration(const Plan<T> &p, cudaStream_t s) {
         V4<T> *Wcur = st == 0 ? p.W[0] : p.W[1];
         V4<T> *Wout = last ? p.W[0] : p.W[1];
         if (opt) launch_chained(k_faces<T, true>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
-        else if (FacesTiled<T>::value)
+        else if (faces_tiled<T>(B))
             launch_chained(k_faces_tile<T>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
         else launch_chained(k_faces<T, false>, G, B, s, p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
         if (FluxTiled<T>::value) launch_chained(k_flux_tile<T>, G, B, s, p.m, p.f, p.FS, p.res, p.ctl);
@@ -1207,7 +1276,7 @@ int enqueue_iteration_timed(const Plan<T> &p, cudaStream_t s, cudaEvent_t *ev, i
         V4<T> *Wout = last ? p.W[0] : p.W[1];
         mark(0);
         if (opt) k_faces<T, true><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
-        else if (FacesTiled<T>::value) k_faces_tile<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
+        else if (faces_tiled<T>(B)) k_faces_tile<T><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
         else k_faces<T, false><<<G, B, 0, s>>>(p.m, p.f, Wcur, p.FS, p.dt, p.ctl, p.phi, st);
         done();
         mark(1);
