@@ -50,6 +50,19 @@ def test_fp64_bit_exact_vs_oracle(lib, oracle, kw):
     np.testing.assert_allclose(hist, r_ref, rtol=1e-12, atol=0)
 
 
+@pytest.mark.parametrize("ordering", [e2d.E2D_ORDER_FILE, e2d.E2D_ORDER_MORTON])
+def test_fp64_bit_exact_partial_tile(lib, oracle, ordering):
+    """A mesh whose cell count is not a multiple of the 128-cell tile (50 x 13
+    O-grid: 1300 cells, the last tile 20 cells): the FP64 passes that work in
+    tiles (pass A's once-per-face spectral radii and warp-shared limiter
+    divisions, pass B's once-per-face Roe fluxes) run padding lanes there."""
+    mesh = e2d.Mesh.ogrid(50, 13, seed=4)
+    s, c, r_ref = run_pair(mesh, oracle, 30, ma=0.75, alpha_deg=2.0, cfl=1.5, ordering=ordering)
+    assert mesh.info().ncell % 128 != 0
+    assert np.array_equal(s.state(), c.state()), np.max(np.abs(s.state() - c.state()))
+    np.testing.assert_allclose(s.history(), r_ref, rtol=1e-12, atol=0)
+
+
 def test_fp64_bit_exact_128x32_morton(lib, oracle):
     mesh = e2d.Mesh.ogrid(128, 32, seed=1)
     s, c, r_ref = run_pair(mesh, oracle, 40, ma=0.5, alpha_deg=1.25, cfl=2.0,
