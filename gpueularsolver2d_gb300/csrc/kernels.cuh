@@ -286,17 +286,25 @@ template <>
 __device__ __forceinline__ V4<float> roe<float>(const V4<float> &LW, const V4<float> &RW, float nx, float ny,
                                                float g, float epsilon) {
     const float gm1 = g - 1.0f;
-    // one reciprocal square root per density gives both its square root and
-    // its reciprocal
-    const float rl = frsqrt(LW.x), rr = frsqrt(RW.x);
-    const float il = rl * rl, ir = rr * rr;
-    const float U0 = LW.y * il, V0 = LW.z * il, U1 = RW.y * ir, V1 = RW.z * ir;
-    const float P0 = gm1 * fmaf(-0.5f * LW.x, fmaf(U0, U0, V0 * V0), LW.w);
-    const float P1 = gm1 * fmaf(-0.5f * RW.x, fmaf(U1, U1, V1 * V1), RW.w);
-    const float H0 = (LW.w + P0) * il, H1 = (RW.w + P1) * ir;
-    const float M0 = fmaf(U0, nx, V0 * ny), M1 = fmaf(U1, nx, V1 * ny);
+    // The left / right quantities as pairs on the packed FP32 units (two
+    // lanes per instruction, each with the scalar form's operation order, so
+    // the bits are those of the scalar expressions); one reciprocal square
+    // root per density gives both its square root and its reciprocal.
+    const float2 rho = make_float2(LW.x, RW.x), en = make_float2(LW.w, RW.w);
+    const float2 rs = make_float2(frsqrt(LW.x), frsqrt(RW.x));
+    const float2 iv = __fmul2_rn(rs, rs);
+    const float2 Up = __fmul2_rn(make_float2(LW.y, RW.y), iv), Vp = __fmul2_rn(make_float2(LW.z, RW.z), iv);
+    const float2 Pp = __fmul2_rn(make_float2(gm1, gm1),
+                                 __ffma2_rn(__fmul2_rn(make_float2(-0.5f, -0.5f), rho),
+                                            __ffma2_rn(Up, Up, __fmul2_rn(Vp, Vp)), en));
+    const float2 Hp = __fmul2_rn(__fadd2_rn(en, Pp), iv);
+    const float2 nx2 = make_float2(nx, nx), ny2 = make_float2(ny, ny);
+    const float2 Mp = __ffma2_rn(Up, nx2, __fmul2_rn(Vp, ny2));
+    const float2 sp = __fmul2_rn(rho, rs);
+    const float U0 = Up.x, U1 = Up.y, V0 = Vp.x, V1 = Vp.y, P0 = Pp.x, P1 = Pp.y, H0 = Hp.x, H1 = Hp.y;
+    const float M0 = Mp.x, M1 = Mp.y;
     const float DVC = M1 - M0;
-    const float sl = LW.x * rl, sr = RW.x * rr;
+    const float sl = sp.x, sr = sp.y;
     const float ROUB = sl * sr, is = frcp(sl + sr);
     const float UB = fmaf(U0, sl, U1 * sr) * is;
     const float VB = fmaf(V0, sl, V1 * sr) * is;
@@ -322,10 +330,11 @@ __device__ __forceinline__ V4<float> roe<float>(const V4<float> &LW, const V4<fl
     const float F11 = fmaf(F10, UB, aR * fmaf(-DVC, nx, du));
     const float F12 = fmaf(F10, VB, aR * fmaf(-DVC, ny, dv));
     const float F13 = fmaf(F10 * 0.5f, QB, aR * fmaf(UB, du, fmaf(VB, dv, -DVC * VC)));
-    const float WL0 = LW.x * M0, WR0 = RW.x * M1;
-    const float WL1 = fmaf(U0, WL0, nx * P0), WR1 = fmaf(U1, WR0, nx * P1);
-    const float WL2 = fmaf(V0, WL0, ny * P0), WR2 = fmaf(V1, WR0, ny * P1);
-    const float WL3 = WL0 * H0, WR3 = WR0 * H1;
+    const float2 W0 = __fmul2_rn(rho, Mp);
+    const float2 W1 = __ffma2_rn(Up, W0, __fmul2_rn(nx2, Pp));
+    const float2 W2 = __ffma2_rn(Vp, W0, __fmul2_rn(ny2, Pp));
+    const float2 W3 = __fmul2_rn(W0, Hp);
+    const float WL0 = W0.x, WR0 = W0.y, WL1 = W1.x, WR1 = W1.y, WL2 = W2.x, WR2 = W2.y, WL3 = W3.x, WR3 = W3.y;
     V4<float> F;
     F.x = 0.5f * ((WL0 + WR0) - (F00 + F10 + F20));
     F.y = 0.5f * ((WL1 + WR1) - (F01 + F11 + F21));
