@@ -315,18 +315,23 @@ __device__ __forceinline__ V4<float> roe<float>(const V4<float> &LW, const V4<fl
     const float AB = c2 * rc;
     const float VC = fmaf(UB, nx, VB * ny);
     const float e2 = epsilon * epsilon, ie = 0.5f / epsilon;
-    const float l0 = VC - AB, l2 = VC + AB;
-    const float AD0 = fabsf(l0) < epsilon ? fmaf(l0, l0, e2) * ie : fabsf(l0);
+    // the two acoustic waves (eigenvalues VC -+ AB) as a pair
+    const float2 abs2 = make_float2(-AB, AB);
+    const float2 lp = __fadd2_rn(make_float2(VC, VC), abs2);  // (VC - AB, VC + AB)
+    const float2 lh = __fmul2_rn(__ffma2_rn(lp, lp, make_float2(e2, e2)), make_float2(ie, ie));
+    const float AD0 = fabsf(lp.x) < epsilon ? lh.x : fabsf(lp.x);
     const float AD1 = fabsf(VC) < epsilon ? fmaf(VC, VC, e2) * ie : fabsf(VC);
-    const float AD2 = fabsf(l2) < epsilon ? fmaf(l2, l2, e2) * ie : fabsf(l2);
+    const float AD2 = fabsf(lp.y) < epsilon ? lh.y : fabsf(lp.y);
     const float dP = P1 - P0, ia2 = rc * rc, rad = ROUB * AB * DVC, h2 = 0.5f * ia2;
-    const float F00 = AD0 * (dP - rad) * h2;
-    const float F20 = AD2 * (dP + rad) * h2;
+    const float2 FA = __fmul2_rn(__fmul2_rn(make_float2(AD0, AD2), __fadd2_rn(make_float2(dP, dP), make_float2(-rad, rad))),
+                                 make_float2(h2, h2));  // (F00, F20)
+    const float F00 = FA.x, F20 = FA.y;
     const float F10 = AD1 * fmaf(-dP, ia2, RW.x - LW.x);
     const float du = U1 - U0, dv = V1 - V0, aR = AD1 * ROUB;
-    const float F01 = F00 * fmaf(-AB, nx, UB), F21 = F20 * fmaf(AB, nx, UB);
-    const float F02 = F00 * fmaf(-AB, ny, VB), F22 = F20 * fmaf(AB, ny, VB);
-    const float F03 = F00 * fmaf(-AB, VC, HB), F23 = F20 * fmaf(AB, VC, HB);
+    const float2 Fk1 = __fmul2_rn(FA, __ffma2_rn(abs2, nx2, make_float2(UB, UB)));  // (F01, F21)
+    const float2 Fk2 = __fmul2_rn(FA, __ffma2_rn(abs2, ny2, make_float2(VB, VB)));  // (F02, F22)
+    const float2 Fk3 = __fmul2_rn(FA, __ffma2_rn(abs2, make_float2(VC, VC), make_float2(HB, HB)));  // (F03, F23)
+    const float F01 = Fk1.x, F21 = Fk1.y, F02 = Fk2.x, F22 = Fk2.y, F03 = Fk3.x, F23 = Fk3.y;
     const float F11 = fmaf(F10, UB, aR * fmaf(-DVC, nx, du));
     const float F12 = fmaf(F10, VB, aR * fmaf(-DVC, ny, dv));
     const float F13 = fmaf(F10 * 0.5f, QB, aR * fmaf(UB, du, fmaf(VB, dv, -DVC * VC)));
@@ -755,8 +760,17 @@ __device__ __forceinline__ void flux_cell(const MeshDev<T> &m, const Flow<T> &f,
     for (int k = 0; k < 3; k++) {
         bool right;
         const V4<T> F = face_flux_of(f, code[k], S[k], own[k], oth[k], right);
-        if (right) { r.x -= F.x; r.y -= F.y; r.z -= F.z; r.w -= F.w; }
-        else { r.x += F.x; r.y += F.y; r.z += F.z; r.w += F.w; }
+        if constexpr (sizeof(T) == 4) {
+            // r +- F as r + (+-1) F: the product is exact, one rounding, the
+            // same bits as the add or subtract; two packed instructions
+            const float sg = right ? -1.0f : 1.0f;
+            const float2 xy = __ffma2_rn(make_float2(F.x, F.y), make_float2(sg, sg), make_float2(r.x, r.y));
+            const float2 zw = __ffma2_rn(make_float2(F.z, F.w), make_float2(sg, sg), make_float2(r.z, r.w));
+            r.x = xy.x; r.y = xy.y; r.z = zw.x; r.w = zw.y;
+        } else {
+            if (right) { r.x -= F.x; r.y -= F.y; r.z -= F.z; r.w -= F.w; }
+            else { r.x += F.x; r.y += F.y; r.z += F.z; r.w += F.w; }
+        }
     }
     res[i] = r;
 }
@@ -810,7 +824,14 @@ __device__ __forceinline__ V4<T> face_flux_of(const Flow<T> &f, const int code, 
     face_inputs(f, code, S, own, oth, a, b, nx, ny, vn, right);
     // one Roe call site for every face
     V4<T> F = roe(a, b, nx, ny, f.gamma, f.eps_entropy);
-    F.x *= vn; F.y *= vn; F.z *= vn; F.w *= vn;
+    if constexpr (sizeof(T) == 4) {
+        // two packed multiplies, the same products
+        const float2 xy = __fmul2_rn(make_float2(F.x, F.y), make_float2(vn, vn));
+        const float2 zw = __fmul2_rn(make_float2(F.z, F.w), make_float2(vn, vn));
+        F.x = xy.x; F.y = xy.y; F.z = zw.x; F.w = zw.y;
+    } else {
+        F.x *= vn; F.y *= vn; F.z *= vn; F.w *= vn;
+    }
     return F;
 }
 
