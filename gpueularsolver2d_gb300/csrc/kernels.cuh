@@ -203,9 +203,11 @@ __device__ __forceinline__ T spectral_radius(const V4<T> &a, const V4<T> &b, T v
 template <>
 __device__ __forceinline__ float spectral_radius<float>(const V4<float> &a, const V4<float> &b, float vectorx,
                                                        float vectory, float g) {
-    const float rou = (a.x + b.x) * 0.5f, ir = frcp(rou);
-    const float u = (a.y + b.y) * (0.5f * ir), v = (a.z + b.z) * (0.5f * ir);
-    const float EE = fmaf((a.w + b.w) * 0.5f, ir, -0.5f * fmaf(u, u, v * v));
+    const float2 s01 = __fadd2_rn(make_float2(a.x, a.y), make_float2(b.x, b.y));
+    const float2 s23 = __fadd2_rn(make_float2(a.z, a.w), make_float2(b.z, b.w));
+    const float rou = s01.x * 0.5f, ir = frcp(rou);
+    const float u = s01.y * (0.5f * ir), v = s23.x * (0.5f * ir);
+    const float EE = fmaf(s23.y * 0.5f, ir, -0.5f * fmaf(u, u, v * v));
     const float VC = fmaf(u, vectory, v * vectorx);
     const float p = rou * EE * (g - 1.0f);
     const float CS = fsqrt(g * p * ir * fmaf(vectorx, vectorx, vectory * vectory));
@@ -417,6 +419,89 @@ __device__ __forceinline__ T face_limiter(const int kind, const Flow<T> &f, cons
 // faces, positivity fallback); without them the reference configuration runs
 // in fewer registers (no spills at the FP32 occupancy target) with the same
 // arithmetic.  first: this iteration uses first-order faces (option).
+// FP32, reference configuration: the arithmetic of faces_cell with the
+// component pairs (rho, rho u) and (rho v, rho E) on the packed FP32 units
+// (two lanes per instruction, each with the scalar operation order, so the
+// bits are those of the scalar form): the gradient sums, the gradients, the
+// reconstruction differences, the limiter quotients and the face states.
+__device__ __forceinline__ float faces_cell_ref32(const MeshDev<float> &m, const Flow<float> &f, const int i,
+                                                  const V4<float> *__restrict__ W, V4<float> *__restrict__ FS,
+                                                  float *__restrict__ dt) {
+    const int n = m.n;
+    const int4 tp = m.topo[i];
+    const int code[3] = {tp.x, tp.y, tp.z};
+    const V4<float> U = W[i];
+    V2<float> S[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) S[k] = m.S[k * n + i];
+    V4<float> nbv[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        nbv[k] = code[k] >= 0 ? W[code[k] >> 3] : ghost(code[k], U, S[k].x, S[k].y, f);
+    const float2 U01 = make_float2(U.x, U.y), U23 = make_float2(U.z, U.w), half = make_float2(0.5f, 0.5f);
+    float2 g0a = make_float2(0.f, 0.f), g0b = g0a, g1a = g0a, g1b = g0a;
+    float jmax[4], jmin[4];
+    float Tsum = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float c = comp(nbv[k], q);
+            if (k == 0) { jmax[q] = c; jmin[q] = c; }
+            else {
+                if (c < jmin[q]) jmin[q] = c;
+                if (c > jmax[q]) jmax[q] = c;
+            }
+        }
+        const float2 ha = __fmul2_rn(half, __fadd2_rn(U01, make_float2(nbv[k].x, nbv[k].y)));
+        const float2 hb = __fmul2_rn(half, __fadd2_rn(U23, make_float2(nbv[k].z, nbv[k].w)));
+        const float2 sx = make_float2(S[k].x, S[k].x), sy = make_float2(S[k].y, S[k].y);
+        g0a = __ffma2_rn(ha, sx, g0a);
+        g0b = __ffma2_rn(hb, sx, g0b);
+        g1a = __ffma2_rn(ha, sy, g1a);
+        g1b = __ffma2_rn(hb, sy, g1b);
+        Tsum += spectral_radius(U, nbv[k], S[k].y, S[k].x, f.gamma);
+    }
+    const float A = cell_area(m, S, i);
+    const float rA = fdiv(1.0f, A);
+    const float2 rA2 = make_float2(rA, rA);
+    const float2 gxa = __fmul2_rn(g0a, rA2), gxb = __fmul2_rn(g0b, rA2);
+    const float2 gya = __fmul2_rn(g1a, rA2), gyb = __fmul2_rn(g1b, rA2);
+    float umax[4], umin[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        umax[q] = tmax(comp(U, q), jmax[q]);
+        umin[q] = tmin(comp(U, q), jmin[q]);
+    }
+    const float2 mone = make_float2(-1.0f, -1.0f);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        V4<float> o = U;
+        if (code[k] >= 0) {
+            const V2<float> r = face_offset(m, S, k, i);
+            const float2 rx = make_float2(r.x, r.x), ry = make_float2(r.y, r.y);
+            const float2 da = __ffma2_rn(gxa, rx, __fmul2_rn(gya, ry));  // delt2 of components 0, 1
+            const float2 db = __ffma2_rn(gxb, rx, __fmul2_rn(gyb, ry));  // and 2, 3
+            // limiter (kind 0): min(1, (bound - u) / delt2), bound - u as
+            // u * (-1) + bound (one rounding, the same bits)
+            const float2 na = __ffma2_rn(U01, mone, make_float2(da.x > 0.f ? umax[0] : umin[0],
+                                                                  da.y > 0.f ? umax[1] : umin[1]));
+            const float2 nb = __ffma2_rn(U23, mone, make_float2(db.x > 0.f ? umax[2] : umin[2],
+                                                                  db.y > 0.f ? umax[3] : umin[3]));
+            const float2 qa = __fmul2_rn(na, make_float2(frcp(da.x), frcp(da.y)));
+            const float2 qb = __fmul2_rn(nb, make_float2(frcp(db.x), frcp(db.y)));
+            const float2 fa = make_float2(da.x == 0.f ? 1.0f : tmin(qa.x, 1.0f), da.y == 0.f ? 1.0f : tmin(qa.y, 1.0f));
+            const float2 fb = make_float2(db.x == 0.f ? 1.0f : tmin(qb.x, 1.0f), db.y == 0.f ? 1.0f : tmin(qb.y, 1.0f));
+            const float2 wa = __ffma2_rn(da, fa, U01), wb = __ffma2_rn(db, fb, U23);
+            o.x = wa.x; o.y = wa.y; o.z = wb.x; o.w = wb.y;
+        }
+        FS[k * n + i] = o;
+    }
+    const float dti = tmin(fdiv(A * f.cfl, Tsum), f.dt_cap);
+    dt[i] = dti;
+    return dti;
+}
+
 // |x| < |y| on the bit patterns (finite values order like their magnitudes'
 // bits; a NaN compares above every finite value)
 __device__ __forceinline__ bool abs_less(double x, double y) {
@@ -441,6 +526,7 @@ __device__ __forceinline__ T faces_cell(const MeshDev<T> &m, const Flow<T> &f, c
                                         T *__restrict__ dt, V4<T> *__restrict__ phi, const int frozen,
                                         const bool first = false, const T tsum_ext = T(0),
                                         T *qv_warp = nullptr, unsigned short *qi = nullptr, const bool live = true) {
+    if constexpr (sizeof(T) == 4 && !OPT && !SRX && !LDQ) return faces_cell_ref32(m, f, i, W, FS, dt);
     const int n = m.n;
     const int4 tp = m.topo[i];
     const int code[3] = {tp.x, tp.y, tp.z};
