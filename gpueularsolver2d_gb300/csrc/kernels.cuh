@@ -872,8 +872,9 @@ template <typename T> __device__ __forceinline__ void unit_normal(const V2<T> S,
 template <> __device__ __forceinline__ void unit_normal<float>(const V2<float> S, float &nx, float &ny, float &vn) {
     const float q = fmaf(S.y, S.y, S.x * S.x), r = frsqrt(q);
     vn = q * r;
-    nx = S.x * r;
-    ny = S.y * r;
+    const float2 nn = __fmul2_rn(make_float2(S.x, S.y), make_float2(r, r));
+    nx = nn.x;
+    ny = nn.y;
 }
 
 // Inputs of the Roe flux of one face in the edge's orientation: left state a,
