@@ -1,14 +1,16 @@
-// mlp_tma.cuh -- the 256 x 256 hidden-layer GEMMs of the warm-start MLP (the
-// forward pass with bias + GELU, and the data gradient with GELU') as one
-// persistent, warp-specialised kernel per layer.  No reference counterpart.
+// mlp_tma.cuh -- the hidden-layer GEMMs of the warm-start MLP (the forward
+// pass with bias + GELU, the data gradient with GELU', and the weight
+// gradient with the bias sums) as persistent, warp-specialised kernels, one
+// launch per layer.  No reference counterpart.
 //
-//   C[B x 256] = A[B x 256] . Wt^T,  A and Wt both K-major (row-major, the
-//   reduction index contiguous): Wt = W (forward) or W^T (data gradient).
+//   C[B x 256] = A[B x K] . Wt^T,  A and Wt both K-major (row-major, the
+//   reduction index contiguous): Wt = W (forward) or W^T (data gradient);
+//   K = 256, or 64 for the first layer (its inputs padded to one slice).
 //
 // One CTA per SM walks 128-row tiles of the batch:
-//   warp 0  (one thread) loads the 256 x 256 weights once and streams each
-//           tile's A in four 128 x 64 slices by TMA (cp.async.bulk.tensor,
-//           128-byte swizzle) into a four-slot ring;
+//   warp 0  (one thread) loads the 256 x K weights once and streams each
+//           tile's A in 128 x 64 slices by TMA (cp.async.bulk.tensor,
+//           128-byte swizzle) into a two-slot ring;
 //   warp 1  (one thread) issues tcgen05.mma (kind::f16, M = 128, N = 256,
 //           K = 16; BF16 operands from shared memory, FP32 accumulate) into
 //           one of two 256-column accumulators in tensor memory; each slice's
