@@ -225,11 +225,14 @@ struct e2d_batch {
     int block = 128, grid = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_ms = 0.0;
+    bool l2_held = false;  // counted among the users of the persisting L2 carve-out
 
     ~e2d_batch() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamSynchronize(stream);
+        release_l2(&l2_held);
         if (stream) cudaStreamDestroy(stream);
         if (ctl_dev) cudaFree(ctl_dev);
         if (ctl_host) cudaFreeHost(ctl_host);
@@ -250,7 +253,7 @@ int rebuild_graph(e2d_batch *b) {
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc) { if (g) cudaGraphDestroy(g); return rc; }
     if (e != cudaSuccess) { set_error(std::string("graph capture: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
-    keep_in_l2(g, b->impl->topo_ptr(), sizeof(int4) * (size_t)b->ntot);
+    keep_in_l2(g, b->impl->topo_ptr(), sizeof(int4) * (size_t)b->ntot, &b->l2_held);
     e = cudaGraphInstantiate(&b->gexec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) { b->gexec = nullptr; set_error(std::string("graph instantiate: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }

@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -111,8 +112,29 @@ bool freezes(const e2d_params &p) { return p.limiter_freeze > 0 || p.limiter_fre
 
 // The topology array (16 bytes per cell) is read by all four passes of every
 // stage; keeping it in L2 across them cut an iteration on 4.2M cells from 1.392
-// to 1.357 ms.  The persisting carve-out is a limit of this process's context.
-void keep_in_l2(cudaGraph_t g, const void *base, size_t bytes) {
+// to 1.357 ms.  The persisting carve-out is a limit of this process's context:
+// it is raised while a solver or batch that uses it exists, and when the last
+// one is destroyed its persisting lines are released and the limit put back
+// (otherwise later work in the process runs with less L2).
+namespace {
+std::mutex l2_mu;
+int l2_users = 0;
+bool l2_raised = false;
+size_t l2_prev = 0;
+}  // namespace
+
+void release_l2(bool *held) {
+    if (!held || !*held) return;
+    *held = false;
+    std::lock_guard<std::mutex> lk(l2_mu);
+    if (--l2_users > 0) return;
+    cudaCtxResetPersistingL2Cache();
+    if (l2_raised) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, l2_prev);
+    l2_raised = false;
+    cudaGetLastError();
+}
+
+void keep_in_l2(cudaGraph_t g, const void *base, size_t bytes, bool *held) {
     int dev = 0;
     cudaDeviceProp prop;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess ||
@@ -122,9 +144,21 @@ void keep_in_l2(cudaGraph_t g, const void *base, size_t bytes) {
     }
     const size_t win = std::min<size_t>(bytes, (size_t)prop.accessPolicyMaxWindowSize);
     const size_t keep = std::min<size_t>(win, (size_t)prop.persistingL2CacheMaxSize);
-    size_t cur = 0;
-    if (cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize) == cudaSuccess && cur < keep)
-        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, keep);
+    {
+        std::lock_guard<std::mutex> lk(l2_mu);
+        if (!*held) {
+            *held = true;
+            l2_users++;
+        }
+        size_t cur = 0;
+        if (cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize) == cudaSuccess && cur < keep) {
+            if (!l2_raised) {
+                l2_prev = cur;
+                l2_raised = true;
+            }
+            cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, keep);
+        }
+    }
     cudaKernelNodeAttrValue v = {};
     v.accessPolicyWindow.base_ptr = const_cast<void *>(base);
     v.accessPolicyWindow.num_bytes = win;
@@ -307,12 +341,15 @@ struct e2d_solver {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_ms = 0.0;
     std::vector<double> hist;  // host copy of Resd[1..step]
+    bool l2_held = false;      // counted among the users of the persisting L2 carve-out
 
     ~e2d_solver() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (gexec1) cudaGraphExecDestroy(gexec1);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        if (own_stream && stream) cudaStreamSynchronize(stream);
+        release_l2(&l2_held);
         if (own_stream && stream) cudaStreamDestroy(stream);
         if (ctl_dev) cudaFree(ctl_dev);
         if (ctl_host) cudaFreeHost(ctl_host);
@@ -371,7 +408,7 @@ int capture(e2d_solver *s, int iters, cudaGraphExec_t *out) {
     cudaError_t e = cudaStreamEndCapture(s->stream, &g);
     if (rc) { if (g) cudaGraphDestroy(g); return rc; }
     if (e != cudaSuccess) { set_error(std::string("graph capture: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }
-    keep_in_l2(g, s->impl->topo_ptr(), sizeof(int4) * (size_t)s->L.n);
+    keep_in_l2(g, s->impl->topo_ptr(), sizeof(int4) * (size_t)s->L.n, &s->l2_held);
     e = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) { *out = nullptr; set_error(std::string("graph instantiate: ") + cudaGetErrorString(e)); return E2D_ERR_CUDA; }

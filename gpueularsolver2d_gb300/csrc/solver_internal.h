@@ -47,7 +47,10 @@ const char *param_error(const e2d_params *p);
 
 // Marks [base, base + bytes) as persisting in L2 for every kernel node of a
 // captured graph (the cell topology, which all four passes read).
-void keep_in_l2(cudaGraph_t g, const void *base, size_t bytes);
+// L2 persistence of a graph's topology reads; *held marks the owner as a user
+// of the persisting carve-out until release_l2(held) (at its destruction).
+void keep_in_l2(cudaGraph_t g, const void *base, size_t bytes, bool *held);
+void release_l2(bool *held);
 
 // Device arena: one cudaMalloc carved into 256-byte aligned pieces.
 struct Arena {
