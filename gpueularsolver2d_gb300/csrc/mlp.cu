@@ -202,8 +202,10 @@ struct e2d_mlp {
     float *tb = nullptr, *y = nullptr, *dy = nullptr;
     std::vector<bf16 *> Gd, Hh;  // [nhidden] of [B][H]: gelu'(z) and gelu(z) of each hidden layer
     bf16 *dz[2] = {nullptr, nullptr};  // [B][H]
-    float *part = nullptr;      // weight-gradient partials (largest tensor x kSplits)
-    float *bpart = nullptr;     // bias-gradient partials
+    // weight- and bias-gradient partials, two sets: a layer's Adam step reads
+    // one on the side stream while the next layer's gradient fills the other
+    float *part[2] = {nullptr, nullptr};
+    float *bpart[2] = {nullptr, nullptr};
     double *loss_part = nullptr;
     int *step_dev = nullptr;
     int *flag_dev = nullptr;    // set by a tensor-core GEMM whose wait timed out
@@ -216,6 +218,8 @@ struct e2d_mlp {
     long long nsamples = 0, cap_samples = 0;
     std::vector<void *> allocs;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;  // Adam steps, overlapping the next layer's gradient
+    cudaEvent_t ev_fork = nullptr, ev_done[2] = {nullptr, nullptr};
     cudaGraphExec_t gexec = nullptr;
     // TMA tensor maps of the 256 x 256 GEMMs (ws::k_gemm_ws), per hidden layer
     // l >= 1: forward A = Hh[l-1], W_l; data gradient A = dz[0] / dz[1], W_l^T
@@ -225,7 +229,7 @@ struct e2d_mlp {
     std::vector<CUtensorMap> mapHo, mapGo;  // Hh[l], Gd[l] in 32 x 32 epilogue slabs
     // dz[0] / dz[1] with 128-row boxes (data gradient), 64-row boxes (weights), 32 x 32 slabs
     CUtensorMap mapDz[2], mapDzw[2], mapDzo[2];
-    CUtensorMap mapPart, mapPart0;  // weight-gradient partials: 256 x 256 layers, the first layer (256 x KX)
+    CUtensorMap mapPart[2], mapPart0[2];  // weight-gradient partials: 256 x 256 layers, the first layer (256 x KX)
     CUtensorMap mapX, mapXw, mapW0;   // the first layer's inputs (128- and 64-row boxes) and BF16 weights
     int wrows = ws::WROWS;  // batch rows per weight-gradient split
     std::vector<double> loss_host;
@@ -233,6 +237,10 @@ struct e2d_mlp {
     ~e2d_mlp() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (stream) cudaStreamDestroy(stream);
+        if (side) cudaStreamDestroy(side);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        for (cudaEvent_t e : ev_done)
+            if (e) cudaEventDestroy(e);
         for (void *p : allocs) cudaFree(p);
         if (X) cudaFree(X);
         if (T) cudaFree(T);
@@ -331,8 +339,10 @@ int build_ws_maps(e2d_mlp *m) {
         ok = ok && map_2d(&m->mapDzw[k], m->dz[k], m->B, H, ws::WCH);
         ok = ok && map_2d(&m->mapDzo[k], m->dz[k], m->B, H, 32, true);
     }
-    ok = ok && map_part(&m->mapPart, m->part, (uint64_t)(m->B / m->wrows) * H, H);
-    ok = ok && map_part(&m->mapPart0, m->part, (uint64_t)(m->B / m->wrows) * H, KX);
+    for (int k = 0; k < 2 && ok; k++) {
+        ok = ok && map_part(&m->mapPart[k], m->part[k], (uint64_t)(m->B / m->wrows) * H, H);
+        ok = ok && map_part(&m->mapPart0[k], m->part[k], (uint64_t)(m->B / m->wrows) * H, KX);
+    }
     ok = ok && map_2d(&m->mapX, m->xb, m->B, KX, ws::BM);
     ok = ok && map_2d(&m->mapXw, m->xb, m->B, KX, ws::WCH);
     ok = ok && map_2d(&m->mapW0, m->W[0].wbf, H, KX, ws::ND);
@@ -392,10 +402,12 @@ int ensure_batch(e2d_mlp *m, int B) {
     // CTAs at batch 65536, 20.7 us per layer against 26.9 us for 1024 rows,
     // with Adam summing twice the partials)
     const int nparts = std::max(kSplits, B / m->wrows);
-    if ((rc = m->alloc(&m->part, sizeof(float) * (size_t)nparts * H * H))) return rc;
+    for (int k = 0; k < 2; k++)
+        if ((rc = m->alloc(&m->part[k], sizeof(float) * (size_t)nparts * H * H))) return rc;
     // bias / output-layer partials: the same, or one per 256 rows for the output layer
-    if ((rc = m->alloc(&m->bpart, sizeof(float) * (size_t)std::max(nparts, B / 256) * (NOUT * H + NOUT + H))))
-        return rc;
+    for (int k = 0; k < 2; k++)
+        if ((rc = m->alloc(&m->bpart[k], sizeof(float) * (size_t)std::max(nparts, B / 256) * (NOUT * H + NOUT + H))))
+            return rc;
     if ((rc = m->alloc(&m->loss_part, sizeof(double) * (B / 256)))) return rc;
     return build_ws_maps(m);
 }
@@ -474,21 +486,37 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
         goff -= t.count();
         return m->grad + goff;
     };
+    // Each layer's Adam step runs on the side stream, forked after the
+    // layer's weight gradient, while the main stream goes on with the next
+    // layer (which needs neither the updated weights nor these partials);
+    // the partial sets alternate, and a set is only refilled after the Adam
+    // step that read it.  Both streams join at the end.
+    bool used[2] = {false, false};
+    auto claim = [&](int k) {
+        if (used[k]) cudaStreamWaitEvent(s, m->ev_done[k], 0);
+    };
+    auto fork_adam = [&](int k, const AdamSeg &w, const AdamSeg &bias) {
+        cudaEventRecord(m->ev_fork, s);
+        cudaStreamWaitEvent(m->side, m->ev_fork, 0);
+        adam2(m, m->side, w, bias, lr);
+        cudaEventRecord(m->ev_done[k], m->side);
+        used[k] = true;
+    };
     // output layer, forward and backward in one pass (loss, its weight / bias
     // partials, and the gradient at the last pre-activation: the output
     // layer's data gradient times the stored gelu'(z))
     Tensor &Wo = m->W[L], &bo = m->b[L];
     const int oparts = B / 256;
     k_out_train<H, NOUT><<<oparts, 256, 0, s>>>(B, m->Hh[L - 1], Wo.w32, bo.w32, m->tb, m->Gd[L - 1], m->y, m->dy,
-                                                m->dz[0], m->bpart, m->loss_part);
+                                                m->dz[0], m->bpart[0], m->loss_part);
     const size_t ostride = NOUT * H + NOUT;
     float *gbo = gslot(bo);
     float *gWo = gslot(Wo);
-    adam2(m, s, adam_seg(Wo, m->bpart, oparts, ostride, gWo), adam_seg(bo, m->bpart + NOUT * H, oparts, ostride, gbo),
-          lr);
+    fork_adam(0, adam_seg(Wo, m->bpart[0], oparts, ostride, gWo),
+              adam_seg(bo, m->bpart[0] + NOUT * H, oparts, ostride, gbo));
     int cur = 0;
     for (int l = L - 1; l >= 0; l--) {
-        const int kin = l == 0 ? NIN : H;
+        const int kin = l == 0 ? NIN : H, pk = (L - l) & 1;  // partial set of this layer
         // gradient at the previous pre-activation, first (it reads W_l before
         // this layer's Adam step changes it): dz W_l, W_l read MN-major
         // ([out][in] = [K][N]); then the weight gradient, whose partials the
@@ -505,6 +533,7 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
             gd.zin = m->Gd[l - 1]; gd.out = m->dz[cur ^ 1]; gd.ldc = H;
             gemm<false, true, EPI_GELU_BWD>(m, gd, dim3(H / BN, (B + BM - 1) / BM, 1), s);
         }
+        claim(pk);
         // dW_l = dz^T hin (split over the batch; both operands are read
         // MN-major, the batch index being their slow one), db_l = column sums
         // of dz
@@ -514,29 +543,31 @@ void backward(e2d_mlp *m, cudaStream_t s, const float *lr, bool want_grad) {
             wparts = B / m->wrows;
             if (l == 0) {
                 pld = KX;
-                ws::k_wgrad_ws<1><<<wparts, ws::WTHREADS, ws::WSMEM, s>>>(m->mapDzw[cur], m->mapXw, m->mapPart0, B,
-                                                                          m->wrows, m->bpart, m->flag_dev);
+                ws::k_wgrad_ws<1><<<wparts, ws::WTHREADS, ws::WSMEM, s>>>(m->mapDzw[cur], m->mapXw, m->mapPart0[pk],
+                                                                          B, m->wrows, m->bpart[pk], m->flag_dev);
             } else {
-                ws::k_wgrad_ws<4><<<wparts, ws::WTHREADS, ws::WSMEM, s>>>(m->mapDzw[cur], m->mapHw[l], m->mapPart, B,
-                                                                          m->wrows, m->bpart, m->flag_dev);
+                ws::k_wgrad_ws<4><<<wparts, ws::WTHREADS, ws::WSMEM, s>>>(m->mapDzw[cur], m->mapHw[l], m->mapPart[pk],
+                                                                          B, m->wrows, m->bpart[pk], m->flag_dev);
             }
         } else {
             GemmArgs gw{};
             gw.M = H; gw.N = kin; gw.K = B;
             gw.A = m->dz[cur]; gw.lda = H;
             gw.B = l == 0 ? m->xb : m->Hh[l - 1]; gw.ldb = l == 0 ? KX : H;
-            gw.part = m->part;
+            gw.part = m->part[pk];
             gemm<true, true, EPI_PARTIAL>(m, gw, dim3((kin + BN - 1) / BN, H / BM, kSplits), s);
             // (the warp-specialised weight-gradient kernel also writes the
             // bias gradient's partials, one per split)
-            k_colsum<<<dim3(H / 32, kSplits), 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart);
+            k_colsum<<<dim3(H / 32, kSplits), 256, 0, s>>>(B, H, rows, m->dz[cur], m->bpart[pk]);
         }
         float *gb = gslot(m->b[l]);
         float *gW = gslot(m->W[l]);
-        adam2(m, s, adam_seg(m->W[l], m->part, wparts, (size_t)H * pld, gW, pld),
-              adam_seg(m->b[l], m->bpart, wparts, H, gb), lr);
+        fork_adam(pk, adam_seg(m->W[l], m->part[pk], wparts, (size_t)H * pld, gW, pld),
+                  adam_seg(m->b[l], m->bpart[pk], wparts, H, gb));
         cur ^= 1;
     }
+    claim(0);
+    claim(1);
 }
 
 int build_train_graph(e2d_mlp *m) {
@@ -589,6 +620,9 @@ int e2d_mlp_create(const e2d_mlp_config *cfg, e2d_mlp **out) {
     m->cfg = *cfg;
     m->nhidden = cfg->nhidden;
     CK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
+    for (cudaEvent_t &e : m->ev_done) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     // He-style initialisation from a fixed-seed generator
     uint64_t st = cfg->seed * 0x9e3779b97f4a7c15ULL + 12345;
     auto rnd = [&]() {
